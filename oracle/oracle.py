@@ -1,0 +1,355 @@
+"""FP64 oracle for the vir projector / reconstruction hot path.
+
+TEST INFRASTRUCTURE ONLY.  Imported by tests/, ``__graft_entry__.smoke()`` and
+the CPU-baseline leg of ``bench.py`` as the checker; the ``vir_gb300`` package
+never imports it.
+
+The projectors are a C restatement (``vir_oracle.c``, built by ``build()`` into
+``oracle/_build/liboracle.so``) of the reference files cited there.  The ramp
+filter and the SIRT loop are restated here in numpy (float64):
+
+* ``ramp_filter`` / ``window_filter`` / ``filter_sino`` follow
+  ``filtration.py:4-112``, ``:115-235`` and ``:238-309``;
+* ``sirt`` follows ``sys_mat/sirt_dd.py:23-76`` (x0 = 1e-5, ``iters - 1``
+  updates, divisions guarded where the weight is zero).
+
+Trig tables follow the reference: the angle array is cast as the reference
+casts it (float32 for the distance-driven functions, ``dd.py:29-36``; as given
+for ``fp_2d_par.siddons_fp_2d``) and numpy's cos/sin of that dtype are passed to
+C as float64.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "liboracle.so")
+_lib = None
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_fp = ctypes.POINTER(ctypes.c_float)
+_ip = ctypes.POINTER(ctypes.c_int32)
+
+
+def build(force: bool = False) -> str:
+    """Compile vir_oracle.c (and, when the vir tree is present, the
+    reference's C into oracle/_ref) with the Makefile beside this file."""
+    if force or not os.path.exists(_LIB_PATH) or (
+        os.path.getmtime(_LIB_PATH) < os.path.getmtime(os.path.join(_HERE, "vir_oracle.c"))
+    ):
+        subprocess.check_call(["make", "-s", "-C", _HERE, "all"])
+    return _LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(_LIB_PATH)
+        L.orc_siddon_fp_2d.argtypes = [_fp, ctypes.c_int, ctypes.c_int, _dp, _dp, ctypes.c_int,
+                                       ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                       ctypes.c_int, _dp]
+        L.orc_siddon_bp_2d.argtypes = [_fp, ctypes.c_int, ctypes.c_int, _dp, _dp, ctypes.c_int,
+                                       ctypes.c_int, ctypes.c_double, ctypes.c_double, _dp]
+        L.orc_siddon_count_2d.argtypes = [ctypes.c_int, ctypes.c_int, _dp, _dp, ctypes.c_int,
+                                          ctypes.c_int, ctypes.c_double, ctypes.c_double]
+        L.orc_siddon_count_2d.restype = ctypes.c_longlong
+        L.orc_dd_fp_2d.argtypes = [ctypes.c_int, _fp, ctypes.c_int, ctypes.c_int, _dp, _dp,
+                                   ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                   ctypes.c_double, ctypes.c_double, ctypes.c_double, _dp]
+        L.orc_dd_bp_2d.argtypes = [ctypes.c_int, _fp, ctypes.c_int, ctypes.c_int, _dp, _dp,
+                                   ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                   ctypes.c_double, ctypes.c_double, ctypes.c_double, _dp]
+        L.orc_dd_fp_cone.argtypes = [_fp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp, _dp,
+                                     ctypes.c_int, ctypes.c_int, ctypes.c_int] + \
+            [ctypes.c_double] * 7 + [_dp]
+        L.orc_dd_bp_cone.argtypes = [_fp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp, _dp,
+                                     ctypes.c_int, ctypes.c_int, ctypes.c_int] + \
+            [ctypes.c_double] * 7 + [_dp]
+        L.orc_sf_fan_2d.argtypes = [ctypes.c_int, _fp, _dp, ctypes.c_int, ctypes.c_int, _dp, _dp,
+                                    ctypes.c_int, ctypes.c_int] + [ctypes.c_double] * 4
+        L.orc_sf_par_rect_2d.argtypes = [ctypes.c_int, _fp, _dp, ctypes.c_int, ctypes.c_int, _dp,
+                                         _dp, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                         ctypes.c_double]
+        L.orc_list_fp.argtypes = [_fp, _ip, _fp, _ip, ctypes.c_int, _dp]
+        L.orc_list_bp.argtypes = [_fp, _ip, _fp, _ip, ctypes.c_int, ctypes.c_int, _dp]
+        L.orc_num_threads.restype = ctypes.c_int
+        _lib = L
+    return _lib
+
+
+def num_threads() -> int:
+    return lib().orc_num_threads()
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def _ptr(a, t):
+    return a.ctypes.data_as(t)
+
+
+def trig(angles, dtype=None):
+    """cos/sin tables as the reference computes them (numpy, in the angle
+    array's own dtype, or in ``dtype`` when the reference casts first)."""
+    a = np.asarray(angles)
+    if dtype is not None:
+        a = a.astype(dtype)
+    a = np.atleast_1d(a)
+    return (np.ascontiguousarray(np.cos(a), dtype=np.float64),
+            np.ascontiguousarray(np.sin(a), dtype=np.float64))
+
+
+# --- Siddon 2D (sys_mat/fp_2d_par.py:11-64) -------------------------------
+
+def siddons_fp_2d(img, Angs, n_dets, d_det=1.0, d_pix=1.0, mode="fp64"):
+    """mode "fp64": FP64 accumulation.  mode "ref": float32-rounded
+    accumulation, bit-identical to the reference's output."""
+    img = _f32(img)
+    nx, ny = img.shape
+    c, s = trig(Angs)
+    out = np.zeros((c.size, n_dets), np.float64)
+    lib().orc_siddon_fp_2d(_ptr(img, _fp), nx, ny, _ptr(c, _dp), _ptr(s, _dp), c.size,
+                           int(n_dets), float(d_det), float(d_pix), 1 if mode == "ref" else 0,
+                           _ptr(out, _dp))
+    return out
+
+
+def siddons_bp_2d(sino, Angs, img_shape, d_det=1.0, d_pix=1.0):
+    sino = _f32(sino)
+    na, nd = sino.shape
+    c, s = trig(Angs)
+    out = np.zeros(img_shape, np.float64)
+    lib().orc_siddon_bp_2d(_ptr(sino, _fp), na, nd, _ptr(c, _dp), _ptr(s, _dp),
+                           int(img_shape[0]), int(img_shape[1]), float(d_det), float(d_pix),
+                           _ptr(out, _dp))
+    return out
+
+
+def siddons_count_2d(img_shape, Angs, n_dets, d_det=1.0, d_pix=1.0):
+    c, s = trig(Angs)
+    return int(lib().orc_siddon_count_2d(int(img_shape[0]), int(img_shape[1]), _ptr(c, _dp),
+                                         _ptr(s, _dp), c.size, int(n_dets), float(d_det),
+                                         float(d_pix)))
+
+
+# --- distance-driven (sys_mat/dd.py) ---------------------------------------
+
+def _dd_trig(ang_arr):
+    return trig(ang_arr, np.float32)
+
+
+def dd_fp_par_2d(img, ang_arr, nu, du=1.0, su=0.0, d_pix=1.0):
+    img = _f32(img)
+    c, s = _dd_trig(ang_arr)
+    out = np.zeros((c.size, nu), np.float64)
+    lib().orc_dd_fp_2d(0, _ptr(img, _fp), img.shape[0], img.shape[1], _ptr(c, _dp),
+                       _ptr(s, _dp), c.size, int(nu), float(np.float32(du)),
+                       float(np.float32(su)), float(np.float32(d_pix)), 0.0, 0.0, _ptr(out, _dp))
+    return out
+
+
+def dd_bp_par_2d(sino, ang_arr, img_shape, du=1.0, su=0.0, d_pix=1.0):
+    sino = _f32(sino)
+    c, s = _dd_trig(ang_arr)
+    out = np.zeros(img_shape, np.float64)
+    lib().orc_dd_bp_2d(0, _ptr(sino, _fp), sino.shape[0], sino.shape[1], _ptr(c, _dp),
+                       _ptr(s, _dp), int(img_shape[0]), int(img_shape[1]), float(np.float32(du)),
+                       float(np.float32(su)), float(np.float32(d_pix)), 0.0, 0.0, _ptr(out, _dp))
+    return out
+
+
+def dd_fp_fan_2d(img, ang_arr, nu, DSO, DSD, du=1.0, su=0.0, d_pix=1.0):
+    img = _f32(img)
+    c, s = _dd_trig(ang_arr)
+    out = np.zeros((c.size, nu), np.float64)
+    lib().orc_dd_fp_2d(1, _ptr(img, _fp), img.shape[0], img.shape[1], _ptr(c, _dp),
+                       _ptr(s, _dp), c.size, int(nu), float(np.float32(du)),
+                       float(np.float32(su)), float(np.float32(d_pix)), float(np.float32(DSO)),
+                       float(np.float32(DSD)), _ptr(out, _dp))
+    return out
+
+
+def dd_bp_fan_2d(sino, ang_arr, img_shape, DSO, DSD, du=1.0, su=0.0, d_pix=1.0):
+    sino = _f32(sino)
+    c, s = _dd_trig(ang_arr)
+    out = np.zeros(img_shape, np.float64)
+    lib().orc_dd_bp_2d(1, _ptr(sino, _fp), sino.shape[0], sino.shape[1], _ptr(c, _dp),
+                       _ptr(s, _dp), int(img_shape[0]), int(img_shape[1]), float(np.float32(du)),
+                       float(np.float32(su)), float(np.float32(d_pix)), float(np.float32(DSO)),
+                       float(np.float32(DSD)), _ptr(out, _dp))
+    return out
+
+
+def dd_fp_cone_3d(img, ang_arr, nu, nv, DSO, DSD, du=1.0, dv=1.0, su=0.0, sv=1.0, d_pix=1.0):
+    img = _f32(img)
+    c, s = _dd_trig(ang_arr)
+    out = np.zeros((c.size, nu, nv), np.float64)
+    f = lambda v: float(np.float32(v))
+    lib().orc_dd_fp_cone(_ptr(img, _fp), *img.shape, _ptr(c, _dp), _ptr(s, _dp), c.size,
+                         int(nu), int(nv), f(du), f(dv), f(su), f(sv), f(d_pix), f(DSO), f(DSD),
+                         _ptr(out, _dp))
+    return out
+
+
+def dd_bp_cone_3d(sino, ang_arr, img_shape, DSO, DSD, du=1.0, dv=1.0, su=0.0, sv=0.0, d_pix=1.0):
+    sino = _f32(sino)
+    c, s = _dd_trig(ang_arr)
+    out = np.zeros(img_shape, np.float64)
+    f = lambda v: float(np.float32(v))
+    lib().orc_dd_bp_cone(_ptr(sino, _fp), *sino.shape, _ptr(c, _dp), _ptr(s, _dp),
+                         *[int(v) for v in img_shape], f(du), f(dv), f(su), f(sv), f(d_pix),
+                         f(DSO), f(DSD), _ptr(out, _dp))
+    return out
+
+
+# --- separable footprint (sys_mat/sp.py:12-87, fp_2d_par.py:67-125) -------
+
+def sf_fp_fan_2d(img, angs, nu, DSO, DSD, du=1.0, d_pix=1.0):
+    img = _f32(img)
+    c, s = trig(angs)
+    out = np.zeros((c.size, nu), np.float64)
+    lib().orc_sf_fan_2d(0, _ptr(img, _fp), _ptr(out, _dp), img.shape[0], img.shape[1],
+                        _ptr(c, _dp), _ptr(s, _dp), c.size, int(nu), float(DSO), float(DSD),
+                        float(du), float(d_pix))
+    return out
+
+
+def sf_bp_fan_2d(sino, angs, img_shape, DSO, DSD, du=1.0, d_pix=1.0):
+    sino = _f32(sino)
+    c, s = trig(angs)
+    out = np.zeros(img_shape, np.float64)
+    lib().orc_sf_fan_2d(1, _ptr(sino, _fp), _ptr(out, _dp), int(img_shape[0]),
+                        int(img_shape[1]), _ptr(c, _dp), _ptr(s, _dp), c.size, sino.shape[1],
+                        float(DSO), float(DSD), float(du), float(d_pix))
+    return out
+
+
+def separable_footprint_fp_2d(img, Angs, n_dets, d_det=1.0, d_pix=1.0):
+    img = _f32(img)
+    c, s = trig(Angs)
+    out = np.zeros((c.size, n_dets), np.float64)
+    lib().orc_sf_par_rect_2d(0, _ptr(img, _fp), _ptr(out, _dp), img.shape[0], img.shape[1],
+                             _ptr(c, _dp), _ptr(s, _dp), c.size, int(n_dets), float(d_det),
+                             float(d_pix))
+    return out
+
+
+def separable_footprint_bp_2d(sino, Angs, img_shape, d_det=1.0, d_pix=1.0):
+    sino = _f32(sino)
+    c, s = trig(Angs)
+    out = np.zeros(img_shape, np.float64)
+    lib().orc_sf_par_rect_2d(1, _ptr(sino, _fp), _ptr(out, _dp), int(img_shape[0]),
+                             int(img_shape[1]), _ptr(c, _dp), _ptr(s, _dp), c.size,
+                             sino.shape[1], float(d_det), float(d_pix))
+    return out
+
+
+# --- list projection (projection/projection_c.c:126-219) -------------------
+
+def list_fp(x, ind, length, off):
+    x = _f32(x).ravel()
+    ind = np.ascontiguousarray(ind, np.int32)
+    length = _f32(length)
+    off = np.ascontiguousarray(off, np.int32)
+    out = np.zeros(off.size - 1, np.float64)
+    lib().orc_list_fp(_ptr(x, _fp), _ptr(ind, _ip), _ptr(length, _fp), _ptr(off, _ip),
+                      off.size - 1, _ptr(out, _dp))
+    return out
+
+
+def list_bp(sino, ind, length, off, nvox):
+    sino = _f32(sino).ravel()
+    ind = np.ascontiguousarray(ind, np.int32)
+    length = _f32(length)
+    off = np.ascontiguousarray(off, np.int32)
+    out = np.zeros(int(nvox), np.float64)
+    lib().orc_list_bp(_ptr(sino, _fp), _ptr(ind, _ip), _ptr(length, _fp), _ptr(off, _ip),
+                      off.size - 1, int(nvox), _ptr(out, _dp))
+    return out
+
+
+# --- ramp filter (filtration.py) -------------------------------------------
+
+def ramp_filter(nu, du=1.0, cutoff=0.5, real_space=True):
+    """Half-spectrum ramp filter and its frequencies (filtration.py:4-112)
+    with zero padding to the next power of two >= 2*nu."""
+    nfu = int(2 ** np.ceil(np.log2(2 * nu)))
+    f = np.fft.rfftfreq(nfu, d=du)
+    if real_space:
+        k = np.fft.fftfreq(nfu, d=1.0 / nfu)
+        h = np.zeros(nfu)
+        h[0] = 1.0 / (4.0 * du ** 2)
+        h[1::2] = -1.0 / (np.pi ** 2 * du ** 2 * k[1::2] ** 2)
+        H = du * np.real(np.fft.rfft(h))
+    else:
+        H = np.abs(f)
+    H[np.abs(f) > cutoff * (1.0 / du)] = 0.0
+    return H, f
+
+
+def window_filter(H, f, du=1.0, filter_type="ramp", cutoff=0.5, sigma=0.5):
+    """filtration.py:115-235."""
+    f_c = cutoff * (1.0 / du)
+    fn = f / f_c
+    valid = np.abs(f) <= f_c
+    W = np.zeros_like(f)
+    if filter_type in ("ram-lak", "ramp"):
+        return H
+    if filter_type == "hann":
+        W[valid] = 0.5 + 0.5 * np.cos(np.pi * fn[valid])
+    elif filter_type == "hamming":
+        W[valid] = 0.54 + 0.46 * np.cos(np.pi * fn[valid])
+    elif filter_type == "blackman":
+        W[valid] = 0.42 + 0.5 * np.cos(np.pi * fn[valid]) + 0.08 * np.cos(2 * np.pi * fn[valid])
+    elif filter_type == "shepp-logan":
+        W[0] = 1.0
+        m = valid & (f != 0)
+        W[m] = np.sin(np.pi * f[m] / (2 * f_c)) / (np.pi * f[m] / (2 * f_c))
+    elif filter_type == "cosine":
+        W[valid] = np.cos(np.pi * fn[valid] / 2.0)
+    elif filter_type == "gaussian":
+        W = np.exp(-0.5 * (f / sigma) ** 2)
+    else:
+        raise ValueError(f"Unknown filter type: {filter_type}")
+    return H * W
+
+
+def filter_sino(sino, du=1.0, filter_type="ramp", cutoff=0.5, real_space=True):
+    """filtration.py:238-309: rFFT along the last axis at the padded length,
+    multiplied by 2H, inverse, cropped to nu."""
+    if filter_type is None:
+        return sino
+    nu = sino.shape[-1]
+    z = int(2 ** np.ceil(np.log2(2 * nu)))
+    H, f = ramp_filter(nu, du=du, cutoff=cutoff, real_space=real_space)
+    H = window_filter(H, f, du=du, filter_type=filter_type, cutoff=cutoff)
+    F = np.fft.rfft(np.asarray(sino, np.float64), axis=-1, n=z)
+    F *= 2.0 * H
+    return np.fft.irfft(F, n=z, axis=-1)[..., :nu]
+
+
+# --- SIRT (sys_mat/sirt_dd.py:23-76) ---------------------------------------
+
+def sirt(sino, fp, bp, img_shape, gamma=1.0, iters=100, x0=1e-5, W_sino=None, W_img=None):
+    """x <- x + gamma * (BP((y - FP x) / W_sino)) / W_img with W_sino = FP 1
+    and W_img = BP 1, run for ``iters - 1`` updates as ``range(1, iters)``
+    does.  ``fp``/``bp`` are FP64 projector callables of this module."""
+    sino = np.asarray(sino, np.float64)
+    if W_sino is None:
+        W_sino = fp(np.ones(img_shape, np.float32))
+    if W_img is None:
+        W_img = bp(np.ones(sino.shape, np.float32))
+    x = np.zeros(img_shape, np.float64) + x0
+    for _ in range(1, iters):
+        est = fp(x.astype(np.float32))
+        r = np.where(W_sino != 0.0, (sino - est) / np.where(W_sino != 0.0, W_sino, 1.0), est)
+        upd = bp(r.astype(np.float32))
+        upd = np.where(W_img != 0.0, upd / np.where(W_img != 0.0, W_img, 1.0), upd)
+        x = x + gamma * upd
+    return x

@@ -1,0 +1,276 @@
+"""Generates the golden fixtures in this directory by running the reference
+(vargasp/vir) itself, imported from its source tree.
+
+Run in a container that holds the vir tree (default ``/root/reference``):
+
+    python tests/golden/make_golden.py [--ref /path/to/vir]
+
+The reference is imported through two shims and nothing else: a ``vir``
+symlink to the tree on ``sys.path`` (every module imports ``vir.*``) and an
+``llvmlite.binding`` stub (``sys_mat/dd.py:11-12`` imports it unconditionally).
+numba is absent here, so the reference's ``@njit`` functions run as plain
+Python through its own fallbacks.  Three modules cannot be imported as modules
+(``sys_mat/sp.py`` runs a 128^3 projection at import, ``sirt_dd.py`` and
+``sirt_numba.py`` import numba unguarded); for those the named functions' own
+source is taken from the file and executed without the module body.
+
+The C list projector is the reference's ``projection/projection_c.c``,
+compiled from its source by ``oracle/Makefile`` into ``oracle/_ref``.
+
+Each fixture stores its inputs and the reference's outputs (float32 as the
+reference returns them).  Nothing here is used at run time on a GPU machine:
+the tests read only the ``.npz`` files.
+"""
+from __future__ import annotations
+
+import argparse
+import ast
+import ctypes
+import os
+import sys
+import tempfile
+import types
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+
+
+def import_reference(ref_root):
+    d = tempfile.mkdtemp(prefix="virref_")
+    os.symlink(ref_root, os.path.join(d, "vir"))
+    sys.path.insert(0, d)
+    llvm = types.ModuleType("llvmlite")
+    binding = types.ModuleType("llvmlite.binding")
+    binding.set_option = lambda *a, **k: None
+    llvm.binding = binding
+    sys.modules.setdefault("llvmlite", llvm)
+    sys.modules.setdefault("llvmlite.binding", binding)
+    import vir  # noqa: F401
+    return d
+
+
+def function_from_source(path, names, extra_globals=None):
+    """Executes only the named top-level functions of a reference file."""
+    src = open(path).read()
+    tree = ast.parse(src)
+    keep = [n for n in tree.body if isinstance(n, ast.FunctionDef) and n.name in names]
+    mod = ast.Module(body=keep, type_ignores=[])
+    g = {"np": np}
+
+    def njit(*a, **k):
+        if a and callable(a[0]):
+            return a[0]
+        return lambda f: f
+
+    g["njit"] = njit
+    g["prange"] = range
+    if extra_globals:
+        g.update(extra_globals)
+    exec(compile(mod, path, "exec"), g)
+    return {n: g[n] for n in names}
+
+
+def ellipse_image(n, n_ell, seed, vmax=0.02):
+    """Seeded random-ellipse image (x-major, img[ix, iy]) used as fixture input."""
+    rng = np.random.default_rng(seed)
+    c = np.arange(n) - n / 2 + 0.5
+    X, Y = np.meshgrid(c, c, indexing="ij")
+    img = np.zeros((n, n), np.float64)
+    for _ in range(n_ell):
+        r = n / 2 * 0.9
+        cx, cy = rng.uniform(-r / 2, r / 2, 2)
+        a, b = rng.uniform(0.1 * r, 0.5 * r, 2)
+        th = rng.uniform(0, np.pi)
+        xr = (X - cx) * np.cos(th) + (Y - cy) * np.sin(th)
+        yr = -(X - cx) * np.sin(th) + (Y - cy) * np.cos(th)
+        img[(xr / a) ** 2 + (yr / b) ** 2 <= 1] += rng.uniform(0, vmax)
+    return img.astype(np.float32)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default="/root/reference")
+    args = ap.parse_args()
+    ref = args.ref
+    import_reference(ref)
+    import vir.sys_mat.dd as dd
+    import vir.sys_mat.fp_2d_par as fp2
+    import vir.sys_mat.siddon as sd
+    import vir.filtration as filt
+    import vir.proj_geom as pg
+    out = {}
+
+    # --- Siddon 2D parallel (fp_2d_par.siddons_fp_2d) ---------------------
+    img = ellipse_image(32, 6, 11, vmax=1.0)
+    angs = np.linspace(0, np.pi, 24, endpoint=False)  # includes 0, 45, 90 deg
+    out["siddon2d_a"] = dict(img=img, angs=angs, n_dets=np.int32(47), d_det=1.0, d_pix=1.0,
+                             sino=fp2.siddons_fp_2d(img, angs, 47, 1.0, 1.0))
+    img2 = ellipse_image(24, 4, 12, vmax=1.0)[:, :20].copy()
+    angs2 = np.linspace(0, 2 * np.pi, 17, endpoint=False)
+    out["siddon2d_b"] = dict(img=img2, angs=angs2, n_dets=np.int32(40), d_det=0.7, d_pix=1.3,
+                             sino=fp2.siddons_fp_2d(img2, angs2, 40, 0.7, 1.3))
+
+    # --- separable footprint, parallel rectangle (fp_2d_par) ---------------
+    out["sf_par_rect"] = dict(img=img, angs=angs[:12], n_dets=np.int32(47), d_det=1.0,
+                              d_pix=1.0,
+                              sino=fp2.separable_footprint_fp_2d(img, angs[:12], 47, 1.0, 1.0))
+
+    # --- distance-driven 2D ---------------------------------------------------
+    img3 = ellipse_image(32, 6, 13, vmax=1.0)
+    a_par = np.linspace(0, np.pi, 24, endpoint=False).astype(np.float32)
+    for tag, (nu, du, su, dp) in {"a": (48, 1.0, 0.0, 1.0), "b": (40, 0.8, 0.25, 0.9)}.items():
+        sino = dd.dd_fp_par_2d(img3, a_par, nu, du=du, su=su, d_pix=dp)
+        y = np.random.default_rng(20).random((a_par.size, nu)).astype(np.float32)
+        bp = dd.dd_bp_par_2d(y, a_par, img3.shape, du=du, su=su, d_pix=dp)
+        out[f"dd_par_{tag}"] = dict(img=img3, angs=a_par, nu=np.int32(nu), du=du, su=su,
+                                    d_pix=dp, sino=sino, y=y, bp=bp)
+    a_fan = np.linspace(0, 2 * np.pi, 24, endpoint=False).astype(np.float32)
+    for tag, (nu, du, su, dp, DSO, DSD) in {"a": (64, 1.2, 0.0, 0.9, 60.0, 120.0),
+                                             "b": (50, 1.0, 0.5, 1.0, 50.0, 90.0)}.items():
+        sino = dd.dd_fp_fan_2d(img3, a_fan, nu, DSO, DSD, du=du, su=su, d_pix=dp)
+        y = np.random.default_rng(21).random((a_fan.size, nu)).astype(np.float32)
+        bp = dd.dd_bp_fan_2d(y, a_fan, img3.shape, DSO, DSD, du=du, su=su, d_pix=dp)
+        out[f"dd_fan_{tag}"] = dict(img=img3, angs=a_fan, nu=np.int32(nu), du=du, su=su,
+                                    d_pix=dp, DSO=DSO, DSD=DSD, sino=sino, y=y, bp=bp)
+
+    # --- distance-driven cone --------------------------------------------------
+    rng = np.random.default_rng(14)
+    vol = rng.random((10, 10, 10)).astype(np.float32)  # dd.py:289,388 unpack (nP, nz, no): cubes only
+    a_cone = np.linspace(0, 2 * np.pi, 8, endpoint=False).astype(np.float32)
+    cone = dict(nu=24, nv=20, DSO=40.0, DSD=80.0, du=1.5, dv=1.4, su=0.25, sv=-0.5, d_pix=1.0)
+    kw = {k: cone[k] for k in ("du", "dv", "su", "sv", "d_pix")}
+    sino_bug = dd.dd_fp_cone_3d(vol, a_cone, cone["nu"], cone["nv"], cone["DSO"], cone["DSD"], **kw)
+    # the same sweep with tmp_u cleared for every (io, iz)
+    fixed_src = open(os.path.join(ref, "sys_mat", "dd.py")).read()
+    s0 = fixed_src.index("def _dd_fp_cone_sweep")
+    s1 = fixed_src.index("@njit", s0)
+    body = fixed_src[s0:s1].replace("tmp_u[iu_min:iu_max] = 0.0", "tmp_u[:] = 0.0")
+    assert "tmp_u[:] = 0.0" in body
+    ns = {"np": np}
+    exec(body, ns)
+    orig = dd._dd_fp_cone_sweep
+    dd._dd_fp_cone_sweep = ns["_dd_fp_cone_sweep"]
+    try:
+        sino_fix = dd.dd_fp_cone_3d(vol, a_cone, cone["nu"], cone["nv"], cone["DSO"], cone["DSD"], **kw)
+    finally:
+        dd._dd_fp_cone_sweep = orig
+    yc = np.random.default_rng(22).random(sino_fix.shape).astype(np.float32)
+    bpc = dd.dd_bp_cone_3d(yc, a_cone, vol.shape, cone["DSO"], cone["DSD"], **kw)
+    out["dd_cone"] = dict(vol=vol, angs=a_cone, sino_ref=sino_bug, sino_fixed=sino_fix, y=yc,
+                          bp=bpc, **{k: (np.int32(v) if isinstance(v, int) else v)
+                                     for k, v in cone.items()})
+
+    # --- separable footprint fan (sp.sf_fp_fan_2d; sp.py not importable) ----
+    fns = function_from_source(os.path.join(ref, "sys_mat", "sp.py"), ["sf_fp_fan_2d"])
+    img4 = ellipse_image(24, 5, 15, vmax=1.0)
+    a_sf = np.linspace(0, 2 * np.pi, 10, endpoint=False)
+    out["sf_fan"] = dict(img=img4, angs=a_sf, nu=np.int32(40), DSO=50.0, DSD=100.0, du=1.3,
+                         d_pix=1.0,
+                         sino=fns["sf_fp_fan_2d"](img4, a_sf, 40, 50.0, 100.0, du=1.3, d_pix=1.0))
+
+    # --- ramp filter (filtration.filter_sino) -----------------------------------
+    rs = np.random.default_rng(16).random((5, 37))
+    for ft in ("ramp", "hann", "hamming", "blackman", "shepp-logan", "cosine", "gaussian"):
+        for rsp in (True, False):
+            for cut in (0.5, 0.4):
+                key = f"filter_{ft}_{int(rsp)}_{int(cut * 10)}"
+                out[key] = dict(sino=rs, du=1.3, cutoff=cut, real_space=rsp,
+                                filter_type=np.array(ft),
+                                filtered=filt.filter_sino(rs, du=1.3, filter_type=ft, cutoff=cut,
+                                                          real_space=rsp))
+
+    # --- Siddon 3D lists (siddon.siddons) -----------------------------------------
+    # edge cases of tests/Test_Siddons/siddons_test1.py:20-80 on a 4x4x1 grid
+    edge = [([-2.1, .25, .25], [2.0, .25, .25]), ([-2.0, .25, .25], [2.0, .25, .25]),
+            ([-1.9, .25, .25], [2.0, .25, .25]), ([-2.0, .25, .25], [1.9, .25, .25]),
+            ([-2.0, .25, .25], [2.1, .25, .25]), ([2.1, .25, .25], [-2.0, .25, .25]),
+            ([2.0, .25, .25], [-2.0, .25, .25]), ([1.9, .25, .25], [-2.0, .25, .25]),
+            ([2.0, .25, .25], [-1.9, .25, .25]), ([2.0, .25, .25], [-2.1, .25, .25]),
+            ([.25, 4.0, .25], [.25, 4.0, .25]), ([-4.0, .25, .25], [-4.0, .25, .25]),
+            ([2.0, -2.0, 0.0], [-2.0, -2.0, 0.0]), ([2.0, -1.0, 0.0], [-2.0, -1.0, 0.0]),
+            ([2.0, 0.0, 0.0], [-2.0, 0.0, 0.0])]
+    srcs = np.array([e[0] for e in edge], np.float32)
+    trgs = np.array([e[1] for e in edge], np.float32)
+    ind, ln, off = sd.siddons(srcs, trgs, (4, 4, 1), 1.0, flat=True)
+    out["siddons_edge"] = dict(src=srcs, trg=trgs, nPixels=np.array([4, 4, 1], np.int32),
+                               dPixels=np.array([1.0, 1.0, 1.0]), ind=ind, len=ln, off=off)
+    # a circular parallel geometry (proj_geom.geom_circular) on a 16x16x1 grid
+    dets = (np.arange(23) - 11).astype(np.float64) * 0.9
+    views = np.linspace(0, np.pi, 12, endpoint=False)
+    src, trg = pg.geom_circular(dets, views, geom="par")
+    ind, ln, off = sd.siddons(src, trg, (16, 16, 1), 1.0, flat=True)
+    out["siddons_par"] = dict(src=src.astype(np.float32), trg=trg.astype(np.float32),
+                              nPixels=np.array([16, 16, 1], np.int32),
+                              dPixels=np.array([1.0, 1.0, 1.0]), ind=ind, len=ln, off=off)
+    # a fan geometry in 3D (cone with one z row offset) on a 12x10x6 grid
+    dets = (np.arange(15) - 7).astype(np.float64) * 1.1
+    dz = (np.arange(5) - 2).astype(np.float64) * 1.2
+    views = np.linspace(0, 2 * np.pi, 7, endpoint=False)
+    src, trg = pg.geom_circular(dets, views, geom="cone", src_iso=30.0, det_iso=20.0, DetsZ=dz)
+    ind, ln, off = sd.siddons(src, trg, (12, 10, 6), (1.0, 0.8, 1.2), flat=True)
+    out["siddons_cone"] = dict(src=src.astype(np.float32), trg=trg.astype(np.float32),
+                               nPixels=np.array([12, 10, 6], np.int32),
+                               dPixels=np.array([1.0, 0.8, 1.2]), ind=ind, len=ln, off=off)
+
+    # --- the reference C list projector (projection_c.c via its own ctypes) ----
+    ref_so = os.path.join(REPO, "oracle", "_ref", "projection.so")
+    if os.path.exists(ref_so):
+        import vir.mpct as mpct
+        so = ctypes.CDLL(ref_so)
+        d = out["siddons_cone"]
+        nvox = int(np.prod(d["nPixels"]))
+        phantom = np.random.default_rng(17).random(tuple(d["nPixels"])).astype(np.float32)
+        nr = d["off"].size - 1
+        rays = (mpct.RaveledRay * nr)()
+        keep = []
+        for r in range(nr):
+            a, b = d["off"][r], d["off"][r + 1]
+            R = np.ascontiguousarray(d["ind"][a:b], np.int32)
+            L = np.ascontiguousarray(d["len"][a:b], np.float32)
+            keep += [R, L]
+            rays[r].n = int(b - a)
+            rays[r].R = R.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+            rays[r].L = L.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+        sino = np.zeros(nr, np.float32)
+        so.forward_proj_ravel_rays_struct(phantom.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                                          sino.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                                          rays, ctypes.c_int(nr))
+        y = np.random.default_rng(18).random(nr).astype(np.float32)
+        bp = np.zeros(nvox, np.float32)
+        so.back_proj_ravel_rays_struct(bp.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                                       y.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                                       rays, ctypes.c_int(nr))
+        out["list_c"] = dict(phantom=phantom, sino=sino, y=y, bp=bp.reshape(phantom.shape))
+
+    # --- SIRT update rule (sirt_dd.py:23-76) around the reference DD projectors --
+    fns = function_from_source(os.path.join(ref, "sys_mat", "sirt_dd.py"),
+                               ["fast_divide1", "fast_divide2"])
+    img5 = ellipse_image(24, 4, 19, vmax=0.02)
+    a5 = np.linspace(0, np.pi, 30, endpoint=False).astype(np.float32)
+    y5 = dd.dd_fp_par_2d(img5, a5, 36, du=1.0, d_pix=1.0)
+    W_sino = dd.dd_fp_par_2d(np.ones_like(img5), a5, 36, du=1.0, d_pix=1.0)
+    W_img = dd.dd_bp_par_2d(np.ones_like(y5), a5, img5.shape, du=1.0, d_pix=1.0)
+    x = np.zeros(img5.shape, np.float32) + .00001
+    iters = 6
+    for _ in range(1, iters):
+        est = dd.dd_fp_par_2d(x, a5, 36, du=1.0, d_pix=1.0)
+        fns["fast_divide1"](y5, est, W_sino)
+        upd = dd.dd_bp_par_2d(est, a5, img5.shape, du=1.0, d_pix=1.0)
+        fns["fast_divide2"](upd, W_img)
+        x = x + 1.0 * upd
+    out["sirt_par"] = dict(img=img5, angs=a5, nu=np.int32(36), sino=y5, W_sino=W_sino,
+                           W_img=W_img, iters=np.int32(iters), gamma=1.0, x=x)
+
+    path = os.path.join(HERE, "golden.npz")
+    flat = {}
+    for k, d in out.items():
+        for kk, v in d.items():
+            flat[f"{k}/{kk}"] = np.asarray(v)
+    np.savez_compressed(path, **flat)
+    print("wrote", path, os.path.getsize(path), "bytes,", len(out), "cases")
+
+
+if __name__ == "__main__":
+    main()
