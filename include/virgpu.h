@@ -1,0 +1,142 @@
+/*
+ * virgpu.h -- C ABI of libvirgpu.so, the GB300 (sm_103a) projector /
+ * backprojector / reconstruction library behind vir_gb300.
+ *
+ * Conventions shared by every entry point:
+ *  - All array arguments are DEVICE pointers (cudaMalloc'd or torch CUDA
+ *    storage), C-contiguous, float32 unless stated.  Images are (nx, ny)
+ *    x-major (img[ix*ny + iy]) as in vir; volumes (nx, ny, nz); sinograms
+ *    (na, nu) or (na, nu, nv) with v fastest (vir's dd.py layout).
+ *  - `trig` is a device array of 2*na doubles (cos0, sin0, cos1, sin1, ...):
+ *    the per-view trig table, computed by the caller exactly as vir does
+ *    (numpy cos/sin in the reference's own angle dtype, widened to double).
+ *  - `stream` is a cudaStream_t passed as void* (NULL = legacy default).
+ *    Calls are asynchronous and reentrant per stream; outputs are
+ *    overwritten, never accumulated, unless a flag says otherwise.
+ *  - Every entry point returns an int status (VG_OK = 0) and never aborts;
+ *    vg_last_error() returns a message for the calling thread's last failure.
+ *
+ * Each declaration names the vir interface it replaces (file:line inside the
+ * vargasp/vir tree).
+ */
+#ifndef VIRGPU_H
+#define VIRGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    VG_OK = 0,
+    VG_ERR_ARG = 1,       /* bad size, null pointer, misaligned buffer */
+    VG_ERR_LAUNCH = 2,    /* kernel launch failed */
+    VG_ERR_TIMEOUT = 3,   /* a bounded device wait gave up */
+    VG_ERR_CANCELLED = 4, /* the host raised the cancel flag */
+    VG_ERR_CUDA = 5       /* another CUDA runtime error */
+};
+
+/* Library identity and diagnostics. */
+int vg_version(void);
+const char *vg_last_error(void);
+const char *vg_status_string(int status);
+
+/* ---- 2D parallel-beam Siddon ------------------------------------------- */
+
+/* Forward projection along exact ray paths, one thread per ray, FP64
+ * geometry (plane crossings merged in FP64 exactly as vir orders them) and
+ * Kahan-compensated FP32 sums.  img (nx, ny) -> sino (na, n_dets).
+ * Replaces fp_2d_par.siddons_fp_2d (sys_mat/fp_2d_par.py:11-64). */
+int vg_siddon2d_fp(const float *img, int nx, int ny, const double *trig, int na,
+                   int n_dets, double d_det, double d_pix, float *sino,
+                   void *stream);
+
+/* Exact adjoint of vg_siddon2d_fp in gather form (one thread per pixel, the
+ * same FP64 segments recomputed per candidate ray; no atomics).
+ * sino (na, n_dets) -> img (nx, ny).  Replaces the list backprojector
+ * back_proj_ravel_rays_struct (projection/projection_c.c:200-208) for the
+ * same geometry, without a stored list. */
+int vg_siddon2d_bp(const float *sino, int na, int n_dets, const double *trig,
+                   int nx, int ny, double d_det, double d_pix, float *img,
+                   void *stream);
+
+/* Per-ray trace of vg_siddon2d_fp's path (no image): segment count, an
+ * order-sensitive 64-bit hash of the voxel indices (h = (h ^ (idx + C1)) *
+ * C2, FNV-style, h0 = 0xCBF29CE484222325) and the FP64 sum of lengths, for
+ * checking voxel index sequences ray by ray against an FP64 restatement of
+ * fp_2d_par.py:22-63.  Arrays are (na, n_dets). */
+int vg_siddon2d_trace(int nx, int ny, const double *trig, int na, int n_dets,
+                      double d_det, double d_pix, int *count,
+                      unsigned long long *hash, double *len, void *stream);
+
+/* ---- 2D distance-driven (parallel and flat-detector fan) --------------- */
+
+/* Geometry of one 2D distance-driven call.  fan = 0: parallel
+ * (dd.py:472-523); fan = 1: fan beam with source at distance DSO from the
+ * isocentre and a flat detector at DSD (dd.py:527-585). */
+typedef struct {
+    int nx, ny;      /* image */
+    int na, nu;      /* views, detector bins */
+    float du, su;    /* bin width, detector shift in bins (dd.py:699) */
+    float d_pix;     /* pixel width */
+    float DSO, DSD;  /* fan only */
+    int fan;
+} vg_dd2d_geom;
+
+/* Forward projection, gather form (one thread per bin, pixels of each
+ * orthogonal line found directly), returns A x * d_pix / du exactly as
+ * dd_fp_par_2d / dd_fp_fan_2d (dd.py:651-661, 725; 730-736, 803).
+ * img is (nx, ny); imgT is its transpose (ny, nx) (the caller keeps both so
+ * that both driving axes read contiguous lines); sino (na, nu). */
+int vg_dd2d_fp(const vg_dd2d_geom *g, const float *img, const float *imgT,
+               const double *trig, float *sino, void *stream);
+
+/* Backprojection, gather form (one thread per pixel over all views, no
+ * atomics), returns A^T y / (na d_pix) exactly as dd_bp_par_2d /
+ * dd_bp_fan_2d (dd.py:666-672, 721-723; 739-745, 799-801). */
+int vg_dd2d_bp(const vg_dd2d_geom *g, const float *sino, const double *trig,
+               float *img, void *stream);
+
+/* One SIRT update on the same projector pair, both halves fused
+ * (sys_mat/sirt_dd.py:51-72):
+ *   r   = (y - FP x) * inv_w_sino  (FP x kept where inv_w_sino == 0)
+ *   x  += gamma * (BP r) * inv_w_img (BP r kept where inv_w_img == 0)
+ * inv_w_* hold 1/W (0 where W == 0).  r is a caller scratch sinogram; x and
+ * xT (its transpose) are updated in place. */
+int vg_dd2d_sirt_iter(const vg_dd2d_geom *g, const float *y,
+                      const float *inv_w_sino, const float *inv_w_img,
+                      float gamma, const double *trig, float *x, float *xT,
+                      float *r, void *stream);
+
+/* Pixel-driven FBP backprojection of a ramp-filtered sinogram q (na, nu)
+ * (filtered by vg_filter_rows, i.e. filtration.filter_sino's 2H):
+ *   img(x, y) = pi / (2 na) * sum_views q(s(x, y)) / U(x, y)^2,
+ * linear interpolation between bin centres; parallel s = -sin x + cos y,
+ * U = 1; fan (flat detector) s = DSD p / (DSO - o), U = (DSO - o) / DSO.
+ * The fan weights follow processing/reconstruction.py:99-107 (equispaced
+ * cosine pre-weight, applied by the caller through vg_filter_rows'
+ * row_weight) and processing/proj2.py:606-613 (1/U^2); vir has no working
+ * fan FBP (reconstruction.fan_fbp, :7-67, calls removed interfaces). */
+int vg_fbp2d_bp(const vg_dd2d_geom *g, const float *q, const double *trig,
+                float *img, void *stream);
+
+/* ---- elementwise / filter helpers -------------------------------------- */
+
+/* out (cols, rows) = transpose of in (rows, cols). */
+int vg_transpose(const float *in, int rows, int cols, float *out, void *stream);
+
+/* Ramp filtering of each sinogram row as a linear convolution with the
+ * spatial kernel of the padded rFFT filter (filtration.filter_sino,
+ * filtration.py:238-309): out[r, i] = sum_j in[r, j] * taps[i - j + nu - 1]
+ * with taps (2 nu - 1) = irfft(2 H, n=z) reordered to lags -(nu-1)..nu-1.
+ * rows x nu in, rows x nu out.  `row_weight` (nu values or NULL) multiplies
+ * each input row first (fan-beam cosine pre-weighting). */
+int vg_filter_rows(const float *in, int rows, int nu, const float *taps,
+                   const float *row_weight, float *out, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* VIRGPU_H */

@@ -55,6 +55,9 @@ def lib():
                                        ctypes.c_int, _dp]
         L.orc_siddon_bp_2d.argtypes = [_fp, ctypes.c_int, ctypes.c_int, _dp, _dp, ctypes.c_int,
                                        ctypes.c_int, ctypes.c_double, ctypes.c_double, _dp]
+        L.orc_siddon_trace_2d.argtypes = [ctypes.c_int, ctypes.c_int, _dp, _dp, ctypes.c_int,
+                                          ctypes.c_int, ctypes.c_double, ctypes.c_double, _ip,
+                                          ctypes.POINTER(ctypes.c_uint64), _dp]
         L.orc_siddon_count_2d.argtypes = [ctypes.c_int, ctypes.c_int, _dp, _dp, ctypes.c_int,
                                           ctypes.c_int, ctypes.c_double, ctypes.c_double]
         L.orc_siddon_count_2d.restype = ctypes.c_longlong
@@ -129,6 +132,19 @@ def siddons_bp_2d(sino, Angs, img_shape, d_det=1.0, d_pix=1.0):
                            int(img_shape[0]), int(img_shape[1]), float(d_det), float(d_pix),
                            _ptr(out, _dp))
     return out
+
+
+def siddons_trace_2d(img_shape, Angs, n_dets, d_det=1.0, d_pix=1.0):
+    """Per ray (count, hash of voxel sequence, FP64 length sum)."""
+    c, s = trig(Angs)
+    na = c.size
+    cnt = np.zeros((na, n_dets), np.int32)
+    h = np.zeros((na, n_dets), np.uint64)
+    ln = np.zeros((na, n_dets), np.float64)
+    lib().orc_siddon_trace_2d(int(img_shape[0]), int(img_shape[1]), _ptr(c, _dp), _ptr(s, _dp),
+                              na, int(n_dets), float(d_det), float(d_pix), _ptr(cnt, _ip),
+                              h.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)), _ptr(ln, _dp))
+    return cnt, h, ln
 
 
 def siddons_count_2d(img_shape, Angs, n_dets, d_det=1.0, d_pix=1.0):

@@ -153,6 +153,41 @@ void orc_siddon_bp_2d(const float *sino, int na, int n_dets, const double *cosv,
     }
 }
 
+/* Per-ray trace for voxel-sequence checks: segment count, order-sensitive
+ * hash of voxel indices ix*ny+iy (h = (h ^ (idx + C1)) * C2 from
+ * h0 = 0xCBF29CE484222325), and the sum of lengths. */
+void orc_siddon_trace_2d(int nx, int ny, const double *cosv, const double *sinv,
+                         int na, int n_dets, double d_det, double d_pix,
+                         int *count, uint64_t *hash, double *len)
+{
+#pragma omp parallel
+    {
+        int cap = nx + ny + 4;
+        double *scr = (double *)malloc(sizeof(double) * cap);
+        int *ix = (int *)malloc(sizeof(int) * cap);
+        int *iy = (int *)malloc(sizeof(int) * cap);
+        double *ln = (double *)malloc(sizeof(double) * cap);
+#pragma omp for schedule(dynamic)
+        for (int ia = 0; ia < na; ia++)
+            for (int k = 0; k < n_dets; k++) {
+                int ns = siddon2d_ray_segments(nx, ny, d_pix, d_det, n_dets, k,
+                                               cosv[ia], sinv[ia], scr, ix, iy, ln);
+                uint64_t h = 0xCBF29CE484222325ull;
+                double l = 0.0;
+                for (int s = 0; s < ns; s++) {
+                    uint64_t v = (uint64_t)ix[s] * (uint64_t)ny + (uint64_t)iy[s];
+                    h = (h ^ (v + 0x9E3779B97F4A7C15ull)) * 0x100000001B3ull;
+                    l += ln[s];
+                }
+                size_t o = (size_t)ia * n_dets + k;
+                count[o] = ns;
+                hash[o] = h;
+                len[o] = l;
+            }
+        free(scr); free(ix); free(iy); free(ln);
+    }
+}
+
 /* Number of nonzero segments per ray (for the intersection count metric). */
 long long orc_siddon_count_2d(int nx, int ny, const double *cosv,
                               const double *sinv, int na, int n_dets,

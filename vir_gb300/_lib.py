@@ -1,0 +1,91 @@
+"""ctypes binding of libvirgpu.so (the C ABI declared in include/virgpu.h).
+
+The library is loaded from vir_gb300/_build (built in tree by
+vir_gb300.build).  There is no CPU fallback: every projector call needs the
+library and a CUDA device, and fails loudly with VirGpuError otherwise.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+from . import build as _build
+
+_lock = threading.Lock()
+_lib = None
+
+c_int, c_float, c_double, c_void_p = ctypes.c_int, ctypes.c_float, ctypes.c_double, ctypes.c_void_p
+
+
+class VirGpuError(RuntimeError):
+    """Raised when a libvirgpu entry point returns a non-zero status."""
+
+    def __init__(self, fn, status, msg):
+        super().__init__(f"{fn} failed with status {status}: {msg}")
+        self.status = status
+
+
+class DD2DGeom(ctypes.Structure):
+    """vg_dd2d_geom (include/virgpu.h)."""
+    _fields_ = [("nx", c_int), ("ny", c_int), ("na", c_int), ("nu", c_int),
+                ("du", c_float), ("su", c_float), ("d_pix", c_float),
+                ("DSO", c_float), ("DSD", c_float), ("fan", c_int)]
+
+
+# name -> argtypes (all return int status)
+_PROTOS = {
+    "vg_siddon2d_fp": [c_void_p, c_int, c_int, c_void_p, c_int, c_int, c_double, c_double,
+                       c_void_p, c_void_p],
+    "vg_siddon2d_bp": [c_void_p, c_int, c_int, c_void_p, c_int, c_int, c_double, c_double,
+                       c_void_p, c_void_p],
+    "vg_siddon2d_trace": [c_int, c_int, c_void_p, c_int, c_int, c_double, c_double, c_void_p,
+                          c_void_p, c_void_p, c_void_p],
+    "vg_dd2d_fp": [ctypes.POINTER(DD2DGeom), c_void_p, c_void_p, c_void_p, c_void_p, c_void_p],
+    "vg_dd2d_bp": [ctypes.POINTER(DD2DGeom), c_void_p, c_void_p, c_void_p, c_void_p],
+    "vg_dd2d_sirt_iter": [ctypes.POINTER(DD2DGeom), c_void_p, c_void_p, c_void_p, c_float,
+                          c_void_p, c_void_p, c_void_p, c_void_p, c_void_p],
+    "vg_fbp2d_bp": [ctypes.POINTER(DD2DGeom), c_void_p, c_void_p, c_void_p, c_void_p],
+    "vg_transpose": [c_void_p, c_int, c_int, c_void_p, c_void_p],
+    "vg_filter_rows": [c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p],
+}
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = True):
+    """Load libvirgpu.so (building it first when absent) and bind prototypes."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        path = _build.LIB
+        if build_if_missing:
+            path = _build.build()
+        if not os.path.exists(path):
+            raise VirGpuError("load", -1, f"{path} is missing; run python -m vir_gb300.build")
+        L = ctypes.CDLL(path)
+        L.vg_last_error.restype = ctypes.c_char_p
+        L.vg_status_string.restype = ctypes.c_char_p
+        L.vg_version.restype = c_int
+        for name, args in _PROTOS.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = c_int
+        _lib = L
+        return L
+
+
+def call(name, *args):
+    """Invoke an entry point and raise VirGpuError on a non-zero status."""
+    L = _lib if _lib is not None else load()
+    st = getattr(L, name)(*args)
+    if st != 0:
+        raise VirGpuError(name, st, L.vg_last_error().decode(errors="replace"))
+    return st
+
+
+def exported_symbols():
+    return list(_PROTOS) + ["vg_version", "vg_last_error", "vg_status_string"]

@@ -1,0 +1,291 @@
+// 2D parallel-beam Siddon forward projector and its exact gather-form
+// adjoint.
+//
+// Geometry follows sys_mat/fp_2d_par.py:11-64 operation for operation, in
+// FP64 with every multiply/add/divide separately rounded (no contraction), so
+// the sorted plane-crossing sequence, the segment midpoints and therefore the
+// voxel index sequence of every ray are the ones vir's FP64 code produces:
+//   edges      X_b[i] = d_pix * (i - nx/2.0)                       (:16-17)
+//   detector   det_k  = d_det * ((k - n_dets/2.0) + 0.5)           (:20)
+//   origin     (x0, y0) = det_k * (-dy, dx), (dx, dy) = (cos, sin) (:23,29-30)
+//   entry/exit t0 = max(min tx, min ty), t1 = min(max tx, max ty)  (:33-43)
+//   crossings  all t = (X_b[i] - x0)/dx, (Y_b[j] - y0)/dy in [t0, t1], sorted
+//   segments   consecutive pairs a < b, voxel floor((x0 + (0.5(a+b))dx - X_b[0])/d_pix)
+// The x- and y-crossing sequences are each monotone in their index, so the
+// sort is a two-way merge.  Intersection lengths (b - a) are rounded to FP32
+// and the ray sum is Kahan-compensated FP32.
+#include "vg_common.cuh"
+
+namespace {
+
+using namespace vg;
+
+struct SidGeom {
+    int nx, ny, n_dets;
+    double d_det, d_pix, inv_dpix;
+    double xb0, xbn, yb0, ybn;
+    int dpix_pow2;  // d_pix is a power of two: x / d_pix == x * (1/d_pix) exactly
+};
+
+__device__ __forceinline__ double edge(double d_pix, int i, int n) {
+    return d_mul(d_pix, (double)i - (double)n * 0.5);
+}
+
+__device__ __forceinline__ double div_pix(const SidGeom &g, double v) {
+    return g.dpix_pow2 ? d_mul(v, g.inv_dpix) : d_div(v, g.d_pix);
+}
+
+struct Ray {
+    double x0, y0, t0, t1;
+    bool valid;
+};
+
+__device__ __forceinline__ Ray ray_setup(const SidGeom &g, int k, double dx, double dy) {
+    Ray r;
+    double det = d_mul(g.d_det, d_add((double)k - (double)g.n_dets * 0.5, 0.5));
+    r.x0 = d_mul(det, -dy);
+    r.y0 = d_mul(det, dx);
+    double tx0 = -INFINITY, txn = INFINITY, ty0 = -INFINITY, tyn = INFINITY;
+    if (dx != 0.0) { tx0 = d_div(d_sub(g.xb0, r.x0), dx); txn = d_div(d_sub(g.xbn, r.x0), dx); }
+    if (dy != 0.0) { ty0 = d_div(d_sub(g.yb0, r.y0), dy); tyn = d_div(d_sub(g.ybn, r.y0), dy); }
+    r.t0 = fmax(fmin(tx0, txn), fmin(ty0, tyn));
+    r.t1 = fmin(fmax(tx0, txn), fmax(ty0, tyn));
+    r.valid = !(r.t1 <= r.t0 || isinf(r.t0) || isinf(r.t1));
+    return r;
+}
+
+// Crossing parameter of the j-th plane in traversal order (t non-decreasing
+// in j): index i = j when the direction component is positive, n - j else.
+__device__ __forceinline__ double cross_t(double d_pix, int n, int j, bool pos, double o, double d) {
+    int i = pos ? j : n - j;
+    return d_div(d_sub(edge(d_pix, i, n), o), d);
+}
+
+// First traversal index whose crossing is >= t0 (n + 1 when none).
+__device__ int first_crossing(double d_pix, int n, bool pos, double o, double d, double t0,
+                              double b0) {
+    double p = d_add(o, d_mul(t0, d));
+    double fi = floor((p - b0) / d_pix);
+    int j = (int)fmin(fmax(pos ? fi : (double)n - fi, 0.0), (double)(n + 1));
+    // settle on the exact boundary (a handful of steps at most)
+    for (int it = 0; it < 4 && j > 0 && cross_t(d_pix, n, j - 1, pos, o, d) >= t0; ++it) --j;
+    while (j > 0 && cross_t(d_pix, n, j - 1, pos, o, d) >= t0) --j;
+    while (j <= n && cross_t(d_pix, n, j, pos, o, d) < t0) ++j;
+    return j;
+}
+
+// TRACE: instead of the line integral, record per ray the number of
+// segments, an order-sensitive hash of their voxel indices and the FP64 sum
+// of their lengths (used to check voxel sequences against the oracle).
+struct Trace {
+    int *count;
+    unsigned long long *hash;
+    double *len;
+};
+
+__device__ __forceinline__ unsigned long long trace_mix(unsigned long long h, unsigned long long v) {
+    return (h ^ (v + 0x9E3779B97F4A7C15ull)) * 0x100000001B3ull;
+}
+
+template <bool TRACE>
+__global__ void
+siddon2d_fp_kernel(SidGeom g, const float *__restrict__ img, const double *__restrict__ trig,
+                   int na, float *__restrict__ sino, Trace tr) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    int ia = blockIdx.y;
+    if (k >= g.n_dets || ia >= na) return;
+    double dx = trig[2 * ia], dy = trig[2 * ia + 1];
+    Ray r = ray_setup(g, k, dx, dy);
+    Kahan acc;
+    int tcount = 0;
+    unsigned long long thash = 0xCBF29CE484222325ull;
+    double tlen = 0.0;
+    if (r.valid) {
+        const double INF = INFINITY;
+        bool px = dx > 0.0, py = dy > 0.0;
+        int jx = g.nx + 1, jy = g.ny + 1;
+        double tx = INF, ty = INF;
+        if (dx != 0.0) {
+            jx = first_crossing(g.d_pix, g.nx, px, r.x0, dx, r.t0, g.xb0);
+            if (jx <= g.nx) tx = cross_t(g.d_pix, g.nx, jx, px, r.x0, dx);
+            if (tx > r.t1) tx = INF;
+        }
+        if (dy != 0.0) {
+            jy = first_crossing(g.d_pix, g.ny, py, r.y0, dy, r.t0, g.yb0);
+            if (jy <= g.ny) ty = cross_t(g.d_pix, g.ny, jy, py, r.y0, dy);
+            if (ty > r.t1) ty = INF;
+        }
+        double tprev = INF;
+        // bounded: every step consumes one of nx + ny + 2 crossings
+        for (int step = 0; step < g.nx + g.ny + 4; ++step) {
+            double tn;
+            if (tx <= ty) {
+                tn = tx;
+                if (tn == INF) break;
+                ++jx;
+                tx = jx <= g.nx ? cross_t(g.d_pix, g.nx, jx, px, r.x0, dx) : INF;
+                if (tx > r.t1) tx = INF;
+            } else {
+                tn = ty;
+                ++jy;
+                ty = jy <= g.ny ? cross_t(g.d_pix, g.ny, jy, py, r.y0, dy) : INF;
+                if (ty > r.t1) ty = INF;
+            }
+            if (tprev != INF && tn > tprev) {
+                double m = d_mul(0.5, d_add(tprev, tn));
+                double fx = floor(div_pix(g, d_sub(d_add(r.x0, d_mul(m, dx)), g.xb0)));
+                double fy = floor(div_pix(g, d_sub(d_add(r.y0, d_mul(m, dy)), g.yb0)));
+                if (fx >= 0.0 && fx < g.nx && fy >= 0.0 && fy < g.ny) {
+                    size_t pix = (size_t)fx * g.ny + (int)fy;
+                    if (TRACE) {
+                        ++tcount;
+                        thash = trace_mix(thash, pix);
+                        tlen = d_add(tlen, d_sub(tn, tprev));
+                    } else {
+                        float w = (float)d_sub(tn, tprev);
+                        acc.add(__fmul_rn(__ldg(img + pix), w));
+                    }
+                }
+            }
+            tprev = tn;
+        }
+    }
+    size_t o = (size_t)ia * g.n_dets + k;
+    if (TRACE) {
+        tr.count[o] = tcount;
+        tr.hash[o] = thash;
+        tr.len[o] = tlen;
+    } else {
+        sino[o] = acc.s;
+    }
+}
+
+// Gather-form adjoint.  For pixel (ix, iy) and view ia, the candidate rays
+// are the bins whose centre lies within the pixel's projected extent (plus a
+// margin).  For each candidate the crossings of the planes around the pixel
+// (x planes ix-1..ix+2, y planes iy-1..iy+2) are recomputed with the forward
+// projector's arithmetic and filtered to [t0, t1]; every consecutive pair whose
+// midpoint voxel (by the forward projector's rule) is (ix, iy) is a segment
+// the forward projector assigns to this pixel, with the same FP64 length.
+// A segment whose midpoint lies in (ix, iy) has both ends on planes bounding
+// this pixel's neighbourhood, so this enumerates exactly the forward
+// segments: the pair is an exact transpose, degenerate rays included.
+__device__ __forceinline__ int window_crossings(double d_pix, int n, int i_lo, double o, double d,
+                                                double t0, double t1, double *out) {
+    int c = 0;
+    if (d == 0.0) return 0;
+    for (int q = 0; q < 4; ++q) {
+        int i = i_lo + q;
+        if (i < 0 || i > n) continue;
+        double t = d_div(d_sub(edge(d_pix, i, n), o), d);
+        if (t0 <= t && t <= t1) out[c++] = t;
+    }
+    // ascending order (the sequence is monotone in i; reverse when d < 0)
+    if (d < 0.0)
+        for (int a = 0, b = c - 1; a < b; ++a, --b) { double t = out[a]; out[a] = out[b]; out[b] = t; }
+    return c;
+}
+
+__global__ void __launch_bounds__(256)
+siddon2d_bp_kernel(SidGeom g, const float *__restrict__ sino, const double *__restrict__ trig,
+                   int na, float *__restrict__ img) {
+    int iy = blockIdx.x * blockDim.x + threadIdx.x;
+    int ix = blockIdx.y;
+    if (iy >= g.ny || ix >= g.nx) return;
+    // pixel centre in FP32 for candidate selection only
+    float xc = (float)(g.d_pix * ((double)ix + 0.5 - g.nx * 0.5));
+    float yc = (float)(g.d_pix * ((double)iy + 0.5 - g.ny * 0.5));
+    float half = 0.5f * (float)g.d_pix;
+    float inv_det = (float)(1.0 / g.d_det);
+    float koff = 0.5f * g.n_dets - 0.5f;
+    Kahan acc;
+    for (int ia = 0; ia < na; ++ia) {
+        double dx = __ldg(trig + 2 * ia), dy = __ldg(trig + 2 * ia + 1);
+        float fdx = (float)dx, fdy = (float)dy;
+        float uc = -fdy * xc + fdx * yc;
+        float hw = half * (fabsf(fdx) + fabsf(fdy)) + 1e-3f * (float)g.d_det + 1e-5f * fabsf(uc);
+        int k_lo = max(0, (int)ceilf((uc - hw) * inv_det + koff));
+        int k_hi = min(g.n_dets - 1, (int)floorf((uc + hw) * inv_det + koff));
+        for (int k = k_lo; k <= k_hi; ++k) {
+            Ray r = ray_setup(g, k, dx, dy);
+            if (!r.valid) continue;
+            double tx[4], ty[4], t[8];
+            int nx_ = window_crossings(g.d_pix, g.nx, ix - 1, r.x0, dx, r.t0, r.t1, tx);
+            int ny_ = window_crossings(g.d_pix, g.ny, iy - 1, r.y0, dy, r.t0, r.t1, ty);
+            // merge the two ascending lists
+            int a = 0, b = 0, n = 0;
+            while (a < nx_ || b < ny_) {
+                if (b >= ny_ || (a < nx_ && tx[a] <= ty[b])) t[n++] = tx[a++];
+                else t[n++] = ty[b++];
+            }
+            float yv = __ldg(sino + (size_t)ia * g.n_dets + k);
+            for (int s = 0; s + 1 < n; ++s) {
+                double ta = t[s], tb = t[s + 1];
+                if (!(tb > ta)) continue;
+                double m = d_mul(0.5, d_add(ta, tb));
+                double fx = floor(div_pix(g, d_sub(d_add(r.x0, d_mul(m, dx)), g.xb0)));
+                if (fx != (double)ix) continue;
+                double fy = floor(div_pix(g, d_sub(d_add(r.y0, d_mul(m, dy)), g.yb0)));
+                if (fy != (double)iy) continue;
+                acc.add(__fmul_rn(yv, (float)d_sub(tb, ta)));
+            }
+        }
+    }
+    img[(size_t)ix * g.ny + iy] = acc.s;
+}
+
+int make_geom(SidGeom &g, int nx, int ny, int n_dets, double d_det, double d_pix) {
+    VG_REQUIRE(nx > 0 && ny > 0 && n_dets > 0, "siddon2d: sizes must be positive");
+    VG_REQUIRE(d_det > 0 && d_pix > 0, "siddon2d: d_det and d_pix must be positive");
+    g.nx = nx; g.ny = ny; g.n_dets = n_dets;
+    g.d_det = d_det; g.d_pix = d_pix;
+    g.inv_dpix = 1.0 / d_pix;
+    int e;
+    g.dpix_pow2 = frexp(d_pix, &e) == 0.5;
+    g.xb0 = d_pix * (0.0 - nx * 0.5);
+    g.xbn = d_pix * ((double)nx - nx * 0.5);
+    g.yb0 = d_pix * (0.0 - ny * 0.5);
+    g.ybn = d_pix * ((double)ny - ny * 0.5);
+    return VG_OK;
+}
+
+}  // namespace
+
+extern "C" int vg_siddon2d_fp(const float *img, int nx, int ny, const double *trig, int na,
+                              int n_dets, double d_det, double d_pix, float *sino, void *stream) {
+    SidGeom g;
+    int st = make_geom(g, nx, ny, n_dets, d_det, d_pix);
+    if (st) return st;
+    VG_REQUIRE(na > 0 && na < 65536, "siddon2d_fp: na out of range");
+    VG_REQUIRE(img && trig && sino, "siddon2d_fp: null pointer");
+    dim3 grid(ceil_div(n_dets, 128), na);
+    siddon2d_fp_kernel<false><<<grid, 128, 0, as_stream(stream)>>>(g, img, trig, na, sino, Trace{});
+    return launch_status("siddon2d_fp");
+}
+
+extern "C" int vg_siddon2d_trace(int nx, int ny, const double *trig, int na, int n_dets,
+                                 double d_det, double d_pix, int *count,
+                                 unsigned long long *hash, double *len, void *stream) {
+    SidGeom g;
+    int st = make_geom(g, nx, ny, n_dets, d_det, d_pix);
+    if (st) return st;
+    VG_REQUIRE(na > 0 && na < 65536, "siddon2d_trace: na out of range");
+    VG_REQUIRE(trig && count && hash && len, "siddon2d_trace: null pointer");
+    dim3 grid(ceil_div(n_dets, 128), na);
+    siddon2d_fp_kernel<true><<<grid, 128, 0, as_stream(stream)>>>(g, nullptr, trig, na, nullptr,
+                                                                 Trace{count, hash, len});
+    return launch_status("siddon2d_trace");
+}
+
+extern "C" int vg_siddon2d_bp(const float *sino, int na, int n_dets, const double *trig, int nx,
+                              int ny, double d_det, double d_pix, float *img, void *stream) {
+    SidGeom g;
+    int st = make_geom(g, nx, ny, n_dets, d_det, d_pix);
+    if (st) return st;
+    VG_REQUIRE(na > 0, "siddon2d_bp: na must be positive");
+    VG_REQUIRE(nx < 65536, "siddon2d_bp: nx out of range");
+    VG_REQUIRE(img && trig && sino, "siddon2d_bp: null pointer");
+    dim3 grid(ceil_div(ny, 256), nx);
+    siddon2d_bp_kernel<<<grid, 256, 0, as_stream(stream)>>>(g, sino, trig, na, img);
+    return launch_status("siddon2d_bp");
+}

@@ -1,0 +1,167 @@
+"""SIRT and FBP on the GPU distance-driven projectors.
+
+SIRT follows vir's update rule (``sys_mat/sirt_dd.py:23-76``):
+
+    x0 = 1e-5;  for i in range(1, iters):
+        r = (y - FP x) / W_sino       (left as FP x where W_sino == 0)
+        x = x + gamma * BP(r) / W_img (left as BP r where W_img == 0)
+
+with ``W_sino = FP(1)`` and ``W_img = BP(1)`` computed by the same projector
+pair.  The reference runs it around its 4-sided translational geometry; the
+same rule wraps the parallel and fan projectors here (as in
+``processing/SIRT/sirt.py:34-40``).  On the GPU one update is two fused
+kernels (``vg_dd2d_sirt_iter``: residual ratio in the FP epilogue, image
+update in the BP epilogue), and a run of updates is captured once as a CUDA
+graph and replayed.
+
+FBP (``fbp_2d``) is filter (``filtration.filter_sino``'s 2H, on the GPU) then
+a pixel-driven backprojection (``vg_fbp2d_bp``); the fan version pre-weights
+rows by DSO / sqrt(DSO^2 + s^2) with s the bin centre scaled to the
+isocentre and filters at the isocentre spacing du * DSO / DSD.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _core
+from ._lib import DD2DGeom, call
+from .filtration import filter_rows_device
+
+
+def _geom(nx, ny, na, nu, du, su, d_pix, DSO, DSD, fan):
+    return DD2DGeom(int(nx), int(ny), int(na), int(nu), _core.f32(du), _core.f32(su),
+                    _core.f32(d_pix), _core.f32(DSO), _core.f32(DSD), int(fan))
+
+
+class SIRT2D:
+    """Resident SIRT state for one 2D problem on one GPU.
+
+    All buffers live in device memory for the life of the object: the
+    measured sinogram ``y``, ``1/W_sino``, ``1/W_img``, the iterate ``x`` and
+    its transpose, and the residual scratch ``r``.
+    """
+
+    def __init__(self, sino, ang_arr, img_shape, geom="par", DSO=0.0, DSD=0.0, du=1.0, su=0.0,
+                 d_pix=1.0, gamma=1.0, x0=1e-5, W_sino=None, W_img=None, device=None):
+        _core.require_cuda()
+        self.dev = device or _core.device_of(sino)
+        self.fan = 1 if geom == "fan" else 0
+        self.y = _core.to_device(sino, self.dev)
+        self.trig = _core.trig_cache.get(ang_arr, np.float32, self.dev)
+        na = self.trig.numel() // 2
+        nx, ny = (int(v) for v in img_shape)
+        nu = self.y.shape[1]
+        if self.y.shape[0] != na:
+            raise ValueError("sino rows must equal len(ang_arr)")
+        self.g = _geom(nx, ny, na, nu, du, su, d_pix, DSO, DSD, self.fan)
+        self.gamma = float(gamma)
+        st = _core.stream(self.dev)
+        if W_sino is None:
+            ones = torch.ones((nx, ny), dtype=torch.float32, device=self.dev)
+            W_sino = self.fp(ones)
+        else:
+            W_sino = _core.to_device(W_sino, self.dev)
+        if W_img is None:
+            W_img = self.bp(torch.ones((na, nu), dtype=torch.float32, device=self.dev))
+        else:
+            W_img = _core.to_device(W_img, self.dev)
+        self.inv_ws = torch.where(W_sino != 0, 1.0 / W_sino, torch.zeros_like(W_sino))
+        self.inv_wi = torch.where(W_img != 0, 1.0 / W_img, torch.zeros_like(W_img))
+        self.x = torch.full((nx, ny), float(np.float32(x0)), dtype=torch.float32, device=self.dev)
+        self.xT = self.x.t().contiguous()
+        self.r = torch.empty((na, nu), dtype=torch.float32, device=self.dev)
+        self._graph = None
+        self._graph_n = 0
+        del st
+
+    # projector pair on this geometry
+    def fp(self, img: torch.Tensor) -> torch.Tensor:
+        out = torch.empty((self.g.na, self.g.nu), dtype=torch.float32, device=self.dev)
+        imgT = img.t().contiguous()
+        call("vg_dd2d_fp", ctypes.byref(self.g), _core.ptr(img), _core.ptr(imgT),
+             _core.ptr(self.trig), _core.ptr(out), _core.stream(self.dev))
+        return out
+
+    def bp(self, sino: torch.Tensor) -> torch.Tensor:
+        out = torch.empty((self.g.nx, self.g.ny), dtype=torch.float32, device=self.dev)
+        call("vg_dd2d_bp", ctypes.byref(self.g), _core.ptr(sino), _core.ptr(self.trig),
+             _core.ptr(out), _core.stream(self.dev))
+        return out
+
+    def _iter(self):
+        call("vg_dd2d_sirt_iter", ctypes.byref(self.g), _core.ptr(self.y), _core.ptr(self.inv_ws),
+             _core.ptr(self.inv_wi), ctypes.c_float(self.gamma), _core.ptr(self.trig),
+             _core.ptr(self.x), _core.ptr(self.xT), _core.ptr(self.r), _core.stream(self.dev))
+
+    def capture(self, n: int):
+        """Capture ``n`` updates as one CUDA graph (replayed by run())."""
+        s = torch.cuda.Stream(self.dev)
+        s.wait_stream(torch.cuda.current_stream(self.dev))
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.stream(s):
+            with torch.cuda.graph(g, stream=s):
+                for _ in range(n):
+                    self._iter()
+        torch.cuda.current_stream(self.dev).wait_stream(s)
+        self._graph, self._graph_n = g, n
+        return g
+
+    def run(self, n_updates: int, graph: bool = True):
+        """Apply ``n_updates`` SIRT updates to x (asynchronous)."""
+        if n_updates <= 0:
+            return self.x
+        if graph:
+            if self._graph is None or self._graph_n != n_updates:
+                self.capture(n_updates)
+            self._graph.replay()
+        else:
+            for _ in range(n_updates):
+                self._iter()
+        return self.x
+
+    def reset(self, x0=1e-5):
+        self.x.fill_(float(np.float32(x0)))
+        self.xT.fill_(float(np.float32(x0)))
+
+
+def sirt_2d(sino, ang_arr, img_shape, geom="par", DSO=0.0, DSD=0.0, du=1.0, su=0.0, d_pix=1.0,
+            gamma=1.0, iters=100, W_sino=None, W_img=None, graph=True):
+    """vir's SIRT (``iters - 1`` updates, x0 = 1e-5) on the parallel or fan
+    distance-driven pair.  numpy in -> numpy out."""
+    s = SIRT2D(sino, ang_arr, img_shape, geom=geom, DSO=DSO, DSD=DSD, du=du, su=su, d_pix=d_pix,
+               gamma=gamma, W_sino=W_sino, W_img=W_img)
+    x = s.run(int(iters) - 1, graph=graph)
+    return _core.to_host_like(x.clone(), sino)
+
+
+def fan_preweight(nu, du, su, DSO, DSD):
+    """Equispaced cosine pre-weight DSO / sqrt(DSO^2 + s^2) at the bin
+    centres scaled to the isocentre (processing/reconstruction.py:99-107)."""
+    s = du * (np.arange(nu) - nu / 2.0 + 0.5 + su) * DSO / DSD
+    return DSO / np.sqrt(DSO ** 2 + s ** 2)
+
+
+def fbp_2d(sino, ang_arr, img_shape, geom="par", DSO=0.0, DSD=0.0, du=1.0, su=0.0, d_pix=1.0,
+           filter_type="ramp", cutoff=0.5, real_space=True):
+    """Filtered backprojection of a full scan (pi parallel, 2 pi fan)."""
+    dev = _core.device_of(sino)
+    y = _core.to_device(sino, dev)
+    trig = _core.trig_cache.get(ang_arr, np.float32, dev)
+    na, nu = y.shape
+    fan = 1 if geom == "fan" else 0
+    if fan:
+        w = torch.from_numpy(fan_preweight(nu, float(np.float32(du)), float(np.float32(su)),
+                                           float(np.float32(DSO)),
+                                           float(np.float32(DSD))).astype(np.float32)).to(dev)
+        q = filter_rows_device(y, du * DSO / DSD, filter_type, cutoff, real_space, row_weight=w)
+    else:
+        q = filter_rows_device(y, du, filter_type, cutoff, real_space)
+    nx, ny = (int(v) for v in img_shape)
+    g = _geom(nx, ny, na, nu, du, su, d_pix, DSO, DSD, fan)
+    img = torch.empty((nx, ny), dtype=torch.float32, device=dev)
+    call("vg_fbp2d_bp", ctypes.byref(g), _core.ptr(q), _core.ptr(trig), _core.ptr(img),
+         _core.stream(dev))
+    return _core.to_host_like(img, sino)

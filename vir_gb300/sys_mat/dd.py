@@ -1,0 +1,80 @@
+"""Distance-driven projectors, drop-in for vir ``sys_mat/dd.py``.
+
+Same names, signatures, return layouts and scales as the reference:
+
+* ``dd_fp_par_2d(img, ang_arr, nu, du=1.0, su=0.0, d_pix=1.0, sample=1)``
+  (dd.py:651) -> ``(na, nu)`` sinogram, ``A x * d_pix / du``;
+* ``dd_bp_par_2d(sino, ang_arr, img_shape, du=1.0, su=0.0, d_pix=1.0)``
+  (dd.py:666) -> ``(nx, ny)`` image, ``A^T y / (na d_pix)``;
+* ``dd_fp_fan_2d`` / ``dd_bp_fan_2d`` (dd.py:730, 739), the same with
+  ``DSO, DSD`` for a flat detector at ``DSD`` from the source.
+
+Inputs are cast to float32 as ``as_float32`` does (dd.py:29-36, 653); angles
+too, so the per-view driving-axis choice (|sin| >= |cos|, dd.py:478) is made
+on the reference's own float32 trig values.  ``sample`` is accepted and, as
+in the reference's 2D functions, unused (dd.py:656-658).
+
+Computation runs on the GPU (libvirgpu: gather-form kernels, see
+csrc/dd2d.cu).  numpy in -> numpy out; torch CUDA tensors stay on the device.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from .. import _core
+from .._lib import DD2DGeom, call
+
+
+def _geom(nx, ny, na, nu, du, su, d_pix, DSO=0.0, DSD=0.0, fan=0):
+    return DD2DGeom(int(nx), int(ny), int(na), int(nu), _core.f32(du), _core.f32(su),
+                    _core.f32(d_pix), _core.f32(DSO), _core.f32(DSD), int(fan))
+
+
+def _fp(img, ang_arr, nu, du, su, d_pix, DSO, DSD, fan):
+    dev = _core.device_of(img)
+    x = _core.to_device(img, dev)
+    if x.ndim != 2:
+        raise ValueError("img must be 2D (nx, ny)")
+    trig = _core.trig_cache.get(ang_arr, np.float32, dev)
+    na = trig.numel() // 2
+    g = _geom(x.shape[0], x.shape[1], na, nu, du, su, d_pix, DSO, DSD, fan)
+    xT = x.t().contiguous()
+    sino = _core.empty((na, nu), dev)
+    call("vg_dd2d_fp", ctypes.byref(g), _core.ptr(x), _core.ptr(xT), _core.ptr(trig),
+         _core.ptr(sino), _core.stream(dev))
+    return _core.to_host_like(sino, img)
+
+
+def _bp(sino, ang_arr, img_shape, du, su, d_pix, DSO, DSD, fan):
+    dev = _core.device_of(sino)
+    y = _core.to_device(sino, dev)
+    if y.ndim != 2:
+        raise ValueError("sino must be 2D (na, nu)")
+    trig = _core.trig_cache.get(ang_arr, np.float32, dev)
+    na = trig.numel() // 2
+    if y.shape[0] != na:
+        raise ValueError(f"sino has {y.shape[0]} views, ang_arr {na}")
+    nx, ny = (int(v) for v in img_shape)
+    g = _geom(nx, ny, na, y.shape[1], du, su, d_pix, DSO, DSD, fan)
+    img = _core.empty((nx, ny), dev)
+    call("vg_dd2d_bp", ctypes.byref(g), _core.ptr(y), _core.ptr(trig), _core.ptr(img),
+         _core.stream(dev))
+    return _core.to_host_like(img, sino)
+
+
+def dd_fp_par_2d(img, ang_arr, nu, du=1.0, su=0.0, d_pix=1.0, sample=1):
+    return _fp(img, ang_arr, nu, du, su, d_pix, 0.0, 0.0, 0)
+
+
+def dd_bp_par_2d(sino, ang_arr, img_shape, du=1.0, su=0.0, d_pix=1.0):
+    return _bp(sino, ang_arr, img_shape, du, su, d_pix, 0.0, 0.0, 0)
+
+
+def dd_fp_fan_2d(img, ang_arr, nu, DSO, DSD, du=1.0, su=0.0, d_pix=1.0):
+    return _fp(img, ang_arr, nu, du, su, d_pix, DSO, DSD, 1)
+
+
+def dd_bp_fan_2d(sino, ang_arr, img_shape, DSO, DSD, du=1.0, su=0.0, d_pix=1.0):
+    return _bp(sino, ang_arr, img_shape, du, su, d_pix, DSO, DSD, 1)
