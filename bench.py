@@ -179,6 +179,21 @@ def run_reference(args):
     return 0
 
 
+def run_kernels_only(n):
+    """Launch the SIRT iteration's kernels n times (for ncu captures)."""
+    import torch
+    from vir_gb300 import reconstruction as rc
+    w = WORKLOAD
+    img, angs, y = make_inputs()
+    sirt = rc.SIRT2D(y, angs, img.shape, geom="fan", DSO=w["DSO"], DSD=w["DSD"], du=w["du"],
+                     d_pix=w["d_pix"])
+    for _ in range(n):
+        sirt.run(1, graph=False)
+    torch.cuda.synchronize()
+    print(json.dumps({"kernels_only": n, "ok": True}))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -186,9 +201,13 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--kernels-only", type=int, default=0, metavar="N",
+                    help="profiling aid: run the two fused SIRT kernels N times each, no timing")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.kernels_only:
+        return run_kernels_only(args.kernels_only)
 
     import torch
     import torch.distributed as dist
