@@ -272,7 +272,7 @@ def main():
              _core.ptr(sirt.trig), _core.ptr(sirt.r), _core.stream(dev))
         e[1].record(stream)
         call("vg_dd2d_bp", ctypes.byref(g), _core.ptr(sirt.r), _core.ptr(sirt.trig),
-             _core.ptr(flush), _core.stream(dev))
+             _core.ptr(flush), _core.ptr(sirt.ws), sirt.ws.numel(), _core.stream(dev))
         e[2].record(stream)
         torch.cuda.synchronize(dev)
         if i >= 2:

@@ -22,6 +22,7 @@
 #ifndef VIRGPU_H
 #define VIRGPU_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -92,11 +93,19 @@ typedef struct {
 int vg_dd2d_fp(const vg_dd2d_geom *g, const float *img, const float *imgT,
                const double *trig, float *sino, void *stream);
 
+/* Bytes of device workspace vg_dd2d_bp and vg_dd2d_sirt_iter need for this
+ * geometry (per-view running integrals of the sinogram rows and line
+ * scales); 0 for an invalid geometry. */
+size_t vg_dd2d_workspace_bytes(const vg_dd2d_geom *g);
+
 /* Backprojection, gather form (one thread per pixel over all views, no
  * atomics), returns A^T y / (na d_pix) exactly as dd_bp_par_2d /
- * dd_bp_fan_2d (dd.py:666-672, 721-723; 739-745, 799-801). */
+ * dd_bp_fan_2d (dd.py:666-672, 721-723; 739-745, 799-801).  `workspace` is
+ * caller-owned device memory of at least vg_dd2d_workspace_bytes(g) bytes,
+ * 256-byte aligned; its contents need no initialisation. */
 int vg_dd2d_bp(const vg_dd2d_geom *g, const float *sino, const double *trig,
-               float *img, void *stream);
+               float *img, void *workspace, size_t workspace_bytes,
+               void *stream);
 
 /* One SIRT update on the same projector pair, both halves fused
  * (sys_mat/sirt_dd.py:51-72):
@@ -107,7 +116,8 @@ int vg_dd2d_bp(const vg_dd2d_geom *g, const float *sino, const double *trig,
 int vg_dd2d_sirt_iter(const vg_dd2d_geom *g, const float *y,
                       const float *inv_w_sino, const float *inv_w_img,
                       float gamma, const double *trig, float *x, float *xT,
-                      float *r, void *stream);
+                      float *r, void *workspace, size_t workspace_bytes,
+                      void *stream);
 
 /* Pixel-driven FBP backprojection of a ramp-filtered sinogram q (na, nu)
  * (filtered by vg_filter_rows, i.e. filtration.filter_sino's 2H):

@@ -16,6 +16,7 @@ _lock = threading.Lock()
 _lib = None
 
 c_int, c_float, c_double, c_void_p = ctypes.c_int, ctypes.c_float, ctypes.c_double, ctypes.c_void_p
+c_size_t = ctypes.c_size_t
 
 
 class VirGpuError(RuntimeError):
@@ -42,9 +43,10 @@ _PROTOS = {
     "vg_siddon2d_trace": [c_int, c_int, c_void_p, c_int, c_int, c_double, c_double, c_void_p,
                           c_void_p, c_void_p, c_void_p],
     "vg_dd2d_fp": [ctypes.POINTER(DD2DGeom), c_void_p, c_void_p, c_void_p, c_void_p, c_void_p],
-    "vg_dd2d_bp": [ctypes.POINTER(DD2DGeom), c_void_p, c_void_p, c_void_p, c_void_p],
+    "vg_dd2d_bp": [ctypes.POINTER(DD2DGeom), c_void_p, c_void_p, c_void_p, c_void_p, c_size_t,
+                   c_void_p],
     "vg_dd2d_sirt_iter": [ctypes.POINTER(DD2DGeom), c_void_p, c_void_p, c_void_p, c_float,
-                          c_void_p, c_void_p, c_void_p, c_void_p, c_void_p],
+                          c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_size_t, c_void_p],
     "vg_fbp2d_bp": [ctypes.POINTER(DD2DGeom), c_void_p, c_void_p, c_void_p, c_void_p],
     "vg_transpose": [c_void_p, c_int, c_int, c_void_p, c_void_p],
     "vg_filter_rows": [c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p],
@@ -74,6 +76,8 @@ def load(build_if_missing: bool = True):
             fn = getattr(L, name)
             fn.argtypes = args
             fn.restype = c_int
+        L.vg_dd2d_workspace_bytes.argtypes = [ctypes.POINTER(DD2DGeom)]
+        L.vg_dd2d_workspace_bytes.restype = c_size_t
         _lib = L
         return L
 
@@ -88,4 +92,17 @@ def call(name, *args):
 
 
 def exported_symbols():
-    return list(_PROTOS) + ["vg_version", "vg_last_error", "vg_status_string"]
+    return list(_PROTOS) + ["vg_version", "vg_last_error", "vg_status_string",
+                            "vg_dd2d_workspace_bytes"]
+
+
+def dd2d_workspace(g, dev):
+    """Device workspace (a uint8 tensor, 256-byte aligned) for vg_dd2d_bp."""
+    import torch
+    L = _lib if _lib is not None else load()
+    n = int(L.vg_dd2d_workspace_bytes(ctypes.byref(g)))
+    if n == 0:
+        raise VirGpuError("vg_dd2d_workspace_bytes", 1, L.vg_last_error().decode(errors="replace"))
+    t = torch.empty(n + 256, dtype=torch.uint8, device=dev)
+    off = (-t.data_ptr()) % 256
+    return t[off:off + n]

@@ -50,21 +50,28 @@ def _digest() -> str:
     return h.hexdigest()
 
 
-def build(force: bool = False, verbose: bool = False) -> str:
-    """Compile (when sources changed) and return the path of libvirgpu.so."""
-    os.makedirs(OUT_DIR, exist_ok=True)
-    stamp = os.path.join(OUT_DIR, "libvirgpu.sha256")
-    dig = _digest()
-    if not force and os.path.exists(LIB) and os.path.exists(stamp):
+def build(force: bool = False, verbose: bool = False, out_dir: str = None,
+          defines=()) -> str:
+    """Compile (when sources changed) and return the path of libvirgpu.so.
+
+    ``out_dir``/``defines`` build a variant (extra -D macros, e.g. tile
+    sizes) into another directory, for tuning sweeps."""
+    out_dir = out_dir or OUT_DIR
+    lib_path = os.path.join(out_dir, "libvirgpu.so")
+    os.makedirs(out_dir, exist_ok=True)
+    stamp = os.path.join(out_dir, "libvirgpu.sha256")
+    dig = _digest() + "|" + ",".join(defines)
+    if not force and os.path.exists(lib_path) and os.path.exists(stamp):
         with open(stamp) as fh:
             if fh.read().strip() == dig:
-                return LIB
+                return lib_path
     cc = nvcc()
+    dflags = [f"-D{d}" for d in defines]
     objs = []
 
     def compile_one(src):
-        obj = os.path.join(OUT_DIR, os.path.basename(src)[:-3] + ".o")
-        cmd = [cc, *ARCH, *NVCC_FLAGS, "-I", INCLUDE, "-c", src, "-o", obj]
+        obj = os.path.join(out_dir, os.path.basename(src)[:-3] + ".o")
+        cmd = [cc, *ARCH, *NVCC_FLAGS, *dflags, "-I", INCLUDE, "-c", src, "-o", obj]
         if verbose:
             cmd += ["-Xptxas", "-v"]
         r = subprocess.run(cmd, capture_output=True, text=True)
@@ -77,15 +84,15 @@ def build(force: bool = False, verbose: bool = False) -> str:
             objs.append(obj)
             if verbose and log:
                 print(log)
-    tmp = LIB + ".tmp"
+    tmp = lib_path + ".tmp"
     r = subprocess.run([cc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"],
                        capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")
-    os.replace(tmp, LIB)
+    os.replace(tmp, lib_path)
     with open(stamp, "w") as fh:
         fh.write(dig)
-    return LIB
+    return lib_path
 
 
 if __name__ == "__main__":

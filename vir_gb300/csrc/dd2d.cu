@@ -37,6 +37,12 @@
 // coefficient is negative the edge order is reversed, as dd.py:516-518 does.
 #include "vg_common.cuh"
 
+// Edge projections divide with __fdividef (reciprocal + multiply, 2 ulp)
+// unless built with -DVG_FAST_DIV=0 (IEEE division).
+#ifndef VG_FAST_DIV
+#define VG_FAST_DIV 1
+#endif
+
 namespace {
 
 using namespace vg;
@@ -54,12 +60,6 @@ __device__ __forceinline__ ViewGeo view_geo(const double *trig, int ia) {
     v.xdrv = fabsf(s) >= fabsf(c);
     if (v.xdrv) { v.pd = -s; v.od = c; v.po = c; v.oo = s; v.tabs = fabsf(s); }
     else        { v.pd = c;  v.od = s; v.po = -s; v.oo = c; v.tabs = fabsf(c); }
-    return v;
-}
-
-__device__ __forceinline__ ViewGeo vg_of(const float *f, int xdrv) {
-    ViewGeo v;
-    v.pd = f[0]; v.od = f[1]; v.po = f[2]; v.oo = f[3]; v.tabs = f[4]; v.xdrv = xdrv;
     return v;
 }
 
@@ -87,7 +87,11 @@ __device__ __forceinline__ float proj(const vg_dd2d_geom &g, const ViewGeo &v, f
                                       float b) {
     float p = v.pd * b + cp;
     if (!FAN) return p;
+#if VG_FAST_DIV
+    return __fdividef(g.DSD * p, g.DSO - (v.od * b + co));
+#else
     return g.DSD * p / (g.DSO - (v.od * b + co));
+#endif
 }
 
 // inverse of proj: driving edge coordinate b whose projection is u
@@ -111,223 +115,329 @@ __device__ __forceinline__ float det_edge(const vg_dd2d_geom &g, int j) {
 }
 
 // ---------------------------------------------------------------------------
-// Forward projection
+// Forward projection (integral form, one warp per orthogonal line)
+//
+// For one view and one orthogonal line, let f(u) be the line's pixels as a
+// piecewise-constant function of the detector coordinate (pixel m spans
+// [P_m, P_m+1], value V_m = img * line scale) and F(u) its running integral:
+//     F(u) = S_k + V_k * (u - P_k),  k the pixel under u,  S_k = sum_{m<k} V_m (P_m+1 - P_m).
+// The line's contribution to bin [U_j, U_j+1] -- the sum of img * overlap *
+// scale that vir's merge accumulates -- is F(U_j+1) - F(U_j).
+//
+// A block owns one view and FP_MAXB * 32 bins; each warp walks the lines
+// io = warp, warp + nwarps, ...: it stages the line's (P, S, V) in its own
+// shared buffer (edges projected once, S by a warp scan; __syncwarp only),
+// then every lane evaluates F at the left edges of its bins j = lane + 32 i,
+// takes right edges from the neighbouring lane, and accumulates.  The pixel
+// k under U comes from the exact inverse of the edge projection (a Moebius
+// map whose denominator does not depend on the line: its reciprocal C(U) is
+// computed once per view).  Per-warp bin sums are added in a fixed order at
+// the end: deterministic, no atomics.
 // ---------------------------------------------------------------------------
 
-constexpr int FP_THREADS = 256;
-constexpr int FP_NB = 4;  // bins per thread (strided by FP_THREADS)
-constexpr int FP_MAXL = 32;  // most lines per shared-memory chunk
+#ifndef VG_FP_MAXB
+#define VG_FP_MAXB 24
+#endif
+#ifndef VG_FP_WARPS
+#define VG_FP_WARPS 8
+#endif
+constexpr int FP_MAXB = VG_FP_MAXB;   // bins per lane (strided by 32)
+constexpr int FP_WARPS = VG_FP_WARPS; // warps per block (lines in flight)
+constexpr int FP_SEG = 16;            // pixels per lane in the line scan
+constexpr int FP_BINS = 32 * FP_MAXB; // bins per block
 
-// Shared memory per chunk line: nd + 1 projected edges and nd scaled pixels.
-__host__ __device__ inline int fp_line_floats(int nd) { return 2 * nd + 1; }
+// padded entry index: one spare entry every 16 keeps the scan's lanes (16
+// entries apart) on distinct shared-memory banks
+__host__ __device__ __forceinline__ int pad_idx(int m) { return m + (m >> 4); }
+__host__ __device__ inline int fp_line_entries(int nd) { return pad_idx(nd) + 1; }
 
 // mode 0: out = FP;  mode 1 (SIRT residual): out = (y - FP) * inv_w, or FP
 // where inv_w == 0.
 template <bool FAN>
-__global__ void __launch_bounds__(FP_THREADS, 1)
+#ifndef VG_FP_MINB
+#define VG_FP_MINB 1
+#endif
+__global__ void __launch_bounds__(FP_WARPS * 32, VG_FP_MINB)
 dd2d_fp_kernel(vg_dd2d_geom g, const float *__restrict__ img, const float *__restrict__ imgT,
                const double *__restrict__ trig, float *__restrict__ out, int mode,
-               const float *__restrict__ y, const float *__restrict__ inv_w, int L) {
-    extern __shared__ float sm[];
+               const float *__restrict__ y, const float *__restrict__ inv_w) {
+    extern __shared__ float4 smem4[];
+    __shared__ float Cs[FP_BINS + 1];
     const int ia = blockIdx.y;
     const ViewGeo v = view_geo(trig, ia);
     const int nd = v.xdrv ? g.nx : g.ny;
     const int no = v.xdrv ? g.ny : g.nx;
     const float *base = v.xdrv ? imgT : img;  // line io is contiguous in k
     const bool rev = v.pd < 0.f;               // edges decreasing in k: sweep reversed
-    const int stride = nd + 1;
-    float *P = sm;                       // [L][nd + 1] projected edges, sweep order
-    float *V = sm + (size_t)L * stride;  // [L][nd] pixel * line scale, sweep order
-    __shared__ float Lcp[FP_MAXL], Lco[FP_MAXL], Lsc[FP_MAXL];
+    const int stride = fp_line_entries(nd);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    float4 *E = smem4 + (size_t)warp * stride;  // this warp's line buffer
+    const int jbase = blockIdx.x * FP_BINS;
+    const int nb = min(FP_BINS, g.nu - jbase);  // bins of this block
+    const float half = 0.5f * (float)nd;
 
-    // this thread's bins
-    int jb[FP_NB];
-    float ul[FP_NB], ur[FP_NB];
-    int kk[FP_NB];
-    Kahan acc[FP_NB];
-#pragma unroll
-    for (int i = 0; i < FP_NB; ++i) {
-        jb[i] = blockIdx.x * FP_THREADS * FP_NB + i * FP_THREADS + threadIdx.x;
-        ul[i] = det_edge(g, jb[i]);
-        ur[i] = det_edge(g, jb[i] + 1);
-        kk[i] = -1;
-    }
-
-    for (int l0 = 0; l0 < no; l0 += L) {
-        const int nl = min(L, no - l0);
-        __syncthreads();  // previous chunk consumed
-        // per-line geometry of lines l0 .. l0 + nl - 1
-        for (int l = threadIdx.x; l < nl; l += FP_THREADS) {
-            const Line Lg = line_geo<FAN>(g, v, centre_coord(g.d_pix, l0 + l, no));
-            Lcp[l] = Lg.cp;
-            Lco[l] = Lg.co;
-            Lsc[l] = Lg.scl;
+    // line-independent factor of the inverse map at every bin edge:
+    // sweep index s(U) = (U a_l - b_l) C(U) + nd/2
+    {
+        const float sig = (rev ? -1.f : 1.f) / g.d_pix;
+        for (int e = threadIdx.x; e <= nb; e += FP_WARPS * 32) {
+            const float U = det_edge(g, jbase + e);
+            Cs[e] = FAN ? sig / (g.DSD * v.pd + U * v.od) : sig / v.pd;
         }
-        __syncthreads();
-        // projected edges and scaled pixels, sweep order
-        {
-            int l = 0, m = threadIdx.x;
-            while (m >= stride) { m -= stride; ++l; }
-            while (l < nl) {
-                const int io = l0 + l;
+    }
+    __syncthreads();
+
+    float acc[FP_MAXB];
+#pragma unroll
+    for (int i = 0; i < FP_MAXB; ++i) acc[i] = 0.f;
+
+    for (int io = warp; io < no; io += FP_WARPS) {
+        const Line Lg = line_geo<FAN>(g, v, centre_coord(g.d_pix, io, no));
+        const float la = FAN ? g.DSO - Lg.co : 1.f;       // inverse map numerator U la - lb
+        const float lb = FAN ? g.DSD * Lg.cp : Lg.cp;
+        const float *row = base + (size_t)io * nd;
+        __syncwarp();  // previous line's reads are done
+        // stage (P, S, V) of the line: lanes own FP_SEG consecutive pixels
+        float carry = 0.f;
+        for (int r0 = 0; r0 <= nd; r0 += 32 * FP_SEG) {
+            const int m0 = r0 + lane * FP_SEG;
+            float Pv[FP_SEG + 1], q[FP_SEG];
+#pragma unroll
+            for (int i = 0; i <= FP_SEG; ++i) {
+                const int m = min(m0 + i, nd);
                 const int kb = rev ? nd - m : m;
-                P[l * stride + m] = proj<FAN>(g, v, Lcp[l], Lco[l], edge_coord(g.d_pix, kb, nd));
-                if (m < nd) {
-                    const int kp = rev ? nd - 1 - m : m;
-                    V[l * nd + m] = __ldg(base + (size_t)io * nd + kp) * Lsc[l];
-                }
-                m += FP_THREADS;
-                while (m >= stride) { m -= stride; ++l; }
+                Pv[i] = proj<FAN>(g, v, Lg.cp, Lg.co, edge_coord(g.d_pix, kb, nd));
+            }
+            float tot = 0.f;
+#pragma unroll
+            for (int i = 0; i < FP_SEG; ++i) {
+                const int m = m0 + i;
+                const float V = (m < nd) ? __ldg(row + (rev ? nd - 1 - m : m)) * Lg.scl : 0.f;
+                q[i] = V;
+                tot = fmaf(V, Pv[i + 1] - Pv[i], tot);
+            }
+            float inc = tot;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const float t = __shfl_up_sync(0xffffffffu, inc, o);
+                if (lane >= o) inc += t;
+            }
+            float run = carry + inc - tot;
+            carry += __shfl_sync(0xffffffffu, inc, 31);
+#pragma unroll
+            for (int i = 0; i < FP_SEG; ++i) {
+                const int m = m0 + i;
+                if (m <= nd) E[pad_idx(m)] = make_float4(Pv[i], run, q[i], 0.f);
+                run = fmaf(q[i], Pv[i + 1] - Pv[i], run);
             }
         }
-        __syncthreads();
+        __syncwarp();
+        // F at the left edge of each of this lane's bins; right edges from lane + 1
+        // (lane 31's right edge is lane 0's next left edge)
+        float Fl[FP_MAXB + 1];
 #pragma unroll
-        for (int i = 0; i < FP_NB; ++i) {
-            if (jb[i] >= g.nu) continue;
-            const float a = ul[i], b = ur[i];
-            int k = kk[i];
-            if (k < 0) {
-                // first line: invert the edge projection to start near the bin
-                const ViewGeo vv = v;
-                const float cen = centre_coord(g.d_pix, l0, no);
-                const float cp = vv.po * cen, co = vv.oo * cen;
-                float kf = unproj<FAN>(g, vv, cp, co, a) / g.d_pix + 0.5f * nd;
-                kf = fminf(fmaxf(kf, 0.f), (float)(nd - 1));
-                k = (int)kf;
-                if (rev) k = nd - 1 - k;
+        for (int i = 0; i <= FP_MAXB; ++i) {
+            const int e = lane + 32 * i;
+            float F = 0.f;
+            if (e <= nb && (i < FP_MAXB || lane == 0)) {
+                const float U = det_edge(g, jbase + e);
+                const float sidx = fmaf(fmaf(U, la, -lb), Cs[e], half);
+                const int k = (int)fminf(fmaxf(sidx, 0.f), (float)nd);
+                const float4 t = E[pad_idx(k)];
+                F = fmaf(t.z, fmaxf(U - t.x, 0.f), t.y);
             }
-            float part = 0.f;
-            for (int l = 0; l < nl; ++l) {
-                const float *Pl = P + l * stride;
-                const float *Vl = V + l * nd;
-                // keep Pl[k] <= a < Pl[k+1] (bounded walks)
-                while (k > 0 && Pl[k] > a) --k;
-                while (k < nd - 1 && Pl[k + 1] <= a) ++k;
-                float pl = Pl[k];
-                for (int m = k; m < nd; ++m) {
-                    const float pr = Pl[m + 1];
-                    const float ov = fminf(pr, b) - fmaxf(pl, a);
-                    if (ov > 0.f) part = fmaf(Vl[m], ov, part);
-                    if (pr >= b) break;
-                    pl = pr;
-                }
-            }
-            acc[i].add(part);
-            kk[i] = k;
+            Fl[i] = F;
+        }
+#pragma unroll
+        for (int i = 0; i < FP_MAXB; ++i) {
+            const float nxt = __shfl_down_sync(0xffffffffu, Fl[i], 1);
+            const float wrap = __shfl_sync(0xffffffffu, Fl[i + 1], 0);
+            acc[i] += ((lane == 31) ? wrap : nxt) - Fl[i];
         }
     }
 
-    const float f = g.d_pix / g.du;
+    // sum the warps' partial bins in a fixed order
+    __syncthreads();
+    float *red = reinterpret_cast<float *>(smem4);  // [FP_WARPS][FP_BINS]
 #pragma unroll
-    for (int i = 0; i < FP_NB; ++i) {
-        if (jb[i] >= g.nu) continue;
-        float fp = acc[i].s * f;
-        const size_t o = (size_t)ia * g.nu + jb[i];
+    for (int i = 0; i < FP_MAXB; ++i) red[warp * FP_BINS + lane + 32 * i] = acc[i];
+    __syncthreads();
+    const float f = g.d_pix / g.du;
+    for (int e = threadIdx.x; e < nb; e += FP_WARPS * 32) {
+        float sum = 0.f;
+#pragma unroll
+        for (int w = 0; w < FP_WARPS; ++w) sum += red[w * FP_BINS + e];
+        float fp = sum * f;
+        const size_t o = (size_t)ia * g.nu + jbase + e;
         if (mode == 1) {
-            const float w = inv_w[o];
-            fp = (w != 0.f) ? (y[o] - fp) * w : fp;
+            const float wi = inv_w[o];
+            fp = (wi != 0.f) ? (y[o] - fp) * wi : fp;
         }
         out[o] = fp;
     }
 }
 
 // ---------------------------------------------------------------------------
-// Backprojection
+// Backprojection (integral form)
+//
+// For one view, let G(u) be the running integral of the sinogram row as a
+// piecewise-constant function of u (bin j spans [U_j, U_j+1]):
+//     G(u) = T_j + du sino_j (u - U_j)/du,  j = floor((u - U_0)/du),  T_j = du sum_{i<j} sino_i.
+// A pixel whose driving edges project to lo <= hi receives
+// scale(line) * (G(hi) - G(lo)) from the view -- the sum of sino * overlap *
+// scale that vir's merge distributes.  dd2d_bp_prep writes, per view, the
+// table (T_j, du sino_j) (prefix accumulated in FP64) and the line scales;
+// the main kernel evaluates G at the two projected edges of each pixel.
 // ---------------------------------------------------------------------------
 
-constexpr int BP_TY = 32;  // pixels along y (threadIdx.x, contiguous in img)
-constexpr int BP_TX = 8;   // pixels along x (threadIdx.y)
-constexpr int BP_VC = 24;  // views per chunk (static shared memory stays under 48 KiB)
-// per view: edges for the tile (X-driven: BP_TY lines x (BP_TX + 1) edges;
-// Y-driven: BP_TX lines x (BP_TY + 1) edges) and one scale per line
-constexpr int BP_EDGES = (BP_TY * (BP_TX + 1) > BP_TX * (BP_TY + 1)) ? BP_TY * (BP_TX + 1)
-                                                                     : BP_TX * (BP_TY + 1);
+#ifndef VG_BP_TY
+#define VG_BP_TY 32
+#endif
+#ifndef VG_BP_TX
+#define VG_BP_TX 8
+#endif
+#ifndef VG_BP_MINB
+#define VG_BP_MINB 1
+#endif
+constexpr int BP_TY = VG_BP_TY;  // pixels along y (threadIdx.x, contiguous in img)
+constexpr int BP_TX = VG_BP_TX;  // pixels along x (threadIdx.y)
+constexpr int BP_VC = (BP_TY * BP_TX < 128) ? BP_TY * BP_TX : 128;  // views staged per chunk
+
+struct BpWork {
+    float2 *ts;  // [na][nu + 1]: (T_j, du * sino_j)
+    float *scl;  // [na][max(nx, ny)]: line scale for the view's driving axis
+};
+
+size_t bp_ws_ts_bytes(const vg_dd2d_geom *g) {
+    return ((size_t)g->na * (g->nu + 1) * sizeof(float2) + 255) & ~(size_t)255;
+}
+size_t bp_ws_bytes(const vg_dd2d_geom *g) {
+    int nm = g->nx > g->ny ? g->nx : g->ny;
+    return bp_ws_ts_bytes(g) + (((size_t)g->na * nm * sizeof(float) + 255) & ~(size_t)255);
+}
+BpWork bp_ws(const vg_dd2d_geom *g, void *ws) {
+    BpWork w;
+    w.ts = reinterpret_cast<float2 *>(ws);
+    w.scl = reinterpret_cast<float *>(reinterpret_cast<char *>(ws) + bp_ws_ts_bytes(g));
+    return w;
+}
+
+// One block per view: prefix table of the sinogram row and line scales.
+template <bool FAN>
+__global__ void __launch_bounds__(256)
+dd2d_bp_prep(vg_dd2d_geom g, const float *__restrict__ sino, const double *__restrict__ trig,
+             BpWork w) {
+    __shared__ double wsum[8];
+    const int ia = blockIdx.x;
+    const float *row = sino + (size_t)ia * g.nu;
+    float2 *ts = w.ts + (size_t)ia * (g.nu + 1);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    // contiguous segment per thread
+    const int per = (g.nu + 255) / 256;
+    const int j0 = threadIdx.x * per;
+    double loc = 0.0;
+    for (int i = 0; i < per; ++i)
+        if (j0 + i < g.nu) loc += (double)__ldg(row + j0 + i);
+    double inc = loc;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const double t = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += t;
+    }
+    if (lane == 31) wsum[warp] = inc;
+    __syncthreads();
+    double off = 0.0;
+    for (int q = 0; q < warp; ++q) off += wsum[q];
+    double run = off + inc - loc;
+    const double du = (double)g.du;
+    for (int i = 0; i < per; ++i) {
+        const int j = j0 + i;
+        if (j < g.nu) {
+            const float sv = __ldg(row + j);
+            ts[j] = make_float2((float)(run * du), g.du * sv);
+            run += (double)sv;
+        }
+    }
+    if (threadIdx.x == 255) ts[g.nu] = make_float2((float)(run * du), 0.f);
+    // line scales of this view
+    const ViewGeo v = view_geo(trig, ia);
+    const int no = v.xdrv ? g.ny : g.nx;
+    const int nm = g.nx > g.ny ? g.nx : g.ny;
+    for (int io = threadIdx.x; io < no; io += 256)
+        w.scl[(size_t)ia * nm + io] = line_geo<FAN>(g, v, centre_coord(g.d_pix, io, no)).scl;
+}
+
+__device__ __forceinline__ float bp_G(const float2 *__restrict__ ts, int nu, float t) {
+    // t: position in bins from U_0
+    const float tc = fminf(fmaxf(t, 0.f), (float)nu);
+    const int j = min((int)tc, nu - 1);
+    const float2 e = __ldg(ts + j);
+    return fmaf(e.y, tc - (float)j, e.x);
+}
 
 // mode 0: img = BP;  mode 1 (SIRT update): x += gamma * BP * inv_w (BP where
 // inv_w == 0), written to x and its transpose xT.
 template <bool FAN>
-__global__ void __launch_bounds__(BP_TY * BP_TX)
-dd2d_bp_kernel(vg_dd2d_geom g, const float *__restrict__ sino, const double *__restrict__ trig,
+__global__ void __launch_bounds__(BP_TY * BP_TX, VG_BP_MINB)
+dd2d_bp_kernel(vg_dd2d_geom g, BpWork w, const double *__restrict__ trig,
                float *__restrict__ img, int mode, const float *__restrict__ inv_w, float gamma,
                float *__restrict__ xT) {
-    __shared__ float Ps[BP_VC][BP_EDGES];
-    __shared__ float Ss[BP_VC][BP_TY], Lcp[BP_VC][BP_TY], Lco[BP_VC][BP_TY];
-    __shared__ float Vg[BP_VC][5];
+    __shared__ float4 Vs[BP_VC];  // (pd, od, po, oo)
     __shared__ int Xs[BP_VC];
     const int tid = threadIdx.y * BP_TY + threadIdx.x;
-    const int iy0 = blockIdx.x * BP_TY, ix0 = blockIdx.y * BP_TX;
-    const int iy = iy0 + threadIdx.x, ix = ix0 + threadIdx.y;
+    const int iy = blockIdx.x * BP_TY + threadIdx.x, ix = blockIdx.y * BP_TX + threadIdx.y;
     const bool inside = iy < g.ny && ix < g.nx;
+    const int nm = g.nx > g.ny ? g.nx : g.ny;
     const float u0 = det_edge(g, 0);
     const float inv_du = 1.0f / g.du;
+    // this pixel's coordinates for either driving axis
+    const float bx = edge_coord(g.d_pix, ix, g.nx), by = edge_coord(g.d_pix, iy, g.ny);
+    const float cx = bx + 0.5f * g.d_pix, cy = by + 0.5f * g.d_pix;
     Kahan acc;
     for (int a0 = 0; a0 < g.na; a0 += BP_VC) {
         const int nv = min(BP_VC, g.na - a0);
         __syncthreads();
-        // stage 1: view geometry of the chunk
         if (tid < nv) {
             const ViewGeo v = view_geo(trig, a0 + tid);
-            Vg[tid][0] = v.pd; Vg[tid][1] = v.od; Vg[tid][2] = v.po; Vg[tid][3] = v.oo;
-            Vg[tid][4] = v.tabs;
+            Vs[tid] = make_float4(v.pd, v.od, v.po, v.oo);
             Xs[tid] = v.xdrv;
         }
         __syncthreads();
-        // stage 2: line geometry (X-driven lines are the tile's rows y, else columns x)
-        for (int e = tid; e < nv * BP_TY; e += BP_TY * BP_TX) {
-            const int vi = e / BP_TY, l = e - vi * BP_TY;
-            const ViewGeo v = vg_of(Vg[vi], Xs[vi]);
-            const int nl = v.xdrv ? BP_TY : BP_TX;
-            const int io = (v.xdrv ? iy0 : ix0) + l, no = v.xdrv ? g.ny : g.nx;
-            if (l < nl && io < no) {
-                const Line Lg = line_geo<FAN>(g, v, centre_coord(g.d_pix, io, no));
-                Lcp[vi][l] = Lg.cp; Lco[vi][l] = Lg.co; Ss[vi][l] = Lg.scl;
+        if (!inside) continue;
+        float part = 0.f;
+        for (int vi = 0; vi < nv; ++vi) {
+            const float4 q = Vs[vi];
+            const bool xd = Xs[vi];
+            const float b0 = xd ? bx : by;   // driving edge
+            const float cen = xd ? cy : cx;  // line centre
+            const int io = xd ? iy : ix;
+            const float cp = q.z * cen;
+            float p0 = fmaf(q.x, b0, cp), p1 = fmaf(q.x, b0 + g.d_pix, cp);
+            if (FAN) {
+                const float co = q.w * cen;
+                const float d0 = g.DSO - fmaf(q.y, b0, co);
+                const float d1 = g.DSO - fmaf(q.y, b0 + g.d_pix, co);
+#if VG_FAST_DIV
+                p0 = __fdividef(g.DSD * p0, d0);
+                p1 = __fdividef(g.DSD * p1, d1);
+#else
+                p0 = g.DSD * p0 / d0;
+                p1 = g.DSD * p1 / d1;
+#endif
             }
+            const float2 *ts = w.ts + (size_t)(a0 + vi) * (g.nu + 1);
+            const float t0 = (fminf(p0, p1) - u0) * inv_du, t1 = (fmaxf(p0, p1) - u0) * inv_du;
+            const float s = bp_G(ts, g.nu, t1) - bp_G(ts, g.nu, t0);
+            part = fmaf(s, __ldg(w.scl + (size_t)(a0 + vi) * nm + io), part);
         }
-        __syncthreads();
-        // stage 3: the tile's projected driving edges per view
-        for (int e = tid; e < nv * BP_EDGES; e += BP_TY * BP_TX) {
-            const int vi = e / BP_EDGES, q = e - vi * BP_EDGES;
-            const ViewGeo v = vg_of(Vg[vi], Xs[vi]);
-            int nd, no, nl, ne;
-            if (v.xdrv) { nl = BP_TY; ne = BP_TX + 1; nd = g.nx; no = g.ny; }
-            else        { nl = BP_TX; ne = BP_TY + 1; nd = g.ny; no = g.nx; }
-            if (q >= nl * ne) continue;
-            const int l = q / ne, b = q - l * ne;
-            const int io = (v.xdrv ? iy0 : ix0) + l;
-            const int k = (v.xdrv ? ix0 : iy0) + b;
-            if (io >= no || k > nd) { Ps[vi][q] = 0.f; continue; }
-            Ps[vi][q] = proj<FAN>(g, v, Lcp[vi][l], Lco[vi][l], edge_coord(g.d_pix, k, nd));
-        }
-        __syncthreads();
-        if (inside) {
-            for (int vi = 0; vi < nv; ++vi) {
-                const bool xd = Xs[vi];
-                const int l = xd ? threadIdx.x : threadIdx.y;
-                const int b = xd ? threadIdx.y : threadIdx.x;
-                const int ne = xd ? BP_TX + 1 : BP_TY + 1;
-                const float pa = Ps[vi][l * ne + b], pb = Ps[vi][l * ne + b + 1];
-                const float lo = fminf(pa, pb), hi = fmaxf(pa, pb);
-                const float *row = sino + (size_t)(a0 + vi) * g.nu;
-                int j = max(0, (int)floorf((lo - u0) * inv_du));
-                float s = 0.f;
-                float el = det_edge(g, j);
-                for (; j < g.nu; ++j) {
-                    const float er = det_edge(g, j + 1);
-                    const float ov = fminf(hi, er) - fmaxf(lo, el);
-                    if (ov > 0.f) s = fmaf(__ldg(row + j), ov, s);
-                    if (er >= hi) break;
-                    el = er;
-                }
-                acc.add(s * Ss[vi][l]);
-            }
-        }
+        acc.add(part);
     }
     if (!inside) return;
     const float bp = acc.s / ((float)g.na * g.d_pix);
     const size_t o = (size_t)ix * g.ny + iy;
     if (mode == 1) {
-        const float w = inv_w[o];
-        const float upd = (w != 0.f) ? bp * w : bp;
+        const float wi = inv_w[o];
+        const float upd = (wi != 0.f) ? bp * wi : bp;
         const float xn = img[o] + gamma * upd;
         img[o] = xn;
         xT[(size_t)iy * g.nx + ix] = xn;
@@ -354,14 +464,6 @@ int check_geom(const vg_dd2d_geom *g) {
     return VG_OK;
 }
 
-// Lines per shared-memory chunk of the FP: as many as fit in FP_SMEM bytes.
-constexpr int FP_SMEM = 48 * 1024;
-int fp_chunk_lines(const vg_dd2d_geom *g) {
-    int nd = g->nx > g->ny ? g->nx : g->ny;
-    int L = FP_SMEM / (fp_line_floats(nd) * (int)sizeof(float));
-    return L < 1 ? 1 : (L > FP_MAXL ? FP_MAXL : L);
-}
-
 template <bool FAN>
 int set_fp_smem(size_t bytes) {
     static size_t done = 0;
@@ -375,31 +477,41 @@ int set_fp_smem(size_t bytes) {
 
 int launch_fp(const vg_dd2d_geom *g, const float *img, const float *imgT, const double *trig,
               float *out, int mode, const float *y, const float *inv_w, cudaStream_t st) {
-    const int L = fp_chunk_lines(g);
     const int nd = g->nx > g->ny ? g->nx : g->ny;
-    const size_t smem = (size_t)L * fp_line_floats(nd) * sizeof(float);
-    VG_REQUIRE(smem <= 200 * 1024, "dd2d_fp: image side too large for one line in shared memory");
-    dim3 grid(ceil_div(g->nu, FP_THREADS * FP_NB), g->na);
+    size_t smem = (size_t)FP_WARPS * fp_line_entries(nd) * sizeof(float4);
+    const size_t red = (size_t)FP_WARPS * FP_BINS * sizeof(float);
+    if (smem < red) smem = red;
+    VG_REQUIRE(smem <= 200 * 1024, "dd2d_fp: image side too large for the line buffers");
+    dim3 grid(ceil_div(g->nu, FP_BINS), g->na);
     int s = g->fan ? set_fp_smem<true>(smem) : set_fp_smem<false>(smem);
     if (s) return s;
     if (g->fan)
-        dd2d_fp_kernel<true><<<grid, FP_THREADS, smem, st>>>(*g, img, imgT, trig, out, mode, y,
-                                                            inv_w, L);
+        dd2d_fp_kernel<true><<<grid, FP_WARPS * 32, smem, st>>>(*g, img, imgT, trig, out, mode,
+                                                               y, inv_w);
     else
-        dd2d_fp_kernel<false><<<grid, FP_THREADS, smem, st>>>(*g, img, imgT, trig, out, mode, y,
-                                                             inv_w, L);
+        dd2d_fp_kernel<false><<<grid, FP_WARPS * 32, smem, st>>>(*g, img, imgT, trig, out, mode,
+                                                                y, inv_w);
     return launch_status("dd2d_fp");
 }
 
 int launch_bp(const vg_dd2d_geom *g, const float *sino, const double *trig, float *img, int mode,
-              const float *inv_w, float gamma, float *xT, cudaStream_t st) {
+              const float *inv_w, float gamma, float *xT, void *ws, size_t ws_bytes,
+              cudaStream_t st) {
+    VG_REQUIRE(ws != nullptr && ws_bytes >= bp_ws_bytes(g),
+               "dd2d_bp: workspace of %zu bytes needed (vg_dd2d_workspace_bytes)", bp_ws_bytes(g));
+    VG_REQUIRE(((uintptr_t)ws & 255) == 0, "dd2d_bp: workspace must be 256-byte aligned");
+    const BpWork w = bp_ws(g, ws);
+    if (g->fan) dd2d_bp_prep<true><<<g->na, 256, 0, st>>>(*g, sino, trig, w);
+    else        dd2d_bp_prep<false><<<g->na, 256, 0, st>>>(*g, sino, trig, w);
+    int s = launch_status("dd2d_bp_prep");
+    if (s) return s;
     dim3 grid(ceil_div(g->ny, BP_TY), ceil_div(g->nx, BP_TX));
     VG_REQUIRE(grid.y < 65536, "dd2d_bp: nx too large");
     dim3 block(BP_TY, BP_TX);
     if (g->fan)
-        dd2d_bp_kernel<true><<<grid, block, 0, st>>>(*g, sino, trig, img, mode, inv_w, gamma, xT);
+        dd2d_bp_kernel<true><<<grid, block, 0, st>>>(*g, w, trig, img, mode, inv_w, gamma, xT);
     else
-        dd2d_bp_kernel<false><<<grid, block, 0, st>>>(*g, sino, trig, img, mode, inv_w, gamma, xT);
+        dd2d_bp_kernel<false><<<grid, block, 0, st>>>(*g, w, trig, img, mode, inv_w, gamma, xT);
     return launch_status("dd2d_bp");
 }
 
@@ -413,22 +525,29 @@ extern "C" int vg_dd2d_fp(const vg_dd2d_geom *g, const float *img, const float *
     return launch_fp(g, img, imgT, trig, sino, 0, nullptr, nullptr, as_stream(stream));
 }
 
+extern "C" size_t vg_dd2d_workspace_bytes(const vg_dd2d_geom *g) {
+    if (check_geom(g)) return 0;
+    return bp_ws_bytes(g);
+}
+
 extern "C" int vg_dd2d_bp(const vg_dd2d_geom *g, const float *sino, const double *trig,
-                          float *img, void *stream) {
+                          float *img, void *workspace, size_t workspace_bytes, void *stream) {
     int st = check_geom(g);
     if (st) return st;
     VG_REQUIRE(img && trig && sino, "dd2d_bp: null pointer");
-    return launch_bp(g, sino, trig, img, 0, nullptr, 0.f, nullptr, as_stream(stream));
+    return launch_bp(g, sino, trig, img, 0, nullptr, 0.f, nullptr, workspace, workspace_bytes,
+                     as_stream(stream));
 }
 
 extern "C" int vg_dd2d_sirt_iter(const vg_dd2d_geom *g, const float *y, const float *inv_w_sino,
                                  const float *inv_w_img, float gamma, const double *trig,
-                                 float *x, float *xT, float *r, void *stream) {
+                                 float *x, float *xT, float *r, void *workspace,
+                                 size_t workspace_bytes, void *stream) {
     int st = check_geom(g);
     if (st) return st;
     VG_REQUIRE(y && inv_w_sino && inv_w_img && trig && x && xT && r, "dd2d_sirt_iter: null pointer");
     cudaStream_t s = as_stream(stream);
     st = launch_fp(g, x, xT, trig, r, 1, y, inv_w_sino, s);
     if (st) return st;
-    return launch_bp(g, r, trig, x, 1, inv_w_img, gamma, xT, s);
+    return launch_bp(g, r, trig, x, 1, inv_w_img, gamma, xT, workspace, workspace_bytes, s);
 }

@@ -27,7 +27,7 @@ import numpy as np
 import torch
 
 from . import _core
-from ._lib import DD2DGeom, call
+from ._lib import DD2DGeom, call, dd2d_workspace
 from .filtration import filter_rows_device
 
 
@@ -58,7 +58,7 @@ class SIRT2D:
             raise ValueError("sino rows must equal len(ang_arr)")
         self.g = _geom(nx, ny, na, nu, du, su, d_pix, DSO, DSD, self.fan)
         self.gamma = float(gamma)
-        st = _core.stream(self.dev)
+        self.ws = dd2d_workspace(self.g, self.dev)
         if W_sino is None:
             ones = torch.ones((nx, ny), dtype=torch.float32, device=self.dev)
             W_sino = self.fp(ones)
@@ -75,7 +75,6 @@ class SIRT2D:
         self.r = torch.empty((na, nu), dtype=torch.float32, device=self.dev)
         self._graph = None
         self._graph_n = 0
-        del st
 
     # projector pair on this geometry
     def fp(self, img: torch.Tensor) -> torch.Tensor:
@@ -88,13 +87,14 @@ class SIRT2D:
     def bp(self, sino: torch.Tensor) -> torch.Tensor:
         out = torch.empty((self.g.nx, self.g.ny), dtype=torch.float32, device=self.dev)
         call("vg_dd2d_bp", ctypes.byref(self.g), _core.ptr(sino), _core.ptr(self.trig),
-             _core.ptr(out), _core.stream(self.dev))
+             _core.ptr(out), _core.ptr(self.ws), self.ws.numel(), _core.stream(self.dev))
         return out
 
     def _iter(self):
         call("vg_dd2d_sirt_iter", ctypes.byref(self.g), _core.ptr(self.y), _core.ptr(self.inv_ws),
              _core.ptr(self.inv_wi), ctypes.c_float(self.gamma), _core.ptr(self.trig),
-             _core.ptr(self.x), _core.ptr(self.xT), _core.ptr(self.r), _core.stream(self.dev))
+             _core.ptr(self.x), _core.ptr(self.xT), _core.ptr(self.r), _core.ptr(self.ws),
+             self.ws.numel(), _core.stream(self.dev))
 
     def capture(self, n: int):
         """Capture ``n`` updates as one CUDA graph (replayed by run())."""

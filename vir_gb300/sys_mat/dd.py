@@ -24,7 +24,7 @@ import ctypes
 import numpy as np
 
 from .. import _core
-from .._lib import DD2DGeom, call
+from .._lib import DD2DGeom, call, dd2d_workspace
 
 
 def _geom(nx, ny, na, nu, du, su, d_pix, DSO=0.0, DSD=0.0, fan=0):
@@ -59,8 +59,9 @@ def _bp(sino, ang_arr, img_shape, du, su, d_pix, DSO, DSD, fan):
     nx, ny = (int(v) for v in img_shape)
     g = _geom(nx, ny, na, y.shape[1], du, su, d_pix, DSO, DSD, fan)
     img = _core.empty((nx, ny), dev)
+    ws = dd2d_workspace(g, dev)
     call("vg_dd2d_bp", ctypes.byref(g), _core.ptr(y), _core.ptr(trig), _core.ptr(img),
-         _core.stream(dev))
+         _core.ptr(ws), ws.numel(), _core.stream(dev))
     return _core.to_host_like(img, sino)
 
 
