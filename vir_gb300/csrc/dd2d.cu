@@ -155,14 +155,14 @@ __host__ __device__ inline int fp_line_entries(int nd) { return pad_idx(nd) + 1;
 // where inv_w == 0.
 template <bool FAN>
 #ifndef VG_FP_MINB
-#define VG_FP_MINB 1
+#define VG_FP_MINB 2
 #endif
 __global__ void __launch_bounds__(FP_WARPS * 32, VG_FP_MINB)
 dd2d_fp_kernel(vg_dd2d_geom g, const float *__restrict__ img, const float *__restrict__ imgT,
                const double *__restrict__ trig, float *__restrict__ out, int mode,
                const float *__restrict__ y, const float *__restrict__ inv_w) {
     extern __shared__ float4 smem4[];
-    __shared__ float Cs[FP_BINS + 1];
+    __shared__ float2 UC[FP_BINS + 32];  // per bin edge (U, C(U)); entries past nb repeat nb
     const int ia = blockIdx.y;
     const ViewGeo v = view_geo(trig, ia);
     const int nd = v.xdrv ? g.nx : g.ny;
@@ -180,9 +180,9 @@ dd2d_fp_kernel(vg_dd2d_geom g, const float *__restrict__ img, const float *__res
     // sweep index s(U) = (U a_l - b_l) C(U) + nd/2
     {
         const float sig = (rev ? -1.f : 1.f) / g.d_pix;
-        for (int e = threadIdx.x; e <= nb; e += FP_WARPS * 32) {
-            const float U = det_edge(g, jbase + e);
-            Cs[e] = FAN ? sig / (g.DSD * v.pd + U * v.od) : sig / v.pd;
+        for (int e = threadIdx.x; e < FP_BINS + 32; e += FP_WARPS * 32) {
+            const float U = det_edge(g, jbase + min(e, nb));
+            UC[e] = make_float2(U, FAN ? sig / (g.DSD * v.pd + U * v.od) : sig / v.pd);
         }
     }
     __syncthreads();
@@ -198,21 +198,23 @@ dd2d_fp_kernel(vg_dd2d_geom g, const float *__restrict__ img, const float *__res
         const float *row = base + (size_t)io * nd;
         __syncwarp();  // previous line's reads are done
         // stage (P, S, V) of the line: lanes own FP_SEG consecutive pixels
+        // (edge coordinate b0 + i db along a lane's segment)
+        const float db = rev ? -g.d_pix : g.d_pix;
         float carry = 0.f;
         for (int r0 = 0; r0 <= nd; r0 += 32 * FP_SEG) {
             const int m0 = r0 + lane * FP_SEG;
+            const float b0 = edge_coord(g.d_pix, rev ? nd - m0 : m0, nd);
             float Pv[FP_SEG + 1], q[FP_SEG];
 #pragma unroll
-            for (int i = 0; i <= FP_SEG; ++i) {
-                const int m = min(m0 + i, nd);
-                const int kb = rev ? nd - m : m;
-                Pv[i] = proj<FAN>(g, v, Lg.cp, Lg.co, edge_coord(g.d_pix, kb, nd));
-            }
+            for (int i = 0; i <= FP_SEG; ++i)
+                Pv[i] = proj<FAN>(g, v, Lg.cp, Lg.co, fmaf((float)i, db, b0));
+            // pixels m0 .. m0 + FP_SEG - 1 (sweep order), clamped reads past nd
+            const float *px = row + (rev ? nd - 1 - m0 : m0);
+            const int step = rev ? -1 : 1;
             float tot = 0.f;
 #pragma unroll
             for (int i = 0; i < FP_SEG; ++i) {
-                const int m = m0 + i;
-                const float V = (m < nd) ? __ldg(row + (rev ? nd - 1 - m : m)) * Lg.scl : 0.f;
+                const float V = (m0 + i < nd) ? __ldg(px + i * step) * Lg.scl : 0.f;
                 q[i] = V;
                 tot = fmaf(V, Pv[i + 1] - Pv[i], tot);
             }
@@ -224,10 +226,11 @@ dd2d_fp_kernel(vg_dd2d_geom g, const float *__restrict__ img, const float *__res
             }
             float run = carry + inc - tot;
             carry += __shfl_sync(0xffffffffu, inc, 31);
+            float4 *Es = E + pad_idx(m0);  // m0 is a multiple of 16: entries m0+i are contiguous
+            const int lim = nd - m0;        // entries m0 + i with i <= lim exist
 #pragma unroll
             for (int i = 0; i < FP_SEG; ++i) {
-                const int m = m0 + i;
-                if (m <= nd) E[pad_idx(m)] = make_float4(Pv[i], run, q[i], 0.f);
+                if (i <= lim) Es[i] = make_float4(Pv[i], run, q[i], 0.f);
                 run = fmaf(q[i], Pv[i + 1] - Pv[i], run);
             }
         }
@@ -237,16 +240,11 @@ dd2d_fp_kernel(vg_dd2d_geom g, const float *__restrict__ img, const float *__res
         float Fl[FP_MAXB + 1];
 #pragma unroll
         for (int i = 0; i <= FP_MAXB; ++i) {
-            const int e = lane + 32 * i;
-            float F = 0.f;
-            if (e <= nb && (i < FP_MAXB || lane == 0)) {
-                const float U = det_edge(g, jbase + e);
-                const float sidx = fmaf(fmaf(U, la, -lb), Cs[e], half);
-                const int k = (int)fminf(fmaxf(sidx, 0.f), (float)nd);
-                const float4 t = E[pad_idx(k)];
-                F = fmaf(t.z, fmaxf(U - t.x, 0.f), t.y);
-            }
-            Fl[i] = F;
+            const float2 uc = UC[lane + 32 * i];  // padded past nb with the last edge
+            const float sidx = fmaf(fmaf(uc.x, la, -lb), uc.y, half);
+            const int k = (int)fminf(fmaxf(sidx, 0.f), (float)nd);
+            const float4 t = E[pad_idx(k)];
+            Fl[i] = fmaf(t.z, fmaxf(uc.x - t.x, 0.f), t.y);
         }
 #pragma unroll
         for (int i = 0; i < FP_MAXB; ++i) {
