@@ -18,3 +18,31 @@ def load():
     """Build (if needed) and load libvirgpu.so; returns the ctypes handle."""
     from ._lib import load as _load
     return _load()
+
+
+# vir module -> {function name: replacement "module:attr" in this package}
+_DROP_INS = {
+    "sys_mat.dd": {n: "vir_gb300.sys_mat.dd:" + n for n in
+                   ("dd_fp_par_2d", "dd_bp_par_2d", "dd_fp_fan_2d", "dd_bp_fan_2d")},
+    "sys_mat.fp_2d_par": {"siddons_fp_2d": "vir_gb300.sys_mat.fp_2d_par:siddons_fp_2d"},
+    "filtration": {"filter_sino": "vir_gb300.filtration:filter_sino"},
+}
+
+
+def install_into(vir_pkg):
+    """Opt-in monkeypatch: replace vir's functions on the hot path with the
+    GPU drop-ins of this package (same signatures, layouts and scales).
+    ``vir_pkg`` is the imported ``vir`` package; returns the list of
+    replaced "module.function" names."""
+    import importlib
+    done = []
+    for mod, fns in _DROP_INS.items():
+        try:
+            target = importlib.import_module(vir_pkg.__name__ + "." + mod)
+        except ImportError:
+            continue
+        for name, spec in fns.items():
+            m, a = spec.split(":")
+            setattr(target, name, getattr(importlib.import_module(m), a))
+            done.append(f"{mod}.{name}")
+    return done
