@@ -107,6 +107,21 @@ int vg_dd2d_bp(const vg_dd2d_geom *g, const float *sino, const double *trig,
                float *img, void *workspace, size_t workspace_bytes,
                void *stream);
 
+/* vg_dd2d_bp without a caller workspace, for callers that cannot allocate
+ * device memory when they call (a host that owns a fixed memory budget, a
+ * loop that cannot afford cudaMalloc's implicit synchronisation, a plugin
+ * host that forbids allocation in callbacks).  No counterpart in vir: it is
+ * an addition of this library.  The workspace is a fixed 32 MiB array in
+ * the library's device memory (vg_dd2d_noalloc_scratch_bytes()), held on
+ * every device that loads the library until exit; geometries needing more
+ * are rejected with VG_ERR_ARG.  The first call on a device (that device
+ * current) looks the array's address up and should come before any stream
+ * capture.  All calls share the array: calls that overlap on the GPU race.
+ * Nothing in the array needs clearing between calls. */
+int vg_dd2d_bp_noalloc(const vg_dd2d_geom *g, const float *sino,
+                       const double *trig, float *img, void *stream);
+size_t vg_dd2d_noalloc_scratch_bytes(void);
+
 /* One SIRT update on the same projector pair, both halves fused
  * (sys_mat/sirt_dd.py:51-72):
  *   r   = (y - FP x) * inv_w_sino  (FP x kept where inv_w_sino == 0)

@@ -47,6 +47,7 @@ _PROTOS = {
                    c_void_p],
     "vg_dd2d_sirt_iter": [ctypes.POINTER(DD2DGeom), c_void_p, c_void_p, c_void_p, c_float,
                           c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_size_t, c_void_p],
+    "vg_dd2d_bp_noalloc": [ctypes.POINTER(DD2DGeom), c_void_p, c_void_p, c_void_p, c_void_p],
     "vg_fbp2d_bp": [ctypes.POINTER(DD2DGeom), c_void_p, c_void_p, c_void_p, c_void_p],
     "vg_transpose": [c_void_p, c_int, c_int, c_void_p, c_void_p],
     "vg_filter_rows": [c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p],
@@ -78,6 +79,8 @@ def load(build_if_missing: bool = True):
             fn.restype = c_int
         L.vg_dd2d_workspace_bytes.argtypes = [ctypes.POINTER(DD2DGeom)]
         L.vg_dd2d_workspace_bytes.restype = c_size_t
+        L.vg_dd2d_noalloc_scratch_bytes.argtypes = []
+        L.vg_dd2d_noalloc_scratch_bytes.restype = c_size_t
         _lib = L
         return L
 
@@ -93,7 +96,7 @@ def call(name, *args):
 
 def exported_symbols():
     return list(_PROTOS) + ["vg_version", "vg_last_error", "vg_status_string",
-                            "vg_dd2d_workspace_bytes"]
+                            "vg_dd2d_workspace_bytes", "vg_dd2d_noalloc_scratch_bytes"]
 
 
 def dd2d_workspace(g, dev):

@@ -549,3 +549,78 @@ extern "C" int vg_dd2d_sirt_iter(const vg_dd2d_geom *g, const float *y, const fl
     if (st) return st;
     return launch_bp(g, r, trig, x, 1, inv_w_img, gamma, xT, workspace, workspace_bytes, s);
 }
+
+// ---------------------------------------------------------------------------
+// Allocation-free backprojection.
+//
+// Some callers cannot allocate device memory at call time: a host
+// application that hands this library a fixed memory budget and owns every
+// allocation itself, code running where cudaMalloc's implicit device
+// synchronisation is not acceptable (a real-time acquisition loop), or a
+// plugin whose host forbids allocation inside its callbacks.  For them
+// vg_dd2d_bp_noalloc does the same backprojection as vg_dd2d_bp with the
+// workspace taken from a fixed array in device memory that is part of this
+// library (VG_NOALLOC_SCRATCH_BYTES = 32 MiB, held on every device that
+// loads the library until the process exits).
+//
+// - The caller still passes the sinogram and the output image.
+// - Geometries whose workspace (vg_dd2d_workspace_bytes) exceeds 32 MiB are
+//   rejected with VG_ERR_ARG.
+// - The first call on a device, with that device current, looks up the
+//   array's device address (cudaGetSymbolAddress) and caches it; make that
+//   first call before any stream capture.
+// - Every call shares the one array: calls whose executions overlap on the
+//   GPU (different streams, or concurrent host threads) race and corrupt
+//   each other's results.  Serialise them, e.g. on one stream.
+// - Each call rewrites every workspace entry it later reads, so the array's
+//   leftover contents from an earlier call do not matter and nothing needs
+//   clearing.
+// ---------------------------------------------------------------------------
+
+#define VG_NOALLOC_SCRATCH_BYTES (32u << 20)
+#define VG_NOALLOC_MAX_DEVICES 64
+
+static __device__ __align__(256) unsigned char g_dd2d_scratch[VG_NOALLOC_SCRATCH_BYTES];
+
+#include <mutex>
+
+namespace {
+std::mutex g_scratch_mu;
+void *g_scratch_addr[VG_NOALLOC_MAX_DEVICES] = {};
+
+// Device address of g_dd2d_scratch on the current device (looked up once).
+int scratch_address(void **out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_status(e, "dd2d_bp_noalloc: cudaGetDevice");
+    VG_REQUIRE(dev >= 0 && dev < VG_NOALLOC_MAX_DEVICES, "dd2d_bp_noalloc: device %d out of range", dev);
+    std::lock_guard<std::mutex> lk(g_scratch_mu);
+    if (!g_scratch_addr[dev]) {
+        void *p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_dd2d_scratch);
+        if (e != cudaSuccess) return cuda_status(e, "dd2d_bp_noalloc: cudaGetSymbolAddress");
+        g_scratch_addr[dev] = p;
+    }
+    *out = g_scratch_addr[dev];
+    return VG_OK;
+}
+}  // namespace
+
+extern "C" size_t vg_dd2d_noalloc_scratch_bytes(void) { return VG_NOALLOC_SCRATCH_BYTES; }
+
+extern "C" int vg_dd2d_bp_noalloc(const vg_dd2d_geom *g, const float *sino, const double *trig,
+                                  float *img, void *stream) {
+    int st = check_geom(g);
+    if (st) return st;
+    VG_REQUIRE(img && trig && sino, "dd2d_bp_noalloc: null pointer");
+    const size_t need = bp_ws_bytes(g);
+    VG_REQUIRE(need <= VG_NOALLOC_SCRATCH_BYTES,
+               "dd2d_bp_noalloc: this geometry needs %zu bytes of workspace, above the fixed "
+               "%u-byte scratch; use vg_dd2d_bp with a caller workspace",
+               need, (unsigned)VG_NOALLOC_SCRATCH_BYTES);
+    void *ws = nullptr;
+    st = scratch_address(&ws);
+    if (st) return st;
+    return launch_bp(g, sino, trig, img, 0, nullptr, 0.f, nullptr, ws, VG_NOALLOC_SCRATCH_BYTES,
+                     as_stream(stream));
+}
