@@ -71,6 +71,54 @@ int vg_siddon2d_trace(int nx, int ny, const double *trig, int na, int n_dets,
                       double d_det, double d_pix, int *count,
                       unsigned long long *hash, double *len, void *stream);
 
+/* ---- Siddon ray lists (3D) ------------------------------------------------ */
+
+/* Per-ray set-up of sys_mat/siddon.py:siddons (computed on the host in the
+ * reference's numpy arithmetic, :681-751) and the grid planes; all arrays are
+ * device pointers.  src/dst are (n_rays, 3) float32 source and target-source
+ * vectors, dist the float32 ray length, amin/amax the alpha range, i0/iN the
+ * per-axis plane index range [i0, iN), valid the rays that cross the grid. */
+typedef struct {
+    int n_rays;
+    int nx, ny, nz;
+    float dx, dy, dz;
+    const float *xb, *yb, *zb;         /* plane coordinates, n + 1 each */
+    const float *src, *dst;            /* (n_rays, 3) */
+    const float *dist, *amin, *amax;   /* (n_rays) */
+    const int *i0, *iN;                /* (n_rays, 3) */
+    const unsigned char *valid;        /* (n_rays) */
+} vg_siddon_rays;
+
+/* Pass 1 of siddons (the per-ray loop, sys_mat/siddon.py:754-826): number
+ * of kept (voxel, length) entries per ray into counts (n_rays ints); *err
+ * (device int, caller-zeroed) is incremented for every ray with a voxel
+ * index outside the grid (where the reference's ravel_multi_index raises). */
+int vg_siddons_count(const vg_siddon_rays *r, int *counts, int *err,
+                     void *stream);
+
+/* Pass 2: the entries themselves, ray by ray at off[ray] (the exclusive scan
+ * of the counts): ind = raveled C-order voxel index (int32), len = float32
+ * intersection length -- the flat (ind, len, off) form of siddons(flat=True). */
+int vg_siddons_fill(const vg_siddon_rays *r, const int *off, int *ind,
+                    float *len, void *stream);
+
+/* List forward projection sino[r] (+)= sum_i x[ind[i]] * len[i] over
+ * i in [off[r], off[r+1]): forward_proj_ravel_rays_struct
+ * (projection/projection_c.c:150-157) and proj.sd_f_proj (proj.py:56-96).
+ * One warp per ray, Kahan sums; accumulate != 0 adds to sino like the C. */
+int vg_list_fp(const float *x, const int *ind, const float *len,
+               const int *off, int nrays, float *sino, int accumulate,
+               void *stream);
+
+/* List backprojection x[ind[i]] (+)= sino[r] * len[i]:
+ * back_proj_ravel_rays_struct (projection/projection_c.c:200-208), with
+ * repeated voxels accumulated (np.add.at semantics).  FP64 atomics into a
+ * workspace of vg_list_bp_workspace_bytes(nvox) bytes, then one rounding. */
+size_t vg_list_bp_workspace_bytes(int nvox);
+int vg_list_bp(const float *sino, const int *ind, const float *len,
+               const int *off, int nrays, int nvox, float *x, int accumulate,
+               void *workspace, size_t workspace_bytes, void *stream);
+
 /* ---- 2D distance-driven (parallel and flat-detector fan) --------------- */
 
 /* Geometry of one 2D distance-driven call.  fan = 0: parallel

@@ -1,0 +1,103 @@
+"""GPU Siddon lists (siddons) and list projection against the reference's
+golden lists, the reference's C list projector and the oracle."""
+import ctypes
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("case", ["siddons_edge", "siddons_par", "siddons_cone"])
+def test_siddons_flat_bit_exact(vg, golden, case):
+    from vir_gb300.sys_mat import siddon
+    g = golden[case]
+    ind, ln, off = siddon.siddons(g["src"], g["trg"], g["nPixels"], g["dPixels"], flat=True)
+    assert np.array_equal(off, g["off"])
+    assert np.array_equal(ind, g["ind"])
+    assert np.array_equal(ln, g["len"])   # same float32 bits
+
+
+def test_siddons_object_forms(vg, golden):
+    from vir_gb300.sys_mat import siddon
+    g = golden["siddons_par"]
+    rays = siddon.siddons(g["src"], g["trg"], g["nPixels"], g["dPixels"], ravel=True)
+    assert rays.shape == g["src"].shape[:-1]
+    flat = rays.reshape(-1)
+    for r in range(flat.size):
+        a, b = g["off"][r], g["off"][r + 1]
+        if a == b:
+            assert flat[r] is None
+        else:
+            assert np.array_equal(flat[r][0], g["ind"][a:b])
+            assert np.array_equal(flat[r][1], g["len"][a:b])
+    un = siddon.siddons(g["src"], g["trg"], g["nPixels"], g["dPixels"], ravel=False)
+    r = next(i for i in range(flat.size) if flat[i] is not None)
+    x, y, z = np.unravel_index(flat[r][0], tuple(g["nPixels"]))
+    assert np.array_equal(un.reshape(-1)[r][0], x) and np.array_equal(un.reshape(-1)[r][2], z)
+
+
+def test_list_projection_vs_reference_c(vg, golden):
+    """proj.sd_f_proj / sd_b_proj on the GPU against projection_c.c's output."""
+    from vir_gb300.projection import proj
+    d, c = golden["siddons_cone"], golden["list_c"]
+    lst = (d["ind"], d["len"], d["off"])
+    fp = proj.sd_f_proj(c["phantom"], lst, flat=True)
+    assert np.abs(fp - c["sino"]).max() <= 2e-6 * np.abs(c["sino"]).max()
+    bp = proj.sd_b_proj(c["y"], lst, c["phantom"].shape)
+    assert np.abs(bp - c["bp"]).max() <= 2e-6 * np.abs(c["bp"]).max()
+
+
+def test_list_c1_scale_vs_oracle(vg, orc):
+    """Config C1 geometry through siddons (GPU) and list FP/BP vs the oracle."""
+    import torch
+    from vir_gb300.projection import proj
+    from vir_gb300.sys_mat import siddon
+    dets = np.arange(367) - 183.0
+    views = np.linspace(0, np.pi, 180, endpoint=False)
+    # proj_geom.geom_circular(..., geom="par") restated: rays along x rotated by each view
+    src = np.zeros((180, 367, 3)); trg = np.zeros((180, 367, 3))
+    for i, v in enumerate(views):
+        c, s = np.cos(v), np.sin(v)
+        R = np.array([[c, s], [-s, c]])
+        src[i, :, :2] = np.stack([np.full(367, -36700.0), dets], -1) @ R
+        trg[i, :, :2] = np.stack([np.full(367, 36700.0), dets], -1) @ R
+    ind, ln, off, shape, grid = siddon.siddons_device(src, trg, (256, 256, 1), 1.0)
+    assert off.numel() == 180 * 367 + 1 and ind.numel() > 14_000_000
+    x = np.random.default_rng(3).random((256, 256, 1)).astype(np.float32)
+    fp = proj.list_fp_device(torch.from_numpy(x).cuda().reshape(-1), ind, ln, off).cpu().numpy()
+    ih, lh, oh = ind.cpu().numpy(), ln.cpu().numpy(), off.cpu().numpy()
+    fo = orc.list_fp(x, ih, lh, oh)
+    assert np.abs(fp - fo).max() <= 2e-6 * np.abs(fo).max()
+    y = np.random.default_rng(4).random(fp.size).astype(np.float32)
+    bp = proj.list_bp_device(torch.from_numpy(y).cuda(), ind, ln, off, x.size).cpu().numpy()
+    bo = orc.list_bp(y, ih, lh, oh, x.size)
+    assert np.abs(bp - bo).max() <= 2e-6 * np.abs(bo).max()
+
+
+class _RaveledRay(ctypes.Structure):   # mpct.RaveledRay layout (mpct.py:103-106)
+    _fields_ = [("n", ctypes.c_int), ("R", ctypes.POINTER(ctypes.c_int)),
+                ("L", ctypes.POINTER(ctypes.c_float))]
+
+
+def test_ctypes_list_entry_points(vg, golden):
+    """proj_ctype.sd_f_proj_c / sd_b_proj_c accumulate in place like the C."""
+    from vir_gb300.projection import proj_ctype
+    d, c = golden["siddons_cone"], golden["list_c"]
+    nr = d["off"].size - 1
+    rays = (_RaveledRay * nr)()
+    keep = []
+    for r in range(nr):
+        a, b = d["off"][r], d["off"][r + 1]
+        R = np.ascontiguousarray(d["ind"][a:b], np.int32)
+        L = np.ascontiguousarray(d["len"][a:b], np.float32)
+        keep += [R, L]
+        rays[r].n = int(b - a)
+        rays[r].R = R.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+        rays[r].L = L.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+    sino = np.ones(nr, np.float32)                 # accumulates onto existing contents
+    proj_ctype.sd_f_proj_c(c["phantom"].copy(), sino, rays)
+    assert np.abs(sino - 1.0 - c["sino"]).max() <= 2e-6 * np.abs(c["sino"]).max()
+    ph = np.zeros(c["phantom"].shape, np.float32)
+    proj_ctype.sd_b_proj_c(ph, c["y"].copy(), rays)
+    assert np.abs(ph - c["bp"]).max() <= 2e-6 * np.abs(c["bp"]).max()

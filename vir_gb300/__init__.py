@@ -26,6 +26,10 @@ _DROP_INS = {
                    ("dd_fp_par_2d", "dd_bp_par_2d", "dd_fp_fan_2d", "dd_bp_fan_2d")},
     "sys_mat.fp_2d_par": {"siddons_fp_2d": "vir_gb300.sys_mat.fp_2d_par:siddons_fp_2d"},
     "filtration": {"filter_sino": "vir_gb300.filtration:filter_sino"},
+    "sys_mat.siddon": {"siddons": "vir_gb300.sys_mat.siddon:siddons"},
+    "projection.proj": {n: "vir_gb300.projection.proj:" + n for n in ("sd_f_proj", "sd_b_proj")},
+    "projection.proj_ctype": {n: "vir_gb300.projection.proj_ctype:" + n
+                              for n in ("sd_f_proj_c", "sd_b_proj_c")},
 }
 
 

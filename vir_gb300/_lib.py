@@ -34,6 +34,15 @@ class DD2DGeom(ctypes.Structure):
                 ("DSO", c_float), ("DSD", c_float), ("fan", c_int)]
 
 
+class SiddonRays(ctypes.Structure):
+    """vg_siddon_rays (include/virgpu.h)."""
+    _fields_ = [("n_rays", c_int), ("nx", c_int), ("ny", c_int), ("nz", c_int),
+                ("dx", c_float), ("dy", c_float), ("dz", c_float),
+                ("xb", c_void_p), ("yb", c_void_p), ("zb", c_void_p),
+                ("src", c_void_p), ("dst", c_void_p), ("dist", c_void_p), ("amin", c_void_p),
+                ("amax", c_void_p), ("i0", c_void_p), ("iN", c_void_p), ("valid", c_void_p)]
+
+
 # name -> argtypes (all return int status)
 _PROTOS = {
     "vg_siddon2d_fp": [c_void_p, c_int, c_int, c_void_p, c_int, c_int, c_double, c_double,
@@ -42,6 +51,11 @@ _PROTOS = {
                        c_void_p, c_void_p],
     "vg_siddon2d_trace": [c_int, c_int, c_void_p, c_int, c_int, c_double, c_double, c_void_p,
                           c_void_p, c_void_p, c_void_p],
+    "vg_siddons_count": [ctypes.POINTER(SiddonRays), c_void_p, c_void_p, c_void_p],
+    "vg_siddons_fill": [ctypes.POINTER(SiddonRays), c_void_p, c_void_p, c_void_p, c_void_p],
+    "vg_list_fp": [c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_int, c_void_p],
+    "vg_list_bp": [c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_int, c_void_p, c_int,
+                   c_void_p, c_size_t, c_void_p],
     "vg_dd2d_fp": [ctypes.POINTER(DD2DGeom), c_void_p, c_void_p, c_void_p, c_void_p, c_void_p],
     "vg_dd2d_bp": [ctypes.POINTER(DD2DGeom), c_void_p, c_void_p, c_void_p, c_void_p, c_size_t,
                    c_void_p],
@@ -79,6 +93,8 @@ def load(build_if_missing: bool = True):
             fn.restype = c_int
         L.vg_dd2d_workspace_bytes.argtypes = [ctypes.POINTER(DD2DGeom)]
         L.vg_dd2d_workspace_bytes.restype = c_size_t
+        L.vg_list_bp_workspace_bytes.argtypes = [c_int]
+        L.vg_list_bp_workspace_bytes.restype = c_size_t
         L.vg_dd2d_noalloc_scratch_bytes.argtypes = []
         L.vg_dd2d_noalloc_scratch_bytes.restype = c_size_t
         _lib = L
@@ -96,7 +112,8 @@ def call(name, *args):
 
 def exported_symbols():
     return list(_PROTOS) + ["vg_version", "vg_last_error", "vg_status_string",
-                            "vg_dd2d_workspace_bytes", "vg_dd2d_noalloc_scratch_bytes"]
+                            "vg_dd2d_workspace_bytes", "vg_dd2d_noalloc_scratch_bytes",
+                            "vg_list_bp_workspace_bytes"]
 
 
 def dd2d_workspace(g, dev):
