@@ -194,6 +194,56 @@ int vg_dd2d_sirt_iter(const vg_dd2d_geom *g, const float *y,
 int vg_fbp2d_bp(const vg_dd2d_geom *g, const float *q, const double *trig,
                 float *img, void *stream);
 
+/* ---- 3D cone-beam distance-driven --------------------------------------- */
+
+/* Circular cone-beam geometry of dd_fp_cone_3d / dd_bp_cone_3d
+ * (sys_mat/dd.py:815-888): volume (nx, ny, nz) of cubic voxels d_pix,
+ * detector (nu, nv) with pitches du, dv and shifts su, sv (in bins), source
+ * at DSO, flat detector at DSD; sinogram (na, nu, nv), v fastest. */
+typedef struct {
+    int nx, ny, nz, na, nu, nv;
+    float du, dv, su, sv, d_pix, DSO, DSD;
+} vg_dd3d_geom;
+
+/* Device workspace (per-view line scales and z magnifications) both cone
+ * calls need; 0 for an invalid geometry. */
+size_t vg_dd3d_workspace_bytes(const vg_dd3d_geom *g);
+
+/* Forward projection (dd.py:815-825, sweep :285-380 as intended; returns
+ * sino * d_pix^2 / (du dv)), one thread per (view, u, v) bin. */
+int vg_dd3d_fp(const vg_dd3d_geom *g, const float *vol, const double *trig,
+               float *sino, void *workspace, size_t workspace_bytes,
+               void *stream);
+
+/* Backprojection (dd.py:829-835, sweep :384-468; returns img / (na d_pix)),
+ * one thread per voxel. */
+int vg_dd3d_bp(const vg_dd3d_geom *g, const float *sino, const double *trig,
+               float *vol, void *workspace, size_t workspace_bytes,
+               void *stream);
+
+/* ---- 2D separable footprint -------------------------------------------- */
+
+/* fan = 1: sys_mat/sp.py:12-87 (sf_fp_fan_2d; bins of width du, source at
+ * DSO, detector at DSD); fan = 0: sys_mat/fp_2d_par.py:67-125
+ * (separable_footprint_fp_2d; du is the detector pitch d_det). */
+typedef struct {
+    int nx, ny, na, nu;
+    float du, d_pix, DSO, DSD;
+    int fan;
+} vg_sf2d_geom;
+
+/* Forward projection, gather form (one thread per bin walking the pixel lines
+ * across its footprint strip), same output and scale as the reference:
+ * sino * d_pix (fan) or overlap / d_det (parallel rectangle).  img (nx, ny)
+ * and its transpose imgT (ny, nx). */
+int vg_sf2d_fp(const vg_sf2d_geom *g, const float *img, const float *imgT,
+               const double *trig, float *sino, void *stream);
+
+/* Its exact adjoint (one thread per pixel over all views); vir has no
+ * backprojector for these footprints. */
+int vg_sf2d_bp(const vg_sf2d_geom *g, const float *sino, const double *trig,
+               float *img, void *stream);
+
 /* ---- elementwise / filter helpers -------------------------------------- */
 
 /* out (cols, rows) = transpose of in (rows, cols). */

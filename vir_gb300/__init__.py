@@ -23,8 +23,11 @@ def load():
 # vir module -> {function name: replacement "module:attr" in this package}
 _DROP_INS = {
     "sys_mat.dd": {n: "vir_gb300.sys_mat.dd:" + n for n in
-                   ("dd_fp_par_2d", "dd_bp_par_2d", "dd_fp_fan_2d", "dd_bp_fan_2d")},
-    "sys_mat.fp_2d_par": {"siddons_fp_2d": "vir_gb300.sys_mat.fp_2d_par:siddons_fp_2d"},
+                   ("dd_fp_par_2d", "dd_bp_par_2d", "dd_fp_fan_2d", "dd_bp_fan_2d",
+                    "dd_fp_cone_3d", "dd_bp_cone_3d")},
+    "sys_mat.sp": {"sf_fp_fan_2d": "vir_gb300.sys_mat.sp:sf_fp_fan_2d"},
+    "sys_mat.fp_2d_par": {n: "vir_gb300.sys_mat.fp_2d_par:" + n
+                          for n in ("siddons_fp_2d", "separable_footprint_fp_2d")},
     "filtration": {"filter_sino": "vir_gb300.filtration:filter_sino"},
     "sys_mat.siddon": {"siddons": "vir_gb300.sys_mat.siddon:siddons"},
     "projection.proj": {n: "vir_gb300.projection.proj:" + n for n in ("sd_f_proj", "sd_b_proj")},

@@ -43,6 +43,19 @@ class SiddonRays(ctypes.Structure):
                 ("amax", c_void_p), ("i0", c_void_p), ("iN", c_void_p), ("valid", c_void_p)]
 
 
+class SF2DGeom(ctypes.Structure):
+    """vg_sf2d_geom (include/virgpu.h)."""
+    _fields_ = [("nx", c_int), ("ny", c_int), ("na", c_int), ("nu", c_int), ("du", c_float),
+                ("d_pix", c_float), ("DSO", c_float), ("DSD", c_float), ("fan", c_int)]
+
+
+class DD3DGeom(ctypes.Structure):
+    """vg_dd3d_geom (include/virgpu.h)."""
+    _fields_ = [("nx", c_int), ("ny", c_int), ("nz", c_int), ("na", c_int), ("nu", c_int),
+                ("nv", c_int), ("du", c_float), ("dv", c_float), ("su", c_float),
+                ("sv", c_float), ("d_pix", c_float), ("DSO", c_float), ("DSD", c_float)]
+
+
 # name -> argtypes (all return int status)
 _PROTOS = {
     "vg_siddon2d_fp": [c_void_p, c_int, c_int, c_void_p, c_int, c_int, c_double, c_double,
@@ -63,6 +76,12 @@ _PROTOS = {
                           c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_size_t, c_void_p],
     "vg_dd2d_bp_noalloc": [ctypes.POINTER(DD2DGeom), c_void_p, c_void_p, c_void_p, c_void_p],
     "vg_fbp2d_bp": [ctypes.POINTER(DD2DGeom), c_void_p, c_void_p, c_void_p, c_void_p],
+    "vg_dd3d_fp": [ctypes.POINTER(DD3DGeom), c_void_p, c_void_p, c_void_p, c_void_p, c_size_t,
+                   c_void_p],
+    "vg_dd3d_bp": [ctypes.POINTER(DD3DGeom), c_void_p, c_void_p, c_void_p, c_void_p, c_size_t,
+                   c_void_p],
+    "vg_sf2d_fp": [ctypes.POINTER(SF2DGeom), c_void_p, c_void_p, c_void_p, c_void_p, c_void_p],
+    "vg_sf2d_bp": [ctypes.POINTER(SF2DGeom), c_void_p, c_void_p, c_void_p, c_void_p],
     "vg_transpose": [c_void_p, c_int, c_int, c_void_p, c_void_p],
     "vg_filter_rows": [c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p],
 }
@@ -93,6 +112,8 @@ def load(build_if_missing: bool = True):
             fn.restype = c_int
         L.vg_dd2d_workspace_bytes.argtypes = [ctypes.POINTER(DD2DGeom)]
         L.vg_dd2d_workspace_bytes.restype = c_size_t
+        L.vg_dd3d_workspace_bytes.argtypes = [ctypes.POINTER(DD3DGeom)]
+        L.vg_dd3d_workspace_bytes.restype = c_size_t
         L.vg_list_bp_workspace_bytes.argtypes = [c_int]
         L.vg_list_bp_workspace_bytes.restype = c_size_t
         L.vg_dd2d_noalloc_scratch_bytes.argtypes = []
@@ -113,7 +134,17 @@ def call(name, *args):
 def exported_symbols():
     return list(_PROTOS) + ["vg_version", "vg_last_error", "vg_status_string",
                             "vg_dd2d_workspace_bytes", "vg_dd2d_noalloc_scratch_bytes",
-                            "vg_list_bp_workspace_bytes"]
+                            "vg_list_bp_workspace_bytes", "vg_dd3d_workspace_bytes"]
+
+
+def dd3d_workspace(g, dev):
+    """Device workspace (float32 tensor) for vg_dd3d_fp / vg_dd3d_bp."""
+    import torch
+    L = _lib if _lib is not None else load()
+    n = int(L.vg_dd3d_workspace_bytes(ctypes.byref(g)))
+    if n == 0:
+        raise VirGpuError("vg_dd3d_workspace_bytes", 1, L.vg_last_error().decode(errors="replace"))
+    return torch.empty((n + 3) // 4, dtype=torch.float32, device=dev)
 
 
 def dd2d_workspace(g, dev):

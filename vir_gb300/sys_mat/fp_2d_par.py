@@ -3,6 +3,10 @@
 * ``siddons_fp_2d(img, Angs, n_dets, d_det=1.0, d_pix=1.0)``
   (fp_2d_par.py:11-64) -> ``(na, n_dets)`` float32 sinogram of exact
   intersection-length line integrals.
+* ``separable_footprint_fp_2d(img, Angs, n_dets, d_det=1.0, d_pix=1.0)``
+  (fp_2d_par.py:67-125): rectangle footprint (the interval of the four
+  projected corners) overlapped with each bin, divided by d_det; and
+  ``separable_footprint_bp_2d`` its exact adjoint (GPU: ``vg_sf2d_*``).
 * ``siddons_bp_2d(sino, Angs, img_shape, d_det=1.0, d_pix=1.0)``: its exact
   adjoint (no counterpart in fp_2d_par.py; the reference's backprojector for
   Siddon paths is the list scatter of projection_c.c:200-208).
@@ -42,3 +46,13 @@ def siddons_bp_2d(sino, Angs, img_shape, d_det=1.0, d_pix=1.0):
     call("vg_siddon2d_bp", _core.ptr(y), na, y.shape[1], _core.ptr(trig), nx, ny, float(d_det),
          float(d_pix), _core.ptr(img), _core.stream(dev))
     return _core.to_host_like(img, sino)
+
+
+def separable_footprint_fp_2d(img, Angs, n_dets, d_det=1.0, d_pix=1.0):
+    from .sp import sf_fp_2d
+    return sf_fp_2d(img, Angs, n_dets, d_det, d_pix, 0.0, 0.0, 0)
+
+
+def separable_footprint_bp_2d(sino, Angs, img_shape, d_det=1.0, d_pix=1.0):
+    from .sp import sf_bp_2d
+    return sf_bp_2d(sino, Angs, img_shape, d_det, d_pix, 0.0, 0.0, 0)
