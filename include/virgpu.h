@@ -221,6 +221,24 @@ int vg_dd3d_bp(const vg_dd3d_geom *g, const float *sino, const double *trig,
                float *vol, void *workspace, size_t workspace_bytes,
                void *stream);
 
+/* ---- FDK (cone-beam filtered backprojection) ----------------------------- */
+
+/* vir has no FDK; these three steps build it on the cone geometry above.
+ * (1) sino (na, nu, nv) -> out (na, nv, nu), each sample times the flat-
+ *     detector cosine weight DSD / sqrt(DSD^2 + u^2 + v^2) (the equispaced
+ *     pre-weight of processing/reconstruction.py:99-107 in 2D);
+ * (2) the caller filters the rows with vg_filter_rows at the isocentre
+ *     pitch du DSO / DSD (filtration.filter_sino's 2H);
+ * (3) vg_fdk_transpose_back returns to (na, nu, nv) and vg_fdk_bp
+ *     backprojects: vol = pi / (2 na) sum_views Q(u, v) / U^2 with
+ *     U = (DSO - o) / DSO (processing/proj2.py:606-613), bilinear in (u, v). */
+int vg_fdk_weight_transpose(const vg_dd3d_geom *g, const float *sino,
+                            float *out, void *stream);
+int vg_fdk_transpose_back(const vg_dd3d_geom *g, const float *in, float *out,
+                          void *stream);
+int vg_fdk_bp(const vg_dd3d_geom *g, const float *q, const double *trig,
+              float *vol, void *stream);
+
 /* ---- 2D separable footprint -------------------------------------------- */
 
 /* fan = 1: sys_mat/sp.py:12-87 (sf_fp_fan_2d; bins of width du, source at
@@ -253,8 +271,9 @@ int vg_transpose(const float *in, int rows, int cols, float *out, void *stream);
  * spatial kernel of the padded rFFT filter (filtration.filter_sino,
  * filtration.py:238-309): out[r, i] = sum_j in[r, j] * taps[i - j + nu - 1]
  * with taps (2 nu - 1) = irfft(2 H, n=z) reordered to lags -(nu-1)..nu-1.
- * rows x nu in, rows x nu out.  `row_weight` (nu values or NULL) multiplies
- * each input row first (fan-beam cosine pre-weighting). */
+ * rows x nu in, rows x nu out (any row count, nu <= 6400).  `row_weight`
+ * (nu values or NULL) multiplies each input row first (fan-beam cosine
+ * pre-weighting). */
 int vg_filter_rows(const float *in, int rows, int nu, const float *taps,
                    const float *row_weight, float *out, void *stream);
 

@@ -80,6 +80,9 @@ _PROTOS = {
                    c_void_p],
     "vg_dd3d_bp": [ctypes.POINTER(DD3DGeom), c_void_p, c_void_p, c_void_p, c_void_p, c_size_t,
                    c_void_p],
+    "vg_fdk_weight_transpose": [ctypes.POINTER(DD3DGeom), c_void_p, c_void_p, c_void_p],
+    "vg_fdk_transpose_back": [ctypes.POINTER(DD3DGeom), c_void_p, c_void_p, c_void_p],
+    "vg_fdk_bp": [ctypes.POINTER(DD3DGeom), c_void_p, c_void_p, c_void_p, c_void_p],
     "vg_sf2d_fp": [ctypes.POINTER(SF2DGeom), c_void_p, c_void_p, c_void_p, c_void_p, c_void_p],
     "vg_sf2d_bp": [ctypes.POINTER(SF2DGeom), c_void_p, c_void_p, c_void_p, c_void_p],
     "vg_transpose": [c_void_p, c_int, c_int, c_void_p, c_void_p],

@@ -61,24 +61,53 @@ __global__ void transpose_kernel(const float *__restrict__ in, int rows, int col
     }
 }
 
-// One block per (row, 256-output chunk).  The (weighted) input row is staged
-// in shared memory; taps are read through L1 (consecutive outputs read
-// consecutive taps).
+// One block per (256-output chunk, group of FILT_R rows).  The group's
+// (weighted) input rows are staged in shared memory; each thread computes
+// one output index for all FILT_R rows, so every tap it loads feeds FILT_R
+// FMAs.  Sums run in blocks of 64 taps added into a running total (two-level
+// summation).  Row groups are walked with a grid stride (any row count).
+constexpr int FILT_R = 8;
+
 __global__ void __launch_bounds__(256)
-filter_rows_kernel(const float *__restrict__ in, int nu, const float *__restrict__ taps,
+filter_rows_kernel(const float *__restrict__ in, int rows, int nu, const float *__restrict__ taps,
                    const float *__restrict__ row_weight, float *__restrict__ out) {
-    extern __shared__ float srow[];
-    int r = blockIdx.y;
-    const float *src = in + (size_t)r * nu;
-    for (int j = threadIdx.x; j < nu; j += blockDim.x)
-        srow[j] = row_weight ? src[j] * row_weight[j] : src[j];
-    __syncthreads();
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nu) return;
-    const float *t = taps + i + nu - 1;  // t[-j] = taps[i - j + nu - 1]
-    Kahan acc;
-    for (int j = 0; j < nu; ++j) acc.add(srow[j] * __ldg(t - j));
-    out[(size_t)r * nu + i] = acc.s;
+    extern __shared__ float srow[];  // [FILT_R][nu]
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    for (int r0 = blockIdx.y * FILT_R; r0 < rows; r0 += gridDim.y * FILT_R) {
+        const int nr = min(FILT_R, rows - r0);
+        __syncthreads();
+        for (int e = threadIdx.x; e < FILT_R * nu; e += blockDim.x) {
+            const int r = e / nu, j = e - r * nu;
+            float v = 0.f;
+            if (r < nr) {
+                v = in[(size_t)(r0 + r) * nu + j];
+                if (row_weight) v *= row_weight[j];
+            }
+            srow[e] = v;
+        }
+        __syncthreads();
+        if (i < nu) {
+            const float *t = taps + i + nu - 1;  // t[-j] = taps[i - j + nu - 1]
+            float tot[FILT_R], blk[FILT_R];
+#pragma unroll
+            for (int r = 0; r < FILT_R; ++r) tot[r] = 0.f;
+            for (int j0 = 0; j0 < nu; j0 += 64) {
+#pragma unroll
+                for (int r = 0; r < FILT_R; ++r) blk[r] = 0.f;
+                const int j1 = min(nu, j0 + 64);
+                for (int j = j0; j < j1; ++j) {
+                    const float tv = __ldg(t - j);
+#pragma unroll
+                    for (int r = 0; r < FILT_R; ++r) blk[r] = fmaf(srow[r * nu + j], tv, blk[r]);
+                }
+#pragma unroll
+                for (int r = 0; r < FILT_R; ++r) tot[r] += blk[r];
+            }
+#pragma unroll
+            for (int r = 0; r < FILT_R; ++r)
+                if (r < nr) out[(size_t)(r0 + r) * nu + i] = tot[r];
+        }
+    }
 }
 
 }  // namespace
@@ -95,10 +124,17 @@ extern "C" int vg_transpose(const float *in, int rows, int cols, float *out, voi
 extern "C" int vg_filter_rows(const float *in, int rows, int nu, const float *taps,
                               const float *row_weight, float *out, void *stream) {
     VG_REQUIRE(in && taps && out, "filter_rows: null pointer");
-    VG_REQUIRE(rows > 0 && rows < 65536 && nu > 0, "filter_rows: bad sizes");
-    VG_REQUIRE(nu <= 48 * 1024 / 4, "filter_rows: nu above 12288");
-    dim3 grid(ceil_div(nu, 256), rows);
-    filter_rows_kernel<<<grid, 256, nu * sizeof(float), as_stream(stream)>>>(in, nu, taps,
-                                                                           row_weight, out);
+    VG_REQUIRE(rows > 0 && nu > 0, "filter_rows: bad sizes");
+    const size_t smem = (size_t)FILT_R * nu * sizeof(float);
+    VG_REQUIRE(smem <= 200 * 1024, "filter_rows: nu above 6400");
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(filter_rows_kernel,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return cuda_status(e, "filter_rows: shared memory attribute");
+    }
+    const int groups = ceil_div(rows, FILT_R);
+    dim3 grid(ceil_div(nu, 256), groups < 65535 ? groups : 65535);
+    filter_rows_kernel<<<grid, 256, smem, as_stream(stream)>>>(in, rows, nu, taps, row_weight,
+                                                               out);
     return launch_status("filter_rows");
 }

@@ -27,7 +27,7 @@ import numpy as np
 import torch
 
 from . import _core
-from ._lib import DD2DGeom, call, dd2d_workspace
+from ._lib import DD2DGeom, DD3DGeom, call, dd2d_workspace
 from .filtration import filter_rows_device
 
 
@@ -165,3 +165,32 @@ def fbp_2d(sino, ang_arr, img_shape, geom="par", DSO=0.0, DSD=0.0, du=1.0, su=0.
     call("vg_fbp2d_bp", ctypes.byref(g), _core.ptr(q), _core.ptr(trig), _core.ptr(img),
          _core.stream(dev))
     return _core.to_host_like(img, sino)
+
+
+def fdk(sino, ang_arr, img_shape, DSO, DSD, du=1.0, dv=1.0, su=0.0, sv=0.0, d_pix=1.0,
+        filter_type="ramp", cutoff=0.5, real_space=True):
+    """FDK reconstruction of a full circular cone-beam scan (na, nu, nv) on the
+    geometry of ``dd_fp_cone_3d``: cosine pre-weight, ramp filter along u at
+    the isocentre pitch, 1/U^2-weighted voxel-driven backprojection.  vir has
+    no FDK; the weights extend its fan-beam FBP spec (see vg_fdk_* in
+    include/virgpu.h)."""
+    dev = _core.device_of(sino)
+    y = _core.to_device(sino, dev)
+    if y.ndim != 3:
+        raise ValueError("sino must be (na, nu, nv)")
+    trig = _core.trig_cache.get(ang_arr, np.float32, dev)
+    na, nu, nv = y.shape
+    f = _core.f32
+    g = DD3DGeom(int(img_shape[0]), int(img_shape[1]), int(img_shape[2]), na, nu, nv,
+                 f(du), f(dv), f(su), f(sv), f(d_pix), f(DSO), f(DSD))
+    t = torch.empty((na, nv, nu), dtype=torch.float32, device=dev)
+    call("vg_fdk_weight_transpose", ctypes.byref(g), _core.ptr(y), _core.ptr(t), _core.stream(dev))
+    qt = filter_rows_device(t.view(na * nv, nu), f(du) * f(DSO) / f(DSD), filter_type, cutoff,
+                            real_space)
+    q = torch.empty((na, nu, nv), dtype=torch.float32, device=dev)
+    call("vg_fdk_transpose_back", ctypes.byref(g), _core.ptr(qt), _core.ptr(q), _core.stream(dev))
+    del t, qt
+    vol = torch.empty(tuple(int(v) for v in img_shape), dtype=torch.float32, device=dev)
+    call("vg_fdk_bp", ctypes.byref(g), _core.ptr(q), _core.ptr(trig), _core.ptr(vol),
+         _core.stream(dev))
+    return _core.to_host_like(vol, sino)
