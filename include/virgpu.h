@@ -131,7 +131,14 @@ typedef struct {
     float d_pix;     /* pixel width */
     float DSO, DSD;  /* fan only */
     int fan;
+    int variant;     /* forward-projector tile variant, 1..vg_dd2d_fp_variants();
+                        0 = chosen from the sizes (vg_dd2d_fp_default_variant) */
 } vg_dd2d_geom;
+
+/* Number of forward-projector tile variants, and the one variant 0 maps to
+ * for a geometry (the autotuner in vir_gb300/autotune.py times the others). */
+int vg_dd2d_fp_variants(void);
+int vg_dd2d_fp_default_variant(const vg_dd2d_geom *g);
 
 /* Forward projection, gather form (one thread per bin, pixels of each
  * orthogonal line found directly), returns A x * d_pix / du exactly as

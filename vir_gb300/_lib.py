@@ -31,7 +31,7 @@ class DD2DGeom(ctypes.Structure):
     """vg_dd2d_geom (include/virgpu.h)."""
     _fields_ = [("nx", c_int), ("ny", c_int), ("na", c_int), ("nu", c_int),
                 ("du", c_float), ("su", c_float), ("d_pix", c_float),
-                ("DSO", c_float), ("DSD", c_float), ("fan", c_int)]
+                ("DSO", c_float), ("DSD", c_float), ("fan", c_int), ("variant", c_int)]
 
 
 class SiddonRays(ctypes.Structure):
@@ -113,6 +113,10 @@ def load(build_if_missing: bool = True):
             fn = getattr(L, name)
             fn.argtypes = args
             fn.restype = c_int
+        L.vg_dd2d_fp_variants.argtypes = []
+        L.vg_dd2d_fp_variants.restype = c_int
+        L.vg_dd2d_fp_default_variant.argtypes = [ctypes.POINTER(DD2DGeom)]
+        L.vg_dd2d_fp_default_variant.restype = c_int
         L.vg_dd2d_workspace_bytes.argtypes = [ctypes.POINTER(DD2DGeom)]
         L.vg_dd2d_workspace_bytes.restype = c_size_t
         L.vg_dd3d_workspace_bytes.argtypes = [ctypes.POINTER(DD3DGeom)]
@@ -137,6 +141,7 @@ def call(name, *args):
 def exported_symbols():
     return list(_PROTOS) + ["vg_version", "vg_last_error", "vg_status_string",
                             "vg_dd2d_workspace_bytes", "vg_dd2d_noalloc_scratch_bytes",
+                            "vg_dd2d_fp_variants", "vg_dd2d_fp_default_variant",
                             "vg_list_bp_workspace_bytes", "vg_dd3d_workspace_bytes"]
 
 

@@ -21,11 +21,11 @@ from .reconstruction import SIRT2D
 
 
 class BatchedSIRT2D:
-    def __init__(self, problems, device=None, n_streams=16):
+    def __init__(self, problems, device=None, n_streams=16, autotune=False):
         """problems: list of dicts with SIRT2D's arguments (sino, ang_arr,
         img_shape, geom, DSO, DSD, du, su, d_pix, gamma)."""
         self.dev = device or torch.device("cuda", torch.cuda.current_device())
-        self.items = [SIRT2D(device=self.dev, **p) for p in problems]
+        self.items = [SIRT2D(device=self.dev, autotune=autotune, **p) for p in problems]
         self.n_streams = max(1, int(n_streams))
         self._graph = None
         self._n = 0

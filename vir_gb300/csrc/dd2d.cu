@@ -135,16 +135,13 @@ __device__ __forceinline__ float det_edge(const vg_dd2d_geom &g, int j) {
 // the end: deterministic, no atomics.
 // ---------------------------------------------------------------------------
 
-#ifndef VG_FP_MAXB
-#define VG_FP_MAXB 24
-#endif
-#ifndef VG_FP_WARPS
-#define VG_FP_WARPS 8
-#endif
-constexpr int FP_MAXB = VG_FP_MAXB;   // bins per lane (strided by 32)
-constexpr int FP_WARPS = VG_FP_WARPS; // warps per block (lines in flight)
-constexpr int FP_SEG = 16;            // pixels per lane in the line scan
-constexpr int FP_BINS = 32 * FP_MAXB; // bins per block
+// Tile variants: WARPS (lines in flight per block) x MAXB (bins per lane,
+// strided by 32; a block owns 32 MAXB bins of one view).  vg_dd2d_geom's
+// `variant` selects one (1..FP_NVARIANTS), 0 picks by size (fp_variant_for).
+constexpr int FP_SEG = 16;  // pixels per lane in the line scan
+struct FpVariant { int warps, maxb; };
+constexpr FpVariant FP_VARIANTS[] = {{8, 6}, {8, 12}, {8, 24}, {4, 24}, {4, 48}, {2, 48}};
+constexpr int FP_NVARIANTS = sizeof(FP_VARIANTS) / sizeof(FP_VARIANTS[0]);
 
 // padded entry index: one spare entry every 16 keeps the scan's lanes (16
 // entries apart) on distinct shared-memory banks
@@ -153,14 +150,12 @@ __host__ __device__ inline int fp_line_entries(int nd) { return pad_idx(nd) + 1;
 
 // mode 0: out = FP;  mode 1 (SIRT residual): out = (y - FP) * inv_w, or FP
 // where inv_w == 0.
-template <bool FAN>
-#ifndef VG_FP_MINB
-#define VG_FP_MINB 2
-#endif
-__global__ void __launch_bounds__(FP_WARPS * 32, VG_FP_MINB)
+template <bool FAN, int FP_WARPS, int FP_MAXB>
+__global__ void __launch_bounds__(FP_WARPS * 32, (FP_MAXB > 24 ? 1 : (FP_WARPS >= 8 ? 2 : 16 / FP_WARPS)))
 dd2d_fp_kernel(vg_dd2d_geom g, const float *__restrict__ img, const float *__restrict__ imgT,
                const double *__restrict__ trig, float *__restrict__ out, int mode,
                const float *__restrict__ y, const float *__restrict__ inv_w) {
+    constexpr int FP_BINS = 32 * FP_MAXB;  // bins per block
     extern __shared__ float4 smem4[];
     __shared__ float2 UC[FP_BINS + 32];  // per bin edge (U, C(U)); entries past nb repeat nb
     const int ia = blockIdx.y;
@@ -462,34 +457,57 @@ int check_geom(const vg_dd2d_geom *g) {
     return VG_OK;
 }
 
+template <bool FAN, int W, int B>
+int launch_fp_t(const vg_dd2d_geom *g, const float *img, const float *imgT, const double *trig,
+                float *out, int mode, const float *y, const float *inv_w, cudaStream_t st) {
+    const int nd = g->nx > g->ny ? g->nx : g->ny;
+    size_t smem = (size_t)W * fp_line_entries(nd) * sizeof(float4);
+    const size_t red = (size_t)W * 32 * B * sizeof(float);
+    if (smem < red) smem = red;
+    VG_REQUIRE(smem <= 200 * 1024, "dd2d_fp: image side too large for this tile variant");
+    static size_t attr = 0;  // per instantiation: largest dynamic smem already allowed
+    if (smem > 48 * 1024 && smem > attr) {
+        cudaError_t e = cudaFuncSetAttribute(dd2d_fp_kernel<FAN, W, B>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return cuda_status(e, "dd2d_fp: shared memory attribute");
+        attr = smem;
+    }
+    dim3 grid(ceil_div(g->nu, 32 * B), g->na);
+    dd2d_fp_kernel<FAN, W, B><<<grid, W * 32, smem, st>>>(*g, img, imgT, trig, out, mode, y,
+                                                         inv_w);
+    return launch_status("dd2d_fp");
+}
+
+// Size heuristic: the fewest bins per lane covering the detector in one
+// block, and fewer warps (line buffers) for long lines.
+int fp_variant_for(const vg_dd2d_geom *g) {
+    const int nd = g->nx > g->ny ? g->nx : g->ny;
+    if (nd > 512) return g->nu > 768 ? 5 : 4;
+    if (g->nu <= 192) return 1;
+    if (g->nu <= 384) return 2;
+    return g->nu <= 768 ? 3 : 5;
+}
+
 template <bool FAN>
-int set_fp_smem(size_t bytes) {
-    static size_t done = 0;
-    if (bytes <= 48 * 1024 || bytes <= done) return VG_OK;
-    cudaError_t e = cudaFuncSetAttribute(dd2d_fp_kernel<FAN>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-    if (e != cudaSuccess) return cuda_status(e, "dd2d_fp: shared memory attribute");
-    done = bytes;
-    return VG_OK;
+int launch_fp_fan(int v, const vg_dd2d_geom *g, const float *img, const float *imgT,
+                  const double *trig, float *out, int mode, const float *y, const float *inv_w,
+                  cudaStream_t st) {
+    switch (v) {
+        case 1: return launch_fp_t<FAN, 8, 6>(g, img, imgT, trig, out, mode, y, inv_w, st);
+        case 2: return launch_fp_t<FAN, 8, 12>(g, img, imgT, trig, out, mode, y, inv_w, st);
+        case 3: return launch_fp_t<FAN, 8, 24>(g, img, imgT, trig, out, mode, y, inv_w, st);
+        case 4: return launch_fp_t<FAN, 4, 24>(g, img, imgT, trig, out, mode, y, inv_w, st);
+        case 5: return launch_fp_t<FAN, 4, 48>(g, img, imgT, trig, out, mode, y, inv_w, st);
+        case 6: return launch_fp_t<FAN, 2, 48>(g, img, imgT, trig, out, mode, y, inv_w, st);
+        default: VG_REQUIRE(false, "dd2d_fp: variant %d out of range 0..%d", v, FP_NVARIANTS);
+    }
 }
 
 int launch_fp(const vg_dd2d_geom *g, const float *img, const float *imgT, const double *trig,
               float *out, int mode, const float *y, const float *inv_w, cudaStream_t st) {
-    const int nd = g->nx > g->ny ? g->nx : g->ny;
-    size_t smem = (size_t)FP_WARPS * fp_line_entries(nd) * sizeof(float4);
-    const size_t red = (size_t)FP_WARPS * FP_BINS * sizeof(float);
-    if (smem < red) smem = red;
-    VG_REQUIRE(smem <= 200 * 1024, "dd2d_fp: image side too large for the line buffers");
-    dim3 grid(ceil_div(g->nu, FP_BINS), g->na);
-    int s = g->fan ? set_fp_smem<true>(smem) : set_fp_smem<false>(smem);
-    if (s) return s;
-    if (g->fan)
-        dd2d_fp_kernel<true><<<grid, FP_WARPS * 32, smem, st>>>(*g, img, imgT, trig, out, mode,
-                                                               y, inv_w);
-    else
-        dd2d_fp_kernel<false><<<grid, FP_WARPS * 32, smem, st>>>(*g, img, imgT, trig, out, mode,
-                                                                y, inv_w);
-    return launch_status("dd2d_fp");
+    const int v = g->variant ? g->variant : fp_variant_for(g);
+    return g->fan ? launch_fp_fan<true>(v, g, img, imgT, trig, out, mode, y, inv_w, st)
+                  : launch_fp_fan<false>(v, g, img, imgT, trig, out, mode, y, inv_w, st);
 }
 
 int launch_bp(const vg_dd2d_geom *g, const float *sino, const double *trig, float *img, int mode,
@@ -521,6 +539,12 @@ extern "C" int vg_dd2d_fp(const vg_dd2d_geom *g, const float *img, const float *
     if (st) return st;
     VG_REQUIRE(img && imgT && trig && sino, "dd2d_fp: null pointer");
     return launch_fp(g, img, imgT, trig, sino, 0, nullptr, nullptr, as_stream(stream));
+}
+
+extern "C" int vg_dd2d_fp_variants(void) { return FP_NVARIANTS; }
+
+extern "C" int vg_dd2d_fp_default_variant(const vg_dd2d_geom *g) {
+    return check_geom(g) ? 0 : fp_variant_for(g);
 }
 
 extern "C" size_t vg_dd2d_workspace_bytes(const vg_dd2d_geom *g) {

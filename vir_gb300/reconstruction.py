@@ -31,9 +31,9 @@ from ._lib import DD2DGeom, DD3DGeom, call, dd2d_workspace
 from .filtration import filter_rows_device
 
 
-def _geom(nx, ny, na, nu, du, su, d_pix, DSO, DSD, fan):
+def _geom(nx, ny, na, nu, du, su, d_pix, DSO, DSD, fan, variant=0):
     return DD2DGeom(int(nx), int(ny), int(na), int(nu), _core.f32(du), _core.f32(su),
-                    _core.f32(d_pix), _core.f32(DSO), _core.f32(DSD), int(fan))
+                    _core.f32(d_pix), _core.f32(DSO), _core.f32(DSD), int(fan), int(variant))
 
 
 class SIRT2D:
@@ -45,7 +45,8 @@ class SIRT2D:
     """
 
     def __init__(self, sino, ang_arr, img_shape, geom="par", DSO=0.0, DSD=0.0, du=1.0, su=0.0,
-                 d_pix=1.0, gamma=1.0, x0=1e-5, W_sino=None, W_img=None, device=None):
+                 d_pix=1.0, gamma=1.0, x0=1e-5, W_sino=None, W_img=None, device=None,
+                 autotune=False):
         _core.require_cuda()
         self.dev = device or _core.device_of(sino)
         self.fan = 1 if geom == "fan" else 0
@@ -57,6 +58,9 @@ class SIRT2D:
         if self.y.shape[0] != na:
             raise ValueError("sino rows must equal len(ang_arr)")
         self.g = _geom(nx, ny, na, nu, du, su, d_pix, DSO, DSD, self.fan)
+        if autotune:
+            from .autotune import best_fp_variant
+            self.g.variant = best_fp_variant(self.g, self.dev)
         self.gamma = float(gamma)
         self.ws = dd2d_workspace(self.g, self.dev)
         if W_sino is None:
