@@ -16,7 +16,7 @@
 //    then each thread walks its bins down the chunk, keeping per bin the
 //    index of the pixel under its left edge (it moves by at most a step from
 //    one line to the next), and sums the 1-3 overlapping pixels.
-//  BP (dd2d_bp_kernel): one block per 32x8 pixel tile.  Views are processed
+//  BP (dd2d_bp_kernel): one block per 64x16 pixel tile (2x2 per thread).  Views are processed
 //    in chunks: the block projects the tile's driving edges for every view of
 //    the chunk into shared memory (one division per edge, shared by the two
 //    pixels on either side) with the line scales; then each thread sums, per
@@ -368,6 +368,10 @@ __device__ __forceinline__ float bp_G(const float2 *__restrict__ ts, int nu, flo
     return fmaf(e.y, tc - (float)j, e.x);
 }
 
+// Each thread owns a 2x2 pixel patch.  A view drives along x (X-driven) or y:
+// its two orthogonal lines through the patch share three driving edges each,
+// so per view the patch needs 6 edge projections and 6 running-integral
+// lookups for its 4 pixels, and the view and line parameters are read once.
 // mode 0: img = BP;  mode 1 (SIRT update): x += gamma * BP * inv_w (BP where
 // inv_w == 0), written to x and its transpose xT.
 template <bool FAN>
@@ -378,15 +382,16 @@ dd2d_bp_kernel(vg_dd2d_geom g, BpWork w, const double *__restrict__ trig,
     __shared__ float4 Vs[BP_VC];  // (pd, od, po, oo)
     __shared__ int Xs[BP_VC];
     const int tid = threadIdx.y * BP_TY + threadIdx.x;
-    const int iy = blockIdx.x * BP_TY + threadIdx.x, ix = blockIdx.y * BP_TX + threadIdx.y;
+    const int iy = blockIdx.x * (2 * BP_TY) + 2 * threadIdx.x;  // patch origin
+    const int ix = blockIdx.y * (2 * BP_TX) + 2 * threadIdx.y;
     const bool inside = iy < g.ny && ix < g.nx;
     const int nm = g.nx > g.ny ? g.nx : g.ny;
     const float u0 = det_edge(g, 0);
     const float inv_du = 1.0f / g.du;
-    // this pixel's coordinates for either driving axis
     const float bx = edge_coord(g.d_pix, ix, g.nx), by = edge_coord(g.d_pix, iy, g.ny);
-    const float cx = bx + 0.5f * g.d_pix, cy = by + 0.5f * g.d_pix;
-    Kahan acc;
+    const float cx0 = bx + 0.5f * g.d_pix, cy0 = by + 0.5f * g.d_pix;
+    const float2 *ts_all = w.ts;
+    Kahan acc[2][2];
     for (int a0 = 0; a0 < g.na; a0 += BP_VC) {
         const int nv = min(BP_VC, g.na - a0);
         __syncthreads();
@@ -397,46 +402,75 @@ dd2d_bp_kernel(vg_dd2d_geom g, BpWork w, const double *__restrict__ trig,
         }
         __syncthreads();
         if (!inside) continue;
-        float part = 0.f;
+        float part[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
         for (int vi = 0; vi < nv; ++vi) {
             const float4 q = Vs[vi];
             const bool xd = Xs[vi];
-            const float b0 = xd ? bx : by;   // driving edge
-            const float cen = xd ? cy : cx;  // line centre
-            const int io = xd ? iy : ix;
-            const float cp = q.z * cen;
-            float p0 = fmaf(q.x, b0, cp), p1 = fmaf(q.x, b0 + g.d_pix, cp);
-            if (FAN) {
-                const float co = q.w * cen;
-                const float d0 = g.DSO - fmaf(q.y, b0, co);
-                const float d1 = g.DSO - fmaf(q.y, b0 + g.d_pix, co);
+            const float b0 = xd ? bx : by;    // first driving edge of the patch
+            const float c0 = xd ? cy0 : cx0;  // centre of the first line
+            const int io0 = xd ? iy : ix;
+            const int no = xd ? g.ny : g.nx;
+            const float2 *ts = ts_all + (size_t)(a0 + vi) * (g.nu + 1);
+            const float *sc = w.scl + (size_t)(a0 + vi) * nm;
+            float cL[2][2];  // [line][position along the driving axis]
+#pragma unroll
+            for (int L = 0; L < 2; ++L) {
+                const float cen = c0 + (float)L * g.d_pix;
+                const float cp = q.z * cen;
+                float P[3];
+#pragma unroll
+                for (int e = 0; e < 3; ++e) {
+                    const float b = fmaf((float)e, g.d_pix, b0);
+                    float p = fmaf(q.x, b, cp);
+                    if (FAN) {
+                        const float den = g.DSO - fmaf(q.y, b, q.w * cen);
 #if VG_FAST_DIV
-                p0 = __fdividef(g.DSD * p0, d0);
-                p1 = __fdividef(g.DSD * p1, d1);
+                        p = __fdividef(g.DSD * p, den);
 #else
-                p0 = g.DSD * p0 / d0;
-                p1 = g.DSD * p1 / d1;
+                        p = g.DSD * p / den;
 #endif
+                    }
+                    P[e] = p;
+                }
+                const float G0 = bp_G(ts, g.nu, (P[0] - u0) * inv_du);
+                const float G1 = bp_G(ts, g.nu, (P[1] - u0) * inv_du);
+                const float G2 = bp_G(ts, g.nu, (P[2] - u0) * inv_du);
+                const float sgn = (P[2] >= P[0]) ? 1.f : -1.f;  // monotone line
+                const float s = (io0 + L < no) ? __ldg(sc + io0 + L) * sgn : 0.f;
+                cL[L][0] = (G1 - G0) * s;
+                cL[L][1] = (G2 - G1) * s;
             }
-            const float2 *ts = w.ts + (size_t)(a0 + vi) * (g.nu + 1);
-            const float t0 = (fminf(p0, p1) - u0) * inv_du, t1 = (fmaxf(p0, p1) - u0) * inv_du;
-            const float s = bp_G(ts, g.nu, t1) - bp_G(ts, g.nu, t0);
-            part = fmaf(s, __ldg(w.scl + (size_t)(a0 + vi) * nm + io), part);
+            // X-driven: line = y offset, position = x offset; Y-driven: the transpose
+            part[0][0] += cL[0][0];
+            part[1][1] += cL[1][1];
+            part[1][0] += xd ? cL[0][1] : cL[1][0];
+            part[0][1] += xd ? cL[1][0] : cL[0][1];
         }
-        acc.add(part);
+#pragma unroll
+        for (int dx = 0; dx < 2; ++dx)
+#pragma unroll
+            for (int dy = 0; dy < 2; ++dy) acc[dx][dy].add(part[dx][dy]);
     }
     if (!inside) return;
-    const float bp = acc.s / ((float)g.na * g.d_pix);
-    const size_t o = (size_t)ix * g.ny + iy;
-    if (mode == 1) {
-        const float wi = inv_w[o];
-        const float upd = (wi != 0.f) ? bp * wi : bp;
-        const float xn = img[o] + gamma * upd;
-        img[o] = xn;
-        xT[(size_t)iy * g.nx + ix] = xn;
-    } else {
-        img[o] = bp;
-    }
+    const float f = 1.0f / ((float)g.na * g.d_pix);
+#pragma unroll
+    for (int dx = 0; dx < 2; ++dx)
+#pragma unroll
+        for (int dy = 0; dy < 2; ++dy) {
+            const int px = ix + dx, py = iy + dy;
+            if (px >= g.nx || py >= g.ny) continue;
+            const float bp = acc[dx][dy].s * f;
+            const size_t o = (size_t)px * g.ny + py;
+            if (mode == 1) {
+                const float wi = inv_w[o];
+                const float upd = (wi != 0.f) ? bp * wi : bp;
+                const float xn = img[o] + gamma * upd;
+                img[o] = xn;
+                xT[(size_t)py * g.nx + px] = xn;
+            } else {
+                img[o] = bp;
+            }
+        }
 }
 
 int check_geom(const vg_dd2d_geom *g) {
@@ -521,7 +555,7 @@ int launch_bp(const vg_dd2d_geom *g, const float *sino, const double *trig, floa
     else        dd2d_bp_prep<false><<<g->na, 256, 0, st>>>(*g, sino, trig, w);
     int s = launch_status("dd2d_bp_prep");
     if (s) return s;
-    dim3 grid(ceil_div(g->ny, BP_TY), ceil_div(g->nx, BP_TX));
+    dim3 grid(ceil_div(g->ny, 2 * BP_TY), ceil_div(g->nx, 2 * BP_TX));
     VG_REQUIRE(grid.y < 65536, "dd2d_bp: nx too large");
     dim3 block(BP_TY, BP_TX);
     if (g->fan)
