@@ -196,7 +196,7 @@ dd2d_fp_kernel(vg_dd2d_geom g, const float *__restrict__ img, const float *__res
         // (edge coordinate b0 + i db along a lane's segment)
         const float db = rev ? -g.d_pix : g.d_pix;
         float carry = 0.f;
-        for (int r0 = 0; r0 <= nd; r0 += 32 * FP_SEG) {
+        for (int r0 = 0; r0 < nd; r0 += 32 * FP_SEG) {
             const int m0 = r0 + lane * FP_SEG;
             const float b0 = edge_coord(g.d_pix, rev ? nd - m0 : m0, nd);
             float Pv[FP_SEG + 1], q[FP_SEG];
@@ -222,13 +222,17 @@ dd2d_fp_kernel(vg_dd2d_geom g, const float *__restrict__ img, const float *__res
             float run = carry + inc - tot;
             carry += __shfl_sync(0xffffffffu, inc, 31);
             float4 *Es = E + pad_idx(m0);  // m0 is a multiple of 16: entries m0+i are contiguous
-            const int lim = nd - m0;        // entries m0 + i with i <= lim exist
+            const int lim = nd - m0;        // pixel entries m0 + i with i < lim exist
 #pragma unroll
             for (int i = 0; i < FP_SEG; ++i) {
-                if (i <= lim) Es[i] = make_float4(Pv[i], run, q[i], 0.f);
+                if (i < lim) Es[i] = make_float4(Pv[i], run, q[i], 0.f);
                 run = fmaf(q[i], Pv[i + 1] - Pv[i], run);
             }
         }
+        // the closing edge nd: its projection and the line total
+        if (lane == 0)
+            E[pad_idx(nd)] = make_float4(
+                proj<FAN>(g, v, Lg.cp, Lg.co, edge_coord(g.d_pix, rev ? 0 : nd, nd)), carry, 0.f, 0.f);
         __syncwarp();
         // F at the left edge of each of this lane's bins; right edges from lane + 1
         // (lane 31's right edge is lane 0's next left edge)
