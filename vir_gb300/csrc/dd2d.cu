@@ -143,20 +143,26 @@ struct FpVariant { int warps, maxb; };
 constexpr FpVariant FP_VARIANTS[] = {{8, 6}, {8, 12}, {8, 24}, {4, 24}, {4, 48}, {2, 48}};
 constexpr int FP_NVARIANTS = sizeof(FP_VARIANTS) / sizeof(FP_VARIANTS[0]);
 
-// padded entry index: one spare entry every 16 keeps the scan's lanes (16
-// entries apart) on distinct shared-memory banks
+// Line entries are (G_k, V_k) with G_k = S_k - V_k P_k, so F(U) = G_k + V_k U
+// for U in pixel k.  Entry slot pad_idx(k + 1) holds edge/pixel k; slot 0 is
+// a zero sentinel for U before the line's first edge (F = 0), and the closing
+// edge nd carries (S_nd, 0).  One spare slot every 16 keeps the scan's lanes
+// (16 entries apart) on different shared-memory banks.
 __host__ __device__ __forceinline__ int pad_idx(int m) { return m + (m >> 4); }
-__host__ __device__ inline int fp_line_entries(int nd) { return pad_idx(nd) + 1; }
+__host__ __device__ inline int fp_line_entries(int nd) { return pad_idx(nd + 1) + 1; }
 
 // mode 0: out = FP;  mode 1 (SIRT residual): out = (y - FP) * inv_w, or FP
 // where inv_w == 0.
 template <bool FAN, int FP_WARPS, int FP_MAXB>
-__global__ void __launch_bounds__(FP_WARPS * 32, (FP_MAXB > 24 ? 1 : (FP_WARPS >= 8 ? 2 : 16 / FP_WARPS)))
+#ifndef VG_FP_MINB8
+#define VG_FP_MINB8 2
+#endif
+__global__ void __launch_bounds__(FP_WARPS * 32, (FP_MAXB > 24 ? 1 : (FP_WARPS >= 8 ? VG_FP_MINB8 : 16 / FP_WARPS)))
 dd2d_fp_kernel(vg_dd2d_geom g, const float *__restrict__ img, const float *__restrict__ imgT,
                const double *__restrict__ trig, float *__restrict__ out, int mode,
                const float *__restrict__ y, const float *__restrict__ inv_w) {
     constexpr int FP_BINS = 32 * FP_MAXB;  // bins per block
-    extern __shared__ float4 smem4[];
+    extern __shared__ float2 smem2[];
     __shared__ float2 UC[FP_BINS + 32];  // per bin edge (U, C(U)); entries past nb repeat nb
     const int ia = blockIdx.y;
     const ViewGeo v = view_geo(trig, ia);
@@ -166,7 +172,7 @@ dd2d_fp_kernel(vg_dd2d_geom g, const float *__restrict__ img, const float *__res
     const bool rev = v.pd < 0.f;               // edges decreasing in k: sweep reversed
     const int stride = fp_line_entries(nd);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    float4 *E = smem4 + (size_t)warp * stride;  // this warp's line buffer
+    float2 *E = smem2 + (size_t)warp * stride;  // this warp's line buffer
     const int jbase = blockIdx.x * FP_BINS;
     const int nb = min(FP_BINS, g.nu - jbase);  // bins of this block
     const float half = 0.5f * (float)nd;
@@ -221,18 +227,18 @@ dd2d_fp_kernel(vg_dd2d_geom g, const float *__restrict__ img, const float *__res
             }
             float run = carry + inc - tot;
             carry += __shfl_sync(0xffffffffu, inc, 31);
-            float4 *Es = E + pad_idx(m0);  // m0 is a multiple of 16: entries m0+i are contiguous
-            const int lim = nd - m0;        // pixel entries m0 + i with i < lim exist
+            const int lim = nd - m0;  // pixel entries m0 + i with i < lim exist
 #pragma unroll
             for (int i = 0; i < FP_SEG; ++i) {
-                if (i < lim) Es[i] = make_float4(Pv[i], run, q[i], 0.f);
+                if (i < lim) E[pad_idx(m0 + i + 1)] = make_float2(fmaf(-q[i], Pv[i], run), q[i]);
                 run = fmaf(q[i], Pv[i + 1] - Pv[i], run);
             }
         }
-        // the closing edge nd: its projection and the line total
-        if (lane == 0)
-            E[pad_idx(nd)] = make_float4(
-                proj<FAN>(g, v, Lg.cp, Lg.co, edge_coord(g.d_pix, rev ? 0 : nd, nd)), carry, 0.f, 0.f);
+        // the sentinel before the first edge and the closing edge nd (line total)
+        if (lane == 0) {
+            E[0] = make_float2(0.f, 0.f);
+            E[pad_idx(nd + 1)] = make_float2(carry, 0.f);
+        }
         __syncwarp();
         // F at the left edge of each of this lane's bins; right edges from lane + 1
         // (lane 31's right edge is lane 0's next left edge)
@@ -241,9 +247,10 @@ dd2d_fp_kernel(vg_dd2d_geom g, const float *__restrict__ img, const float *__res
         for (int i = 0; i <= FP_MAXB; ++i) {
             const float2 uc = UC[lane + 32 * i];  // padded past nb with the last edge
             const float sidx = fmaf(fmaf(uc.x, la, -lb), uc.y, half);
-            const int k = (int)fminf(fmaxf(sidx, 0.f), (float)nd);
-            const float4 t = E[pad_idx(k)];
-            Fl[i] = fmaf(t.z, fmaxf(uc.x - t.x, 0.f), t.y);
+            // slot of pixel floor(sidx): sentinel below the line, closing edge above
+            const int k = (int)floorf(fminf(fmaxf(sidx, -1.f), (float)nd)) + 1;
+            const float2 t = E[pad_idx(k)];
+            Fl[i] = fmaf(t.y, uc.x, t.x);
         }
 #pragma unroll
         for (int i = 0; i < FP_MAXB; ++i) {
@@ -255,7 +262,7 @@ dd2d_fp_kernel(vg_dd2d_geom g, const float *__restrict__ img, const float *__res
 
     // sum the warps' partial bins in a fixed order
     __syncthreads();
-    float *red = reinterpret_cast<float *>(smem4);  // [FP_WARPS][FP_BINS]
+    float *red = reinterpret_cast<float *>(smem2);  // [FP_WARPS][FP_BINS]
 #pragma unroll
     for (int i = 0; i < FP_MAXB; ++i) red[warp * FP_BINS + lane + 32 * i] = acc[i];
     __syncthreads();
@@ -499,7 +506,7 @@ template <bool FAN, int W, int B>
 int launch_fp_t(const vg_dd2d_geom *g, const float *img, const float *imgT, const double *trig,
                 float *out, int mode, const float *y, const float *inv_w, cudaStream_t st) {
     const int nd = g->nx > g->ny ? g->nx : g->ny;
-    size_t smem = (size_t)W * fp_line_entries(nd) * sizeof(float4);
+    size_t smem = (size_t)W * fp_line_entries(nd) * sizeof(float2);
     const size_t red = (size_t)W * 32 * B * sizeof(float);
     if (smem < red) smem = red;
     VG_REQUIRE(smem <= 200 * 1024, "dd2d_fp: image side too large for this tile variant");
