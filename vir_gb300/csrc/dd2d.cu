@@ -163,7 +163,7 @@ dd2d_fp_kernel(vg_dd2d_geom g, const float *__restrict__ img, const float *__res
                const float *__restrict__ y, const float *__restrict__ inv_w) {
     constexpr int FP_BINS = 32 * FP_MAXB;  // bins per block
     extern __shared__ float2 smem2[];
-    __shared__ float2 UC[FP_BINS + 32];  // per bin edge (U, C(U)); entries past nb repeat nb
+    __shared__ float Cs[FP_BINS + 32];  // per bin edge C(U); entries past nb repeat nb
     const int ia = blockIdx.y;
     const ViewGeo v = view_geo(trig, ia);
     const int nd = v.xdrv ? g.nx : g.ny;
@@ -172,6 +172,8 @@ dd2d_fp_kernel(vg_dd2d_geom g, const float *__restrict__ img, const float *__res
     const bool rev = v.pd < 0.f;               // edges decreasing in k: sweep reversed
     const int stride = fp_line_entries(nd);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    // rows start on 64-byte boundaries when nd % 16 == 0 (and the image is 16-byte aligned)
+    const bool vec_rows = (nd % FP_SEG == 0) && ((reinterpret_cast<uintptr_t>(base) & 15) == 0);
     float2 *E = smem2 + (size_t)warp * stride;  // this warp's line buffer
     const int jbase = blockIdx.x * FP_BINS;
     const int nb = min(FP_BINS, g.nu - jbase);  // bins of this block
@@ -183,7 +185,7 @@ dd2d_fp_kernel(vg_dd2d_geom g, const float *__restrict__ img, const float *__res
         const float sig = (rev ? -1.f : 1.f) / g.d_pix;
         for (int e = threadIdx.x; e < FP_BINS + 32; e += FP_WARPS * 32) {
             const float U = det_edge(g, jbase + min(e, nb));
-            UC[e] = make_float2(U, FAN ? sig / (g.DSD * v.pd + U * v.od) : sig / v.pd);
+            Cs[e] = FAN ? sig / (g.DSD * v.pd + U * v.od) : sig / v.pd;
         }
     }
     __syncthreads();
@@ -209,16 +211,28 @@ dd2d_fp_kernel(vg_dd2d_geom g, const float *__restrict__ img, const float *__res
 #pragma unroll
             for (int i = 0; i <= FP_SEG; ++i)
                 Pv[i] = proj<FAN>(g, v, Lg.cp, Lg.co, fmaf((float)i, db, b0));
-            // pixels m0 .. m0 + FP_SEG - 1 (sweep order), clamped reads past nd
-            const float *px = row + (rev ? nd - 1 - m0 : m0);
-            const int step = rev ? -1 : 1;
+            // pixels m0 .. m0 + FP_SEG - 1 (sweep order): four 16-byte loads when
+            // the segment is whole and aligned, else element by element
             float tot = 0.f;
+            if (vec_rows && m0 + FP_SEG <= nd) {
+                const float4 *p4 = reinterpret_cast<const float4 *>(row + (rev ? nd - FP_SEG - m0 : m0));
+                float raw[FP_SEG];
 #pragma unroll
-            for (int i = 0; i < FP_SEG; ++i) {
-                const float V = (m0 + i < nd) ? __ldg(px + i * step) * Lg.scl : 0.f;
-                q[i] = V;
-                tot = fmaf(V, Pv[i + 1] - Pv[i], tot);
+                for (int j = 0; j < FP_SEG / 4; ++j) {
+                    const float4 t = __ldg(p4 + j);
+                    raw[4 * j] = t.x; raw[4 * j + 1] = t.y; raw[4 * j + 2] = t.z; raw[4 * j + 3] = t.w;
+                }
+#pragma unroll
+                for (int i = 0; i < FP_SEG; ++i) q[i] = (rev ? raw[FP_SEG - 1 - i] : raw[i]) * Lg.scl;
+            } else {
+                const float *px = row + (rev ? nd - 1 - m0 : m0);
+                const int step = rev ? -1 : 1;
+#pragma unroll
+                for (int i = 0; i < FP_SEG; ++i)
+                    q[i] = (m0 + i < nd) ? __ldg(px + i * step) * Lg.scl : 0.f;
             }
+#pragma unroll
+            for (int i = 0; i < FP_SEG; ++i) tot = fmaf(q[i], Pv[i + 1] - Pv[i], tot);
             float inc = tot;
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
@@ -245,7 +259,8 @@ dd2d_fp_kernel(vg_dd2d_geom g, const float *__restrict__ img, const float *__res
         float Fl[FP_MAXB + 1];
 #pragma unroll
         for (int i = 0; i <= FP_MAXB; ++i) {
-            const float2 uc = UC[lane + 32 * i];  // padded past nb with the last edge
+            const int e = min(lane + 32 * i, nb);  // edges past nb repeat the last one
+            const float2 uc = make_float2(det_edge(g, jbase + e), Cs[lane + 32 * i]);
             const float sidx = fmaf(fmaf(uc.x, la, -lb), uc.y, half);
             // slot of pixel floor(sidx): sentinel below the line, closing edge above
             const int k = (int)floorf(fminf(fmaxf(sidx, -1.f), (float)nd)) + 1;
