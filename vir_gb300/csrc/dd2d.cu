@@ -318,6 +318,10 @@ dd2d_fp_kernel(vg_dd2d_geom g, const float *__restrict__ img, const float *__res
 #ifndef VG_BP_MINB
 #define VG_BP_MINB 1
 #endif
+#ifndef VG_BP_UNROLL
+#define VG_BP_UNROLL 2
+#endif
+constexpr int BP_UNROLL = VG_BP_UNROLL;  // views per unrolled step of the view loop
 constexpr int BP_TY = VG_BP_TY;  // pixels along y (threadIdx.x, contiguous in img)
 constexpr int BP_TX = VG_BP_TX;  // pixels along x (threadIdx.y)
 constexpr int BP_VC = (BP_TY * BP_TX < 128) ? BP_TY * BP_TX : 128;  // views staged per chunk
@@ -429,6 +433,7 @@ dd2d_bp_kernel(vg_dd2d_geom g, BpWork w, const double *__restrict__ trig,
         __syncthreads();
         if (!inside) continue;
         float part[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
+#pragma unroll BP_UNROLL
         for (int vi = 0; vi < nv; ++vi) {
             const float4 q = Vs[vi];
             const bool xd = Xs[vi];
