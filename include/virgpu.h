@@ -228,6 +228,44 @@ int vg_dd3d_bp(const vg_dd3d_geom *g, const float *sino, const double *trig,
                float *vol, void *workspace, size_t workspace_bytes,
                void *stream);
 
+/* ---- translational "square" geometry ------------------------------------ */
+
+/* dd_fp_square / dd_bp_square (sys_mat/dd.py:903, 1104): an n x n x nz
+ * object (x, y, z; z fastest) seen from four sides, each a plane of
+ * nsrc_p x nsrc_z sources at distance DSO from the centre (centres
+ * pf.censpace(nsrc, dsrc, ssrc)) and a flat detector DSD from the sources
+ * (cell boundaries pf.boundspace(nu, du, su + ssrc_p) and
+ * pf.boundspace(nv, dv, sv + ssrc_z)).  Sinogram (nsrc_p, nsrc_z, nv, nu, 4),
+ * the side index fastest, 16-byte aligned. */
+typedef struct {
+    int n, nz, nu, nv, nsrc_p, nsrc_z;
+    float DSO, DSD, du, dv, dsrc_p, dsrc_z, su, sv, ssrc_p, ssrc_z, d_pix;
+} vg_dd_square_geom;
+
+/* Device workspace of the backprojection (four FP64 planes of the volume,
+ * 8-byte aligned); 0 for an invalid geometry. */
+size_t vg_dd_square_workspace_bytes(const vg_dd_square_geom *g);
+
+/* Forward projection, dd_fp_square (dd.py:903-930, dd_fp_translational
+ * :959-1100): sino = A vol * d_pix^2 / (du dv); slabs whose magnification
+ * DSD / (DSO - o) is not positive are skipped (dd.py:988). */
+int vg_dd_square_fp(const vg_dd_square_geom *g, const float *vol, float *sino,
+                    void *stream);
+
+/* Backprojection, dd_bp_square (dd.py:1104-1135, dd_bp_translational
+ * :1164-1313): vol = A^T sino, no scaling. */
+int vg_dd_square_bp(const vg_dd_square_geom *g, const float *sino, float *vol,
+                    void *workspace, size_t workspace_bytes, void *stream);
+
+/* One update of sirt_dd.sirt (sirt_dd.py:50-72):
+ *   r = FP(x); r = (y - r) / w_sino where w_sino != 0 (fast_divide1);
+ *   u = BP(r); u = u / w_vol where w_vol != 0 (fast_divide2); x += gamma u.
+ * y, w_sino, r: sinogram layout; w_vol, x: volume layout. */
+int vg_dd_square_sirt_iter(const vg_dd_square_geom *g, const float *y,
+                           const float *w_sino, const float *w_vol, float gamma,
+                           float *x, float *r, void *workspace,
+                           size_t workspace_bytes, void *stream);
+
 /* ---- FDK (cone-beam filtered backprojection) ----------------------------- */
 
 /* vir has no FDK; these three steps build it on the cone geometry above.

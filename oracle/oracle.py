@@ -78,6 +78,8 @@ def lib():
         L.orc_sf_par_rect_2d.argtypes = [ctypes.c_int, _fp, _dp, ctypes.c_int, ctypes.c_int, _dp,
                                          _dp, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                          ctypes.c_double]
+        L.orc_dd_fp_square.argtypes = [_fp, _ip, _dp, _dp]
+        L.orc_dd_bp_square.argtypes = [_fp, _ip, _dp, _dp]
         L.orc_list_fp.argtypes = [_fp, _ip, _fp, _ip, ctypes.c_int, _dp]
         L.orc_list_bp.argtypes = [_fp, _ip, _fp, _ip, ctypes.c_int, ctypes.c_int, _dp]
         L.orc_num_threads.restype = ctypes.c_int
@@ -221,6 +223,45 @@ def dd_bp_cone_3d(sino, ang_arr, img_shape, DSO, DSD, du=1.0, dv=1.0, su=0.0, sv
     lib().orc_dd_bp_cone(_ptr(sino, _fp), *sino.shape, _ptr(c, _dp), _ptr(s, _dp),
                          *[int(v) for v in img_shape], f(du), f(dv), f(su), f(sv), f(d_pix),
                          f(DSO), f(DSD), _ptr(out, _dp))
+    return out
+
+
+# --- translational square geometry (sys_mat/dd.py:895-1313) ----------------
+
+def _square_args(n, nz, nu, nv, nsrc_p, nsrc_z, DSO, DSD, du, dv, dsrc_p, dsrc_z, su, sv,
+                 ssrc_p, ssrc_z, d_pix):
+    # dd.py:916-917 and 1120-1121 cast these to float32; su and sv enter as given
+    f = lambda v: float(np.float32(v))
+    dims = np.array([n, nz, nu, nv, nsrc_p, nsrc_z], np.int32)
+    prm = np.array([f(DSO), f(DSD), f(du), f(dv), f(dsrc_p), f(dsrc_z), float(su), float(sv),
+                    f(ssrc_p), f(ssrc_z), f(d_pix)], np.float64)
+    return dims, prm
+
+
+def dd_fp_square(img, nu, nv, nsrc_p, nsrc_z, DSO, DSD, du=1.0, dv=1.0, dsrc_p=1.0, dsrc_z=1.0,
+                 su=0.0, sv=0.0, ssrc_p=0.0, ssrc_z=0.0, d_pix=1.0):
+    img = _f32(img)
+    nx, ny, nz = img.shape
+    if nx != ny:
+        raise ValueError("nx must equal ny")
+    dims, prm = _square_args(nx, nz, nu, nv, nsrc_p, nsrc_z, DSO, DSD, du, dv, dsrc_p, dsrc_z,
+                             su, sv, ssrc_p, ssrc_z, d_pix)
+    out = np.zeros((nsrc_p, nsrc_z, nv, nu, 4), np.float64)
+    lib().orc_dd_fp_square(_ptr(img, _fp), _ptr(dims, _ip), _ptr(prm, _dp), _ptr(out, _dp))
+    return out
+
+
+def dd_bp_square(sino, img_shape, DSO, DSD, du=1.0, dv=1.0, dsrc_p=1.0, dsrc_z=1.0, su=0.0,
+                 sv=0.0, ssrc_p=0.0, ssrc_z=0.0, d_pix=1.0):
+    sino = _f32(sino)
+    nx, ny, nz = (int(v) for v in img_shape)
+    if nx != ny:
+        raise ValueError("nx must equal ny")
+    nsrc_p, nsrc_z, nv, nu, _ = sino.shape
+    dims, prm = _square_args(nx, nz, nu, nv, nsrc_p, nsrc_z, DSO, DSD, du, dv, dsrc_p, dsrc_z,
+                             su, sv, ssrc_p, ssrc_z, d_pix)
+    out = np.zeros((nx, ny, nz), np.float64)
+    lib().orc_dd_bp_square(_ptr(sino, _fp), _ptr(dims, _ip), _ptr(prm, _dp), _ptr(out, _dp))
     return out
 
 

@@ -551,6 +551,197 @@ void orc_dd_bp_cone(const float *sino, int na, int nu, int nv, const double *cos
 }
 
 /* ------------------------------------------------------------------------ */
+/* Translational "square" geometry, sys_mat/dd.py:895-1313                   */
+/* ------------------------------------------------------------------------ */
+
+/* Geometry of dd_fp_square / dd_bp_square.  prm holds, in this order:
+ * DSO, DSD, du, dv, dsrc_p, dsrc_z, su, sv, ssrc_p, ssrc_z, d_pix.
+ * Grids follow pf.boundspace / pf.censpace (pf.py:43-56): boundaries
+ * d*(k - n/2) + s, centres d*(k - (n-1)/2) + s.  The object is n x n x nz
+ * (x, y, z; z fastest); for side s the voxel in the side's frame (io: the
+ * orthogonal slab, ip: the parallel index) is the image voxel below
+ * (dd.py:1004-1007 + 1042-1045 for the forward, 1264-1267 + 1132-1135 for
+ * the back projection: imgX/imgY transposes and their flipped slices). */
+typedef struct {
+    int n, nz, nu, nv, nsp, nsz;
+    double DSO, DSD, du, dv, dsp, dsz, su, sv, ssp, ssz, d_pix;
+} sq_geom;
+
+static sq_geom sq_make(const int *dims, const double *prm)
+{
+    sq_geom g;
+    g.n = dims[0]; g.nz = dims[1]; g.nu = dims[2]; g.nv = dims[3];
+    g.nsp = dims[4]; g.nsz = dims[5];
+    g.DSO = prm[0]; g.DSD = prm[1]; g.du = prm[2]; g.dv = prm[3]; g.dsp = prm[4];
+    g.dsz = prm[5]; g.su = prm[6]; g.sv = prm[7]; g.ssp = prm[8]; g.ssz = prm[9];
+    g.d_pix = prm[10];
+    return g;
+}
+
+static inline size_t sq_vox(const sq_geom *g, int side, int io, int ip, int iz)
+{
+    int n = g->n, ix, iy;
+    switch (side) {
+    case 0: ix = io; iy = ip; break;                  /* imgY[io, iz, ip]           */
+    case 1: ix = n - 1 - ip; iy = io; break;          /* imgX[io, iz, nP-1-ip]      */
+    case 2: ix = n - 1 - io; iy = n - 1 - ip; break;  /* imgY[no-1-io, iz, nP-1-ip] */
+    default: ix = ip; iy = n - 1 - io; break;         /* imgX[no-1-io, iz, ip]      */
+    }
+    return ((size_t)ix * n + iy) * g->nz + iz;
+}
+
+/* Magnification of slab io: DSD / (DSO - o_bnd[io]), the slab's lower
+ * boundary (dd.py:972 and 1179, M_arr indexed by io). */
+static inline double sq_mag(const sq_geom *g, int io)
+{
+    double o = g->d_pix * ((double)io - g->n / 2.0);
+    return g->DSD / (g->DSO - o);
+}
+
+/* Overlap of [a0, a1] with detector cell k of a boundary grid (b0, d): the
+ * index range is widened by one on each side and the overlaps are clamped,
+ * so rounding of the estimate cannot drop a cell. */
+static inline void sq_range(double a0, double a1, double b0, double d, int n, int *lo, int *hi)
+{
+    double f0 = floor((a0 - b0) / d) - 1.0, f1 = floor((a1 - b0) / d) + 2.0;
+    if (f0 < 0.0) f0 = 0.0;
+    if (f1 > n) f1 = n;
+    *lo = (int)f0;
+    *hi = f1 > f0 ? (int)f1 : (int)f0;
+}
+
+/* dd_fp_translational (dd.py:959-1100): per source column i_sp, slab io
+ * (skipped when M <= 0, :987-989) and z slice iz, the u overlaps of the
+ * projected parallel boundaries M*p_bnd - (M*src_p - ssrc_p) with the u
+ * boundaries fill tmp_u[iu][side] (:1028-1059); each source row i_sz then
+ * spreads tmp_u over the v overlaps of M*z_bnd - (M*src_z - ssrc_z)
+ * (:1061-1098).  Returns sino[i_sp][i_sz][iv][iu][side] * d_pix^2 / (du dv)
+ * (dd.py:930). */
+void orc_dd_fp_square(const float *img, const int *dims, const double *prm, double *sino)
+{
+    sq_geom g = sq_make(dims, prm);
+    int n = g.n, nz = g.nz, nu = g.nu, nv = g.nv;
+    double u0 = g.du * (0.0 - nu / 2.0) + (g.su + g.ssp);
+    double v0 = g.dv * (0.0 - nv / 2.0) + (g.sv + g.ssz);
+    size_t per_sp = (size_t)g.nsz * nv * nu * 4;
+    memset(sino, 0, sizeof(double) * per_sp * g.nsp);
+#pragma omp parallel
+    {
+        double *tmp = (double *)malloc(sizeof(double) * nu * 4);
+#pragma omp for schedule(dynamic)
+        for (int isp = 0; isp < g.nsp; isp++) {
+            double src_p = g.dsp * ((double)isp - (g.nsp - 1) * 0.5) + g.ssp;
+            for (int io = 0; io < n; io++) {
+                double M = sq_mag(&g, io);
+                if (!(M > 0.0)) continue;
+                double cp = M * src_p - g.ssp;
+                for (int iz = 0; iz < nz; iz++) {
+                    memset(tmp, 0, sizeof(double) * nu * 4);
+                    for (int ip = 0; ip < n; ip++) {
+                        double pl = M * (g.d_pix * ((double)ip - n / 2.0)) - cp;
+                        double pr = M * (g.d_pix * ((double)(ip + 1) - n / 2.0)) - cp;
+                        int lo, hi;
+                        sq_range(pl, pr, u0, g.du, nu, &lo, &hi);
+                        double val[4];
+                        for (int s = 0; s < 4; s++) val[s] = img[sq_vox(&g, s, io, ip, iz)];
+                        for (int iu = lo; iu < hi; iu++) {
+                            double ov = fmin(pr, u0 + g.du * (iu + 1)) - fmax(pl, u0 + g.du * iu);
+                            if (ov <= 0.0) continue;
+                            for (int s = 0; s < 4; s++) tmp[iu * 4 + s] += val[s] * ov;
+                        }
+                    }
+                    for (int isz = 0; isz < g.nsz; isz++) {
+                        double src_z = g.dsz * ((double)isz - (g.nsz - 1) * 0.5) + g.ssz;
+                        double cz = M * src_z - g.ssz;
+                        double zl = M * (g.d_pix * ((double)iz - nz / 2.0)) - cz;
+                        double zr = M * (g.d_pix * ((double)(iz + 1) - nz / 2.0)) - cz;
+                        int lo, hi;
+                        sq_range(zl, zr, v0, g.dv, nv, &lo, &hi);
+                        double *base = sino + (size_t)isp * per_sp + (size_t)isz * nv * nu * 4;
+                        for (int iv = lo; iv < hi; iv++) {
+                            double ov = fmin(zr, v0 + g.dv * (iv + 1)) - fmax(zl, v0 + g.dv * iv);
+                            if (ov <= 0.0) continue;
+                            double *row = base + (size_t)iv * nu * 4;
+                            for (int k = 0; k < nu * 4; k++) row[k] += tmp[k] * ov;
+                        }
+                    }
+                }
+            }
+        }
+        free(tmp);
+    }
+    double f = g.d_pix * g.d_pix / (g.du * g.dv);
+    for (size_t i = 0; i < per_sp * g.nsp; i++) sino[i] *= f;
+}
+
+/* dd_bp_translational (dd.py:1164-1313): per slab io (skipped when M <= 0),
+ * source column i_sp and z slice iz, tmp_v[iu][side] collects the sinogram
+ * rows weighted by their v overlaps over every source row (:1194-1253); each
+ * parallel voxel then takes the u-overlap-weighted sum of tmp_v
+ * (:1270-1313).  The four sides accumulate in separate planes (one slab per
+ * thread, no shared writes) and are summed as (side0 + side2) + (side1 +
+ * side3), the imgX + imgY of dd.py:1135.  No output scaling (dd.py:1135). */
+void orc_dd_bp_square(const float *sino, const int *dims, const double *prm, double *img)
+{
+    sq_geom g = sq_make(dims, prm);
+    int n = g.n, nz = g.nz, nu = g.nu, nv = g.nv;
+    double u0 = g.du * (0.0 - nu / 2.0) + (g.su + g.ssp);
+    double v0 = g.dv * (0.0 - nv / 2.0) + (g.sv + g.ssz);
+    size_t nvox = (size_t)n * n * nz;
+    size_t per_sp = (size_t)g.nsz * nv * nu * 4;
+    double *pl4 = (double *)calloc(4 * nvox, sizeof(double));
+#pragma omp parallel
+    {
+        double *tmp = (double *)malloc(sizeof(double) * nu * 4);
+#pragma omp for schedule(dynamic)
+        for (int io = 0; io < n; io++) {
+            double M = sq_mag(&g, io);
+            if (!(M > 0.0)) continue;
+            for (int isp = 0; isp < g.nsp; isp++) {
+                double src_p = g.dsp * ((double)isp - (g.nsp - 1) * 0.5) + g.ssp;
+                double cp = M * src_p - g.ssp;
+                for (int iz = 0; iz < nz; iz++) {
+                    memset(tmp, 0, sizeof(double) * nu * 4);
+                    for (int isz = 0; isz < g.nsz; isz++) {
+                        double src_z = g.dsz * ((double)isz - (g.nsz - 1) * 0.5) + g.ssz;
+                        double cz = M * src_z - g.ssz;
+                        double zl = M * (g.d_pix * ((double)iz - nz / 2.0)) - cz;
+                        double zr = M * (g.d_pix * ((double)(iz + 1) - nz / 2.0)) - cz;
+                        int lo, hi;
+                        sq_range(zl, zr, v0, g.dv, nv, &lo, &hi);
+                        const float *base = sino + (size_t)isp * per_sp + (size_t)isz * nv * nu * 4;
+                        for (int iv = lo; iv < hi; iv++) {
+                            double ov = fmin(zr, v0 + g.dv * (iv + 1)) - fmax(zl, v0 + g.dv * iv);
+                            if (ov <= 0.0) continue;
+                            const float *row = base + (size_t)iv * nu * 4;
+                            for (int k = 0; k < nu * 4; k++) tmp[k] += row[k] * ov;
+                        }
+                    }
+                    for (int ip = 0; ip < n; ip++) {
+                        double pl = M * (g.d_pix * ((double)ip - n / 2.0)) - cp;
+                        double pr = M * (g.d_pix * ((double)(ip + 1) - n / 2.0)) - cp;
+                        int lo, hi;
+                        sq_range(pl, pr, u0, g.du, nu, &lo, &hi);
+                        double acc[4] = {0.0, 0.0, 0.0, 0.0};
+                        for (int iu = lo; iu < hi; iu++) {
+                            double ov = fmin(pr, u0 + g.du * (iu + 1)) - fmax(pl, u0 + g.du * iu);
+                            if (ov <= 0.0) continue;
+                            for (int s = 0; s < 4; s++) acc[s] += tmp[iu * 4 + s] * ov;
+                        }
+                        for (int s = 0; s < 4; s++)
+                            pl4[(size_t)s * nvox + sq_vox(&g, s, io, ip, iz)] += acc[s];
+                    }
+                }
+            }
+        }
+        free(tmp);
+    }
+    for (size_t i = 0; i < nvox; i++)
+        img[i] = (pl4[i] + pl4[2 * nvox + i]) + (pl4[nvox + i] + pl4[3 * nvox + i]);
+    free(pl4);
+}
+
+/* ------------------------------------------------------------------------ */
 /* Separable footprint, sys_mat/sp.py:12-87 and sys_mat/fp_2d_par.py:67-125  */
 /* ------------------------------------------------------------------------ */
 

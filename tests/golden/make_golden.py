@@ -5,9 +5,11 @@ Run in a container that holds the vir tree (default ``/root/reference``):
 
     python tests/golden/make_golden.py [--ref /path/to/vir]
 
-The reference is imported through two shims and nothing else: a ``vir``
-symlink to the tree on ``sys.path`` (every module imports ``vir.*``) and an
-``llvmlite.binding`` stub (``sys_mat/dd.py:11-12`` imports it unconditionally).
+The reference is imported through three shims and nothing else: a ``vir``
+symlink to the tree on ``sys.path`` (every module imports ``vir.*``), an
+``llvmlite.binding`` stub (``sys_mat/dd.py:11-12`` imports it unconditionally)
+and ``dd.prange = range`` (the numba-less fallback of ``dd.py:18-24`` defines
+``njit`` but not ``prange``, which the square-geometry loops call).
 numba is absent here, so the reference's ``@njit`` functions run as plain
 Python through its own fallbacks.  Three modules cannot be imported as modules
 (``sys_mat/sp.py`` runs a 128^3 projection at import, ``sirt_dd.py`` and
@@ -96,6 +98,7 @@ def main():
     ref = args.ref
     import_reference(ref)
     import vir.sys_mat.dd as dd
+    dd.prange = range  # dd.py:18-24 binds no prange when numba is absent
     import vir.sys_mat.fp_2d_par as fp2
     import vir.sys_mat.siddon as sd
     import vir.filtration as filt
@@ -262,6 +265,51 @@ def main():
         x = x + 1.0 * upd
     out["sirt_par"] = dict(img=img5, angs=a5, nu=np.int32(36), sino=y5, W_sino=W_sino,
                            W_img=W_img, iters=np.int32(iters), gamma=1.0, x=x)
+
+    # --- translational square geometry (dd.py:895-1313) and its SIRT ------------
+    # (sirt_dd.py:37-76 executed from source around the reference projectors)
+    rng = np.random.default_rng(23)
+    sq_cases = {
+        # detector truncated on both axes, shifted sources and cells
+        "a": dict(shape=(8, 8, 6), nu=14, nv=10, nsrc_p=3, nsrc_z=2, DSO=20.0, DSD=36.0,
+                  du=1.0, dv=0.9, dsrc_p=0.5, dsrc_z=0.5, su=0.3, sv=4.0, ssrc_p=0.2,
+                  ssrc_z=-3.0, d_pix=1.0),
+        # source plane inside the object: slab 7 (o_bnd = 3 > DSO) is skipped
+        "b": dict(shape=(8, 8, 5), nu=20, nv=12, nsrc_p=2, nsrc_z=3, DSO=2.5, DSD=9.0,
+                  du=1.3, dv=1.1, dsrc_p=0.7, dsrc_z=0.4, su=0.0, sv=1.5, ssrc_p=-0.4,
+                  ssrc_z=-1.0, d_pix=0.8),
+    }
+    for tag, c in sq_cases.items():
+        vol = rng.random(c["shape"]).astype(np.float32)
+        geo = {k: c[k] for k in ("du", "dv", "dsrc_p", "dsrc_z", "su", "sv", "ssrc_p", "ssrc_z",
+                                 "d_pix")}
+        sino = dd.dd_fp_square(vol, c["nu"], c["nv"], c["nsrc_p"], c["nsrc_z"], c["DSO"],
+                               c["DSD"], **geo)
+        y = rng.random(sino.shape).astype(np.float32)
+        bp = dd.dd_bp_square(y, vol.shape, c["DSO"], c["DSD"], **geo)
+        out[f"square_{tag}"] = dict(vol=vol, sino=sino, y=y, bp=bp, **{
+            k: (np.int32(v) if isinstance(v, int) else np.asarray(v))
+            for k, v in c.items() if k != "shape"})
+    fns = function_from_source(os.path.join(ref, "sys_mat", "sirt_dd.py"),
+                               ["fast_divide1", "fast_divide2", "sirt"], {"dd": dd})
+    c = sq_cases["a"]
+    n, nz = c["shape"][0], c["shape"][2]
+    vol = np.zeros(c["shape"], np.float32)
+    vol[2:6, 3:7, 1:5] = 1.0
+    geo = {k: c[k] for k in ("du", "dv", "dsrc_p", "dsrc_z", "su", "sv", "ssrc_p", "ssrc_z",
+                             "d_pix")}
+    args = (c["nu"], c["nv"], c["nsrc_p"], c["nsrc_z"], c["DSO"], c["DSD"])
+    sino = dd.dd_fp_square(vol, *args, **geo)
+    W_sino = dd.dd_fp_square(np.ones(c["shape"], np.float32), *args, **geo)
+    W_img = dd.dd_bp_square(np.ones(sino.shape, np.float32), c["shape"], c["DSO"], c["DSD"], **geo)
+    prms = ((c["DSO"], c["DSD"]), (n, n, nz, c["d_pix"]),
+            (c["nsrc_p"], c["nsrc_z"], c["dsrc_p"], c["dsrc_z"], c["ssrc_p"], c["ssrc_z"]),
+            (c["nu"], c["nv"], c["du"], c["dv"], c["su"], c["sv"]), (1.0, 5))
+    x = fns["sirt"](sino, W_sino, W_img, *prms)
+    out["sirt_square"] = dict(vol=vol, sino=sino, W_sino=W_sino, W_img=W_img, x=x,
+                              gem_prms=np.array(prms[0]), img_prms=np.array(prms[1]),
+                              src_prms=np.array(prms[2]), det_prms=np.array(prms[3]),
+                              srt_prms=np.array(prms[4]))
 
     path = os.path.join(HERE, "golden.npz")
     flat = {}

@@ -24,7 +24,11 @@ def load():
 _DROP_INS = {
     "sys_mat.dd": {n: "vir_gb300.sys_mat.dd:" + n for n in
                    ("dd_fp_par_2d", "dd_bp_par_2d", "dd_fp_fan_2d", "dd_bp_fan_2d",
-                    "dd_fp_cone_3d", "dd_bp_cone_3d")},
+                    "dd_fp_cone_3d", "dd_bp_cone_3d", "dd_fp_square", "dd_bp_square")},
+    "sys_mat.sirt_dd": {n: "vir_gb300.sys_mat.sirt_dd:" + n
+                        for n in ("sirt", "fast_divide1", "fast_divide2")},
+    "sys_mat.sirt_numba": {n: "vir_gb300.sys_mat.sirt_dd:" + n
+                           for n in ("sirt", "fast_divide1", "fast_divide2")},
     "sys_mat.sp": {"sf_fp_fan_2d": "vir_gb300.sys_mat.sp:sf_fp_fan_2d"},
     "sys_mat.fp_2d_par": {n: "vir_gb300.sys_mat.fp_2d_par:" + n
                           for n in ("siddons_fp_2d", "separable_footprint_fp_2d")},

@@ -56,6 +56,14 @@ class DD3DGeom(ctypes.Structure):
                 ("sv", c_float), ("d_pix", c_float), ("DSO", c_float), ("DSD", c_float)]
 
 
+class DDSquareGeom(ctypes.Structure):
+    """vg_dd_square_geom (include/virgpu.h)."""
+    _fields_ = [("n", c_int), ("nz", c_int), ("nu", c_int), ("nv", c_int), ("nsrc_p", c_int),
+                ("nsrc_z", c_int), ("DSO", c_float), ("DSD", c_float), ("du", c_float),
+                ("dv", c_float), ("dsrc_p", c_float), ("dsrc_z", c_float), ("su", c_float),
+                ("sv", c_float), ("ssrc_p", c_float), ("ssrc_z", c_float), ("d_pix", c_float)]
+
+
 # name -> argtypes (all return int status)
 _PROTOS = {
     "vg_siddon2d_fp": [c_void_p, c_int, c_int, c_void_p, c_int, c_int, c_double, c_double,
@@ -80,6 +88,11 @@ _PROTOS = {
                    c_void_p],
     "vg_dd3d_bp": [ctypes.POINTER(DD3DGeom), c_void_p, c_void_p, c_void_p, c_void_p, c_size_t,
                    c_void_p],
+    "vg_dd_square_fp": [ctypes.POINTER(DDSquareGeom), c_void_p, c_void_p, c_void_p],
+    "vg_dd_square_bp": [ctypes.POINTER(DDSquareGeom), c_void_p, c_void_p, c_void_p, c_size_t,
+                        c_void_p],
+    "vg_dd_square_sirt_iter": [ctypes.POINTER(DDSquareGeom), c_void_p, c_void_p, c_void_p,
+                               c_float, c_void_p, c_void_p, c_void_p, c_size_t, c_void_p],
     "vg_fdk_weight_transpose": [ctypes.POINTER(DD3DGeom), c_void_p, c_void_p, c_void_p],
     "vg_fdk_transpose_back": [ctypes.POINTER(DD3DGeom), c_void_p, c_void_p, c_void_p],
     "vg_fdk_bp": [ctypes.POINTER(DD3DGeom), c_void_p, c_void_p, c_void_p, c_void_p],
@@ -121,6 +134,8 @@ def load(build_if_missing: bool = True):
         L.vg_dd2d_workspace_bytes.restype = c_size_t
         L.vg_dd3d_workspace_bytes.argtypes = [ctypes.POINTER(DD3DGeom)]
         L.vg_dd3d_workspace_bytes.restype = c_size_t
+        L.vg_dd_square_workspace_bytes.argtypes = [ctypes.POINTER(DDSquareGeom)]
+        L.vg_dd_square_workspace_bytes.restype = c_size_t
         L.vg_list_bp_workspace_bytes.argtypes = [c_int]
         L.vg_list_bp_workspace_bytes.restype = c_size_t
         L.vg_dd2d_noalloc_scratch_bytes.argtypes = []
@@ -142,7 +157,19 @@ def exported_symbols():
     return list(_PROTOS) + ["vg_version", "vg_last_error", "vg_status_string",
                             "vg_dd2d_workspace_bytes", "vg_dd2d_noalloc_scratch_bytes",
                             "vg_dd2d_fp_variants", "vg_dd2d_fp_default_variant",
-                            "vg_list_bp_workspace_bytes", "vg_dd3d_workspace_bytes"]
+                            "vg_list_bp_workspace_bytes", "vg_dd3d_workspace_bytes",
+                            "vg_dd_square_workspace_bytes"]
+
+
+def dd_square_workspace(g, dev):
+    """Device workspace (float64 tensor) for vg_dd_square_bp / _sirt_iter."""
+    import torch
+    L = _lib if _lib is not None else load()
+    n = int(L.vg_dd_square_workspace_bytes(ctypes.byref(g)))
+    if n == 0:
+        raise VirGpuError("vg_dd_square_workspace_bytes", 1,
+                          L.vg_last_error().decode(errors="replace"))
+    return torch.empty((n + 7) // 8, dtype=torch.float64, device=dev)
 
 
 def dd3d_workspace(g, dev):

@@ -18,6 +18,13 @@ Same names, signatures, return layouts and scales as the reference:
   works, and the FP is the overlap integral the reference's sweep intends
   (its u buffer is not cleared between lines, dd.py:300, 335).
 
+The translational square geometry: ``dd_fp_square(img, nu, nv, nsrc_p,
+nsrc_z, DSO, DSD, du=1.0, dv=1.0, dsrc_p=1.0, dsrc_z=1.0, su=0.0, sv=0.0,
+ssrc_p=0.0, ssrc_z=0.0, d_pix=1.0)`` (dd.py:903) -> ``(nsrc_p, nsrc_z, nv,
+nu, 4)``, ``A x * d_pix^2/(du dv)``, and ``dd_bp_square(sino, img_shape,
+DSO, DSD, ...)`` (dd.py:1104) -> ``(nx, ny, nz)``, ``A^T y`` unscaled; both
+raise ``ValueError("nx must equal ny")`` as the reference does.
+
 Inputs are cast to float32 as ``as_float32`` does (dd.py:29-36, 653); angles
 too, so the per-view driving-axis choice (|sin| >= |cos|, dd.py:478) is made
 on the reference's own float32 trig values.  ``sample`` is accepted and, as
@@ -33,7 +40,8 @@ import ctypes
 import numpy as np
 
 from .. import _core
-from .._lib import DD2DGeom, DD3DGeom, call, dd2d_workspace, dd3d_workspace
+from .._lib import (DD2DGeom, DD3DGeom, DDSquareGeom, call, dd2d_workspace, dd3d_workspace,
+                    dd_square_workspace)
 
 
 def _geom(nx, ny, na, nu, du, su, d_pix, DSO=0.0, DSD=0.0, fan=0):
@@ -132,4 +140,51 @@ def dd_bp_cone_3d(sino, ang_arr, img_shape, DSO, DSD, du=1.0, dv=1.0, su=0.0, sv
     vol = _core.empty(tuple(int(v) for v in img_shape), dev)
     call("vg_dd3d_bp", ctypes.byref(g), _core.ptr(y), _core.ptr(trig), _core.ptr(vol),
          _core.ptr(ws), ws.numel() * 4, _core.stream(dev))
+    return _core.to_host_like(vol, sino)
+
+
+def square_geom(img_shape, nu, nv, nsrc_p, nsrc_z, DSO, DSD, du=1.0, dv=1.0, dsrc_p=1.0,
+                dsrc_z=1.0, su=0.0, sv=0.0, ssrc_p=0.0, ssrc_z=0.0, d_pix=1.0):
+    """vg_dd_square_geom for an (n, n, nz) object (dd.py:907-909, 1110-1112)."""
+    nx, ny, nz = (int(v) for v in img_shape)
+    if nx != ny:
+        raise ValueError("nx must equal ny")
+    f = _core.f32
+    return DDSquareGeom(nx, nz, int(nu), int(nv), int(nsrc_p), int(nsrc_z), f(DSO), f(DSD),
+                        f(du), f(dv), f(dsrc_p), f(dsrc_z), f(su), f(sv), f(ssrc_p), f(ssrc_z),
+                        f(d_pix))
+
+
+def dd_fp_square(img, nu, nv, nsrc_p, nsrc_z, DSO, DSD, du=1.0, dv=1.0, dsrc_p=1.0, dsrc_z=1.0,
+                 su=0.0, sv=0.0, ssrc_p=0.0, ssrc_z=0.0, d_pix=1.0):
+    shape = tuple(img.shape) if hasattr(img, "shape") else np.shape(img)
+    if len(shape) == 3 and shape[0] != shape[1]:
+        raise ValueError("nx must equal ny")
+    dev = _core.device_of(img)
+    x = _core.to_device(img, dev)
+    if x.ndim != 3:
+        raise ValueError("img must be 3D (nx, ny, nz)")
+    g = square_geom(x.shape, nu, nv, nsrc_p, nsrc_z, DSO, DSD, du, dv, dsrc_p, dsrc_z, su, sv,
+                    ssrc_p, ssrc_z, d_pix)
+    sino = _core.empty((int(nsrc_p), int(nsrc_z), int(nv), int(nu), 4), dev)
+    call("vg_dd_square_fp", ctypes.byref(g), _core.ptr(x), _core.ptr(sino), _core.stream(dev))
+    return _core.to_host_like(sino, img)
+
+
+def dd_bp_square(sino, img_shape, DSO, DSD, du=1.0, dv=1.0, dsrc_p=1.0, dsrc_z=1.0, su=0.0,
+                 sv=0.0, ssrc_p=0.0, ssrc_z=0.0, d_pix=1.0):
+    nx, ny, nz = (int(v) for v in img_shape)
+    if nx != ny:
+        raise ValueError("nx must equal ny")
+    dev = _core.device_of(sino)
+    y = _core.to_device(sino, dev)
+    if y.ndim != 5 or y.shape[4] != 4:
+        raise ValueError("sino must be (nsrc_p, nsrc_z, nv, nu, 4)")
+    nsrc_p, nsrc_z, nv, nu, _ = y.shape
+    g = square_geom(img_shape, nu, nv, nsrc_p, nsrc_z, DSO, DSD, du, dv, dsrc_p, dsrc_z, su, sv,
+                    ssrc_p, ssrc_z, d_pix)
+    ws = dd_square_workspace(g, dev)
+    vol = _core.empty((nx, ny, nz), dev)
+    call("vg_dd_square_bp", ctypes.byref(g), _core.ptr(y), _core.ptr(vol), _core.ptr(ws),
+         ws.numel() * 8, _core.stream(dev))
     return _core.to_host_like(vol, sino)
