@@ -126,13 +126,15 @@ def reconstruct_adam(y, geom, steps=200, lr=1e-3, lam=1e-3, x0=None, callback=No
     return x.detach()
 
 
-def sirt(y, geom, iters=20, gamma=1.0, x0=1e-5, callback=None):
+def sirt(y, geom, iters=20, gamma=1.0, x0=1e-5, callback=None, W_sino=None, W_img=None):
     """vir's SIRT rule (sirt_dd.py:23-76; iters - 1 updates) on any pair of
-    this module (cone or 2D), on device tensors."""
+    this module (cone or 2D), on device tensors.  Every step is a separate
+    projector call or torch elementwise op (the unfused path)."""
     dev = y.device
-    ones_x = torch.ones(geom.img_shape, device=dev)
-    W_sino = geom.fp(ones_x)
-    W_img = geom.bp(torch.ones_like(y))
+    if W_sino is None:
+        W_sino = geom.fp(torch.ones(geom.img_shape, device=dev))
+    if W_img is None:
+        W_img = geom.bp(torch.ones_like(y))
     inv_ws = torch.where(W_sino != 0, 1.0 / W_sino, torch.zeros_like(W_sino))
     inv_wi = torch.where(W_img != 0, 1.0 / W_img, torch.zeros_like(W_img))
     x = torch.full(geom.img_shape, float(np.float32(x0)), device=dev)
