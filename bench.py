@@ -194,6 +194,144 @@ def run_kernels_only(n):
     return 0
 
 
+# ---- the other configurations (not the default line) -----------------------
+
+EXTRA = {
+    "c1": "2D parallel Siddon FP + gather BP: 256x256 random-ellipse phantom, 1 mm pixels, "
+          "180 views over pi, 367 bins of 1 mm",
+    "c3": "batched SIRT: 64 parallel/fan problems (seed 3), sides in {128,256,512,1024}, "
+          "90-1440 views, 1.5x detectors; 50 updates, one CUDA graph vs one launch per step",
+    "c4": "3D cone DD FP + BP + FDK: 512^3 volume of 20 random ellipsoids, 0.5 mm voxels, "
+          "720 views over 2pi, 1024x768 detector at 0.8 mm, DSO 600 mm, DSD 1100 mm",
+    "c5": "3D cone DD FP + BP: 256^3 volume of 20 random ellipsoids, 1 mm voxels, 360 views "
+          "over 2pi, 512x384 detector at 1.6 mm, DSO 600 mm, DSD 1100 mm",
+    "square": "translational square geometry DD FP + BP (dd_fp_square / dd_bp_square) at the "
+              "reference's SIRT-script size (64^3, 96x10 sources, 129x64 cells) and at its "
+              "nice.py size (250^3, 650x10 sources, 961x121 cells)",
+}
+
+
+def _event_ms(fn, reps, stream):
+    import torch
+    fn()
+    torch.cuda.synchronize()
+    out = []
+    for _ in range(reps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        out.append(a.elapsed_time(b))
+    return statistics.median(out)
+
+
+def _roof(units, ms, peak):
+    gbs = 4.0 * units / (ms / 1e3) / 1e9
+    return {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
+            "algorithmic_bytes_per_launch": 4.0 * units}
+
+
+def run_workload(args):
+    """One JSON line for a configuration other than the default C2 line:
+    per-kernel CUDA-event times (median of --steps after --warmup), GUPS and
+    the algorithmic-byte roofline.  With --kernels-only N the projector pair
+    is just launched N times (for ncu captures)."""
+    import torch
+    from vir_gb300 import phantoms as ph
+    from vir_gb300.sys_mat import dd
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.current_stream(dev)
+    peak, _ = load_peaks()
+    reps = max(args.steps, 1)
+    wl = args.workload
+    line = {"workload": wl, "config": EXTRA[wl], "n_gpus": 1, "dtype": "f32",
+            "data": "synthetic"}
+    if wl == "c1":
+        from vir_gb300.sys_mat import fp_2d_par as f2
+        img, _ = ph.ellipse_phantom(256, 10, seed=2025, d_pix=1.0)
+        angs = np.linspace(0, np.pi, 180, endpoint=False)
+        x = torch.from_numpy(img).to(dev)
+        y = f2.siddons_fp_2d(x, angs, 367, 1.0, 1.0)
+        fp = lambda: f2.siddons_fp_2d(x, angs, 367, 1.0, 1.0)
+        bp = lambda: f2.siddons_bp_2d(y, angs, (256, 256), 1.0, 1.0)
+        units = 180 * 256 * 256
+    elif wl in ("c4", "c5"):
+        n, na, nu, nv, dp, du = ((512, 720, 1024, 768, 0.5, 0.8) if wl == "c4"
+                                 else (256, 360, 512, 384, 1.0, 1.6))
+        e = ph.random_ellipsoids(20, fov_radius=n * dp / 2, seed=2027)
+        x = ph.rasterize3d_device(e, n, dp, device=dev)
+        angs = np.linspace(0, 2 * np.pi, na, endpoint=False)
+        kw = dict(du=du, dv=du, su=0.0, sv=0.0, d_pix=dp)
+        y = dd.dd_fp_cone_3d(x, angs, nu, nv, 600.0, 1100.0, **kw)
+        fp = lambda: dd.dd_fp_cone_3d(x, angs, nu, nv, 600.0, 1100.0, **kw)
+        bp = lambda: dd.dd_bp_cone_3d(y, angs, (n, n, n), 600.0, 1100.0, **kw)
+        units = na * n ** 3
+    elif wl == "square":
+        cases = {"script": (64, 64, 129, 64, 96, 10, 40.0, 72.0,
+                            dict(du=1.0, dv=1.0, dsrc_p=0.5, dsrc_z=0.5, su=0.0, sv=32.0,
+                                 ssrc_p=0.0, ssrc_z=-27.0, d_pix=1.0)),
+                 "nice": (250, 250, 961, 121, 650, 10, 141.381, 261.381,
+                          dict(du=2.61381, dv=2.61381, dsrc_p=.48, dsrc_z=.48, su=0.0,
+                               sv=158.13554, ssrc_p=0.0, ssrc_z=-74.4, d_pix=.96))}
+        out = {}
+        for name, (n, nz, nu, nv, nsp, nsz, DSO, DSD, kw) in cases.items():
+            e = ph.random_ellipsoids(10, fov_radius=n * kw["d_pix"] / 2, seed=2028)
+            x = ph.rasterize3d_device(e, n, kw["d_pix"], device=dev)
+            y = dd.dd_fp_square(x, nu, nv, nsp, nsz, DSO, DSD, **kw)
+            fp = lambda: dd.dd_fp_square(x, nu, nv, nsp, nsz, DSO, DSD, **kw)
+            bp = lambda: dd.dd_bp_square(y, (n, n, nz), DSO, DSD, **kw)
+            if args.kernels_only:
+                for _ in range(args.kernels_only):
+                    fp(); bp()
+                continue
+            r = 1 if name == "nice" else reps
+            t_fp, t_bp = _event_ms(fp, r, stream), _event_ms(bp, r, stream)
+            units = 4 * nsp * nsz * n * n * nz
+            out[name] = {"kernel_ms": {"fp": t_fp, "bp": t_bp},
+                         "fwd_back_gups": 2 * units / ((t_fp + t_bp) / 1e3) / 1e9,
+                         "roofline_fp": _roof(units, t_fp, peak),
+                         "roofline_bp": _roof(units, t_bp, peak)}
+            del x, y
+            torch.cuda.empty_cache()
+        if not args.kernels_only:
+            line["cases"] = out
+            print(json.dumps(line), flush=True)
+        return 0
+    elif wl == "c3":
+        from vir_gb300.batched import BatchedSIRT2D
+        from vir_gb300.workloads import batched_problems
+        probs = batched_problems(64, seed=3)
+        b = BatchedSIRT2D(probs, n_streams=16)
+        res = {}
+        for mode in ("graph", "plain"):
+            b.reset()
+            res[mode] = _event_ms(lambda: b.run(50) if mode == "graph" else b.plain(50), 1, stream)
+        units = sum(p["sino"].shape[0] * p["img_shape"][0] * p["img_shape"][1] for p in probs)
+        line.update({"metric": "batched SIRT iter/s (50 updates x 64 problems)",
+                     "graph_ms": res["graph"], "plain_ms": res["plain"],
+                     "speedup_vs_plain": res["plain"] / res["graph"],
+                     "fwd_back_gups_graph": 2 * 50 * units / (res["graph"] / 1e3) / 1e9})
+        print(json.dumps(line), flush=True)
+        return 0
+    if args.kernels_only:
+        for _ in range(args.kernels_only):
+            fp(); bp()
+        torch.cuda.synchronize()
+        print(json.dumps({"kernels_only": args.kernels_only, "workload": wl, "ok": True}))
+        return 0
+    t_fp, t_bp = _event_ms(fp, reps, stream), _event_ms(bp, reps, stream)
+    line.update({"kernel_ms": {"fp": t_fp, "bp": t_bp},
+                 "fwd_back_gups": 2 * units / ((t_fp + t_bp) / 1e3) / 1e9,
+                 "roofline_fp": _roof(units, t_fp, peak), "roofline_bp": _roof(units, t_bp, peak)})
+    if wl == "c4":
+        from vir_gb300 import reconstruction as rc
+        line["kernel_ms"]["fdk"] = _event_ms(
+            lambda: rc.fdk(y, angs, (n, n, n), 600.0, 1100.0, du=du, dv=du, d_pix=dp), 1, stream)
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -203,9 +341,14 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--kernels-only", type=int, default=0, metavar="N",
                     help="profiling aid: run the two fused SIRT kernels N times each, no timing")
+    ap.add_argument("--workload", default="c2", choices=["c2"] + sorted(EXTRA),
+                    help="c2 (default) is the benchmark line; the others print one extra "
+                         "JSON line for that configuration")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload != "c2":
+        return run_workload(args)
     if args.kernels_only:
         return run_kernels_only(args.kernels_only)
 

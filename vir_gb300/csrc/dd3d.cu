@@ -44,17 +44,34 @@ __device__ __forceinline__ float projU(const vg_dd3d_geom &g, const View3 &v, fl
     return __fdividef(g.DSD * fmaf(v.pd, b, cp), g.DSO - fmaf(v.od, b, co));
 }
 
-size_t ws_bytes(const vg_dd3d_geom *g) {
+// Workspace: tab[na][max(nx, ny)] float2 (scale, zmag) per (view, line),
+// then, 16-byte aligned, vf[na][2] float4 per view: (pd, od, po, oo) and
+// (|trig|, xdrv, 0, 0), the float view geometry of view3.
+size_t tab_bytes(const vg_dd3d_geom *g) {
     const int nm = g->nx > g->ny ? g->nx : g->ny;
-    return (size_t)g->na * nm * 2 * sizeof(float);
+    return ((size_t)g->na * nm * 2 * sizeof(float) + 15) & ~(size_t)15;
 }
 
-// tab[ia][io] = (scale, zmag)
-__global__ void dd3d_prep(vg_dd3d_geom g, const double *__restrict__ trig, float2 *__restrict__ tab) {
+size_t ws_bytes(const vg_dd3d_geom *g) { return tab_bytes(g) + (size_t)g->na * 2 * sizeof(float4); }
+
+__device__ __forceinline__ View3 view_f(const float4 *__restrict__ vf, int ia) {
+    const float4 a = vf[2 * ia], b = vf[2 * ia + 1];
+    View3 v;
+    v.pd = a.x; v.od = a.y; v.po = a.z; v.oo = a.w; v.tabs = b.x; v.xdrv = b.y != 0.f;
+    return v;
+}
+
+// tab[ia][io] = (scale, zmag); vf[ia] = float view geometry
+__global__ void dd3d_prep(vg_dd3d_geom g, const double *__restrict__ trig, float2 *__restrict__ tab,
+                          float4 *__restrict__ vf) {
     const int ia = blockIdx.x;
     const View3 v = view3(trig, ia);
     const int no = v.xdrv ? g.ny : g.nx;
     const int nm = g.nx > g.ny ? g.nx : g.ny;
+    if (threadIdx.x == 0) {
+        vf[2 * ia] = make_float4(v.pd, v.od, v.po, v.oo);
+        vf[2 * ia + 1] = make_float4(v.tabs, v.xdrv ? 1.f : 0.f, 0.f, 0.f);
+    }
     for (int io = threadIdx.x; io < no; io += blockDim.x) {
         const float c = cen(g.d_pix, io, no);
         const float cp = v.po * c, co = v.oo * c;
@@ -70,103 +87,397 @@ __device__ __forceinline__ float vfloor_edge(const vg_dd3d_geom &g, int j) {
     return g.dv * ((float)j - 0.5f * g.nv + g.sv);
 }
 
-__global__ void __launch_bounds__(256)
+// One cell's share of one line, straight from global memory (any geometry).
+__device__ __noinline__ float fp_cell_line(const vg_dd3d_geom &g, const View3 &v, const float *__restrict__ vol,
+                              size_t sk, size_t so, int nd, int io, float cp, float co, float zmag,
+                              float Ul, float Ur, float Vl, float Vr) {
+    const float inv_d = 1.0f / g.d_pix;
+    const float rl = 1.0f / (g.DSD * v.pd + Ul * v.od), rr = 1.0f / (g.DSD * v.pd + Ur * v.od);
+    const float kl = fmaf(Ul, g.DSO - co, -g.DSD * cp) * rl * inv_d + 0.5f * nd;
+    const float kr = fmaf(Ur, g.DSO - co, -g.DSD * cp) * rr * inv_d + 0.5f * nd;
+    const int k0 = max(0, (int)floorf(fminf(kl, kr)));
+    const int k1 = min(nd - 1, (int)floorf(fmaxf(kl, kr)));
+    const float izl = Vl / (zmag * g.d_pix) + 0.5f * g.nz;
+    const float izr = Vr / (zmag * g.d_pix) + 0.5f * g.nz;
+    const int z0 = max(0, (int)floorf(izl)), z1 = min(g.nz - 1, (int)floorf(izr));
+    float part = 0.f;
+    if (k0 > k1 || z0 > z1) return part;
+    float pa = projU(g, v, cp, co, edg(g.d_pix, k0, nd));
+    for (int k = k0; k <= k1; ++k) {
+        const float pb = projU(g, v, cp, co, edg(g.d_pix, k + 1, nd));
+        const float ou = fminf(fmaxf(pa, pb), Ur) - fmaxf(fminf(pa, pb), Ul);
+        pa = pb;
+        if (ou <= 0.f) continue;
+        const float *col = vol + k * sk + io * so;
+        float colsum = 0.f;
+        for (int iz = z0; iz <= z1; ++iz) {
+            const float zl = zmag * edg(g.d_pix, iz, g.nz), zr = zmag * edg(g.d_pix, iz + 1, g.nz);
+            const float ov = fminf(zr, Vr) - fmaxf(zl, Vl);
+            if (ov > 0.f) colsum = fmaf(__ldg(col + iz), ov, colsum);
+        }
+        part = fmaf(colsum, ou, part);
+    }
+    return part;
+}
+
+// Forward projection, tiled.  Block = (view, FT_U u-cells x FT_V v-cells).
+// For each line io whose shadow meets the tile, the block stages the
+// voxels under its cells (a k x z tile of the line, zero padded) in shared
+// memory, and one thread per cell row / column forms that cell's overlap
+// weights (at most 3 pixels per u-cell and 3 slices per v-cell, the same
+// float expressions as the backprojector).  Each thread then forms its
+// 4 adjacent u-cells x 2 v-cells as sum_a sum_b ou_a ov_b t[k_a][z_b] from
+// shared memory.  Lines whose tile or weights exceed that capacity take
+// the per-cell global-memory path.  Line sums are added in groups of
+// FT_GROUP lines, each group with compensation.
+constexpr int FT_U = 32, FT_V = 64;
+constexpr int FT_KMAX = 48, FT_ZMAX = 96, FT_ZP = FT_ZMAX + 4;
+constexpr int FT_GROUP = 16;
+
+struct FpTile {
+    float t[(FT_KMAX + 2) * FT_ZP];  // volume tile: row = pixel k - kA, column = slice z - zA
+    float4 uw[FT_U];                 // per u-cell: weights of pixels ka, ka+1, ka+2
+    float4 vw[FT_V];                 // per v-cell: weights of slices za, za+1, za+2
+    int uk[FT_U], vz[FT_V];          // ka - kA, za - zA
+    int wide;
+};
+
+__global__ void __launch_bounds__(256, 2)
 dd3d_fp_kernel(vg_dd3d_geom g, const float *__restrict__ vol, const double *__restrict__ trig,
                const float2 *__restrict__ tab, float *__restrict__ sino) {
-    const int iv = blockIdx.x * 32 + threadIdx.x;
-    const int iu = blockIdx.y * 8 + threadIdx.y;
+    __shared__ FpTile S;
     const int ia = blockIdx.z;
-    if (iv >= g.nv || iu >= g.nu) return;
+    const int u0 = blockIdx.y * FT_U, v0 = blockIdx.x * FT_V;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const View3 v = view3(trig, ia);
     const int nd = v.xdrv ? g.nx : g.ny;
     const int no = v.xdrv ? g.ny : g.nx;
     const int nm = g.nx > g.ny ? g.nx : g.ny;
-    const float Ul = ufloor_edge(g, iu), Ur = ufloor_edge(g, iu + 1);
-    const float Vl = vfloor_edge(g, iv), Vr = vfloor_edge(g, iv + 1);
-    // inverse edge map (natural pixel coordinate): b(U) = (U (DSO - co) - DSD cp) / (DSD pd + U od)
-    const float rl = 1.0f / (g.DSD * v.pd + Ul * v.od), rr = 1.0f / (g.DSD * v.pd + Ur * v.od);
-    const float inv_d = 1.0f / g.d_pix;
     const size_t sk = v.xdrv ? (size_t)g.ny * g.nz : (size_t)g.nz;  // stride of k
     const size_t so = v.xdrv ? (size_t)g.nz : (size_t)g.ny * g.nz;  // stride of io
-    Kahan acc;
+    const float inv_d = 1.0f / g.d_pix;
+    // the tile's outer u edges and their inverse-map denominators
+    const float TUl = ufloor_edge(g, u0), TUr = ufloor_edge(g, min(u0 + FT_U, g.nu));
+    const float TVl = vfloor_edge(g, v0), TVr = vfloor_edge(g, min(v0 + FT_V, g.nv));
+    const float rTl = 1.0f / (g.DSD * v.pd + TUl * v.od), rTr = 1.0f / (g.DSD * v.pd + TUr * v.od);
+    // weight threads: tid < FT_U owns u-cell u0 + tid, FT_U <= tid < FT_U + FT_V owns v-cell
+    const int wu_i = u0 + tid, wv_i = v0 + tid - FT_U;
+    const bool is_u = tid < FT_U && wu_i < g.nu;
+    const bool is_v = tid >= FT_U && tid < FT_U + FT_V && wv_i < g.nv;
+    float cUl = 0.f, cUr = 0.f, crl = 0.f, crr = 0.f, cVl = 0.f, cVr = 0.f;
+    if (is_u) {
+        cUl = ufloor_edge(g, wu_i); cUr = ufloor_edge(g, wu_i + 1);
+        crl = 1.0f / (g.DSD * v.pd + cUl * v.od); crr = 1.0f / (g.DSD * v.pd + cUr * v.od);
+    }
+    if (is_v) { cVl = vfloor_edge(g, wv_i); cVr = vfloor_edge(g, wv_i + 1); }
+
+    Kahan acc[8];
+    float grp[8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) grp[c] = 0.f;
+    int ngrp = 0;
+    // S.wide == io + 1 marks line io for the global path; writers only ever
+    // store that marker, so no reset races with them
+    if (tid == 0) S.wide = -1;
     for (int io = 0; io < no; ++io) {
         const float c = cen(g.d_pix, io, no);
         const float cp = v.po * c, co = v.oo * c;
         const float2 sz = __ldg(tab + (size_t)ia * nm + io);
-        // pixels under [Ul, Ur]
-        const float kl = fmaf(Ul, g.DSO - co, -g.DSD * cp) * rl * inv_d + 0.5f * nd;
-        const float kr = fmaf(Ur, g.DSO - co, -g.DSD * cp) * rr * inv_d + 0.5f * nd;
-        const int k0 = max(0, (int)floorf(fminf(kl, kr)));
-        const int k1 = min(nd - 1, (int)floorf(fmaxf(kl, kr)));
-        if (k0 > k1) continue;
-        // slices under [Vl, Vr]: v edge of slice iz is zmag d (iz - nz/2)
-        const float izl = Vl / (sz.y * g.d_pix) + 0.5f * g.nz;
-        const float izr = Vr / (sz.y * g.d_pix) + 0.5f * g.nz;
-        const int z0 = max(0, (int)floorf(izl)), z1 = min(g.nz - 1, (int)floorf(izr));
-        if (z0 > z1) continue;
-        float part = 0.f;
-        float pa = projU(g, v, cp, co, edg(g.d_pix, k0, nd));
-        for (int k = k0; k <= k1; ++k) {
-            const float pb = projU(g, v, cp, co, edg(g.d_pix, k + 1, nd));
-            const float ou = fminf(fmaxf(pa, pb), Ur) - fmaxf(fminf(pa, pb), Ul);
-            pa = pb;
-            if (ou <= 0.f) continue;
-            const float *col = vol + k * sk + io * so;
-            float colsum = 0.f;
-            for (int iz = z0; iz <= z1; ++iz) {
-                const float zl = sz.y * edg(g.d_pix, iz, g.nz), zr = sz.y * edg(g.d_pix, iz + 1, g.nz);
-                const float ov = fminf(zr, Vr) - fmaxf(zl, Vl);
-                if (ov > 0.f) colsum = fmaf(__ldg(col + iz), ov, colsum);
-            }
-            part = fmaf(colsum, ou, part);
+        const float kl = fmaf(TUl, g.DSO - co, -g.DSD * cp) * rTl * inv_d + 0.5f * nd;
+        const float kr = fmaf(TUr, g.DSO - co, -g.DSD * cp) * rTr * inv_d + 0.5f * nd;
+        const int kA = max(0, (int)floorf(fminf(kl, kr)));
+        const int kB = min(nd - 1, (int)floorf(fmaxf(kl, kr)));
+        const int zA = max(0, (int)floorf(TVl / (sz.y * g.d_pix) + 0.5f * g.nz));
+        const int zB = min(g.nz - 1, (int)floorf(TVr / (sz.y * g.d_pix) + 0.5f * g.nz));
+        if (kA > kB || zA > zB) continue;  // block-uniform
+        const int nk = kB - kA + 1, nzt = zB - zA + 1;
+        const bool fits = nk <= FT_KMAX && nzt <= FT_ZMAX;
+        __syncthreads();  // the previous line's reads of S are done
+        if (fits) {
+            const float *base = vol + (size_t)kA * sk + (size_t)io * so + zA;
+            for (int r = warp; r < nk + 2; r += 8)
+                for (int q = lane; q < nzt + 2; q += 32)
+                    S.t[r * FT_ZP + q] = (r < nk && q < nzt) ? __ldg(base + (size_t)r * sk + q) : 0.f;
         }
-        acc.add(part * sz.x);
+        if (tid == 0 && !fits) S.wide = io + 1;
+        if (is_u || (tid < FT_U)) {
+            float4 w = make_float4(0.f, 0.f, 0.f, 0.f);
+            int rel = 0;
+            if (is_u && fits) {
+                const float a = fmaf(cUl, g.DSO - co, -g.DSD * cp) * crl * inv_d + 0.5f * nd;
+                const float b = fmaf(cUr, g.DSO - co, -g.DSD * cp) * crr * inv_d + 0.5f * nd;
+                const int ka = max(kA, (int)floorf(fminf(a, b)));
+                const int kb = min(kB, (int)floorf(fmaxf(a, b)));
+                if (ka <= kb) {
+                    if (kb - ka > 2) {
+                        S.wide = io + 1;
+                    } else {
+                        float pa = projU(g, v, cp, co, edg(g.d_pix, ka, nd));
+                        float ow[3];
+#pragma unroll
+                        for (int t = 0; t < 3; ++t) {
+                            const float pb = projU(g, v, cp, co, edg(g.d_pix, ka + t + 1, nd));
+                            const float o = fminf(fmaxf(pa, pb), cUr) - fmaxf(fminf(pa, pb), cUl);
+                            ow[t] = (ka + t <= kb && o > 0.f) ? o : 0.f;
+                            pa = pb;
+                        }
+                        w = make_float4(ow[0], ow[1], ow[2], 0.f);
+                        rel = ka - kA;
+                    }
+                }
+            }
+            S.uw[tid] = w;
+            S.uk[tid] = rel;
+        } else if (tid < FT_U + FT_V) {
+            float4 w = make_float4(0.f, 0.f, 0.f, 0.f);
+            int rel = 0;
+            if (is_v && fits) {
+                const int za = max(zA, (int)floorf(cVl / (sz.y * g.d_pix) + 0.5f * g.nz));
+                const int zb = min(zB, (int)floorf(cVr / (sz.y * g.d_pix) + 0.5f * g.nz));
+                if (za <= zb) {
+                    if (zb - za > 2) {
+                        S.wide = io + 1;
+                    } else {
+                        float ow[3];
+#pragma unroll
+                        for (int t = 0; t < 3; ++t) {
+                            const float zl = sz.y * edg(g.d_pix, za + t, g.nz);
+                            const float zr = sz.y * edg(g.d_pix, za + t + 1, g.nz);
+                            const float o = fminf(zr, cVr) - fmaxf(zl, cVl);
+                            ow[t] = (za + t <= zb && o > 0.f) ? o : 0.f;
+                        }
+                        w = make_float4(ow[0], ow[1], ow[2], 0.f);
+                        rel = za - zA;
+                    }
+                }
+            }
+            S.vw[tid - FT_U] = w;
+            S.vz[tid - FT_U] = rel;
+        }
+        __syncthreads();
+        float part[8];
+        if (S.wide != io + 1) {
+            const float4 wa = S.vw[lane], wb = S.vw[32 + lane];
+            const int za = S.vz[lane], zb = S.vz[32 + lane];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const float4 wu = S.uw[4 * warp + j];
+                const float *r = S.t + S.uk[4 * warp + j] * FT_ZP;
+                float ca = 0.f, cb = 0.f;
+#pragma unroll
+                for (int t = 0; t < 3; ++t) {
+                    const float *q = r + t * FT_ZP;
+                    const float sa = fmaf(wa.x, q[za], fmaf(wa.y, q[za + 1], wa.z * q[za + 2]));
+                    const float sb = fmaf(wb.x, q[zb], fmaf(wb.y, q[zb + 1], wb.z * q[zb + 2]));
+                    const float wt = t == 0 ? wu.x : (t == 1 ? wu.y : wu.z);
+                    ca = fmaf(wt, sa, ca);
+                    cb = fmaf(wt, sb, cb);
+                }
+                part[2 * j] = ca;
+                part[2 * j + 1] = cb;
+            }
+        } else {
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int iu = u0 + 4 * warp + j;
+                const float Ul = ufloor_edge(g, iu), Ur = ufloor_edge(g, iu + 1);
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const int iv = v0 + 32 * h + lane;
+                    part[2 * j + h] = (iu < g.nu && iv < g.nv)
+                        ? fp_cell_line(g, v, vol, sk, so, nd, io, cp, co, sz.y, Ul, Ur,
+                                       vfloor_edge(g, iv), vfloor_edge(g, iv + 1))
+                        : 0.f;
+                }
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < 8; ++q) grp[q] = fmaf(part[q], sz.x, grp[q]);
+        if (++ngrp == FT_GROUP) {
+#pragma unroll
+            for (int q = 0; q < 8; ++q) { acc[q].add(grp[q]); grp[q] = 0.f; }
+            ngrp = 0;
+        }
     }
-    sino[((size_t)ia * g.nu + iu) * g.nv + iv] = acc.s * (g.d_pix * g.d_pix / (g.du * g.dv));
+    const float f = g.d_pix * g.d_pix / (g.du * g.dv);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const int iu = u0 + 4 * warp + j;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int iv = v0 + 32 * h + lane;
+            acc[2 * j + h].add(grp[2 * j + h]);
+            if (iu < g.nu && iv < g.nv)
+                sino[((size_t)ia * g.nu + iu) * g.nv + iv] = acc[2 * j + h].s * f;
+        }
+    }
 }
 
-__global__ void __launch_bounds__(256)
-dd3d_bp_kernel(vg_dd3d_geom g, const float *__restrict__ sino, const double *__restrict__ trig,
-               const float2 *__restrict__ tab, float *__restrict__ vol) {
-    const int iz = blockIdx.x * 32 + threadIdx.x;
-    const int iy = blockIdx.y * 8 + threadIdx.y;
-    const int ix = blockIdx.z;
-    if (iz >= g.nz || iy >= g.ny) return;
-    const int nm = g.nx > g.ny ? g.nx : g.ny;
-    const float zl0 = edg(g.d_pix, iz, g.nz), zr0 = edg(g.d_pix, iz + 1, g.nz);
+// Backprojection, tiled.  Block = 8 x 8 columns (x, y) x 32 slices; thread =
+// one slice z (lane) of one y row (warp), 8 voxels along x.  Per view the
+// block first tabulates in shared memory the overlap weights every voxel
+// needs: per column (its pixel on its line) the first detector column and
+// 3 u-overlaps times the line scale, per (line, slice) the first detector
+// row and 3 v-overlaps -- the same float expressions as the forward
+// projector.  Each voxel then sums 3 x 3 sinogram cells (L1-cached reads,
+// lanes on consecutive rows of one column).  Views whose voxels overlap more
+// than 3 cells along u or v take the per-voxel global path.  The tables are
+// double-buffered, so one barrier per view suffices.
+constexpr int BT = 8, BZ = 32;
+
+struct BpTables {
+    float4 uw[2][BT * BT];  // per column (cx + 8 cy): weights of cells j, j+1, j+2 (x scale)
+    int uj[2][BT * BT];
+    float4 vw[2][BT][BZ];   // per (line in tile, slice): weights of rows q, q+1, q+2
+    int vq[2][BT][BZ];
+    int wide[2];
+};
+
+__device__ float bp_voxel_view(const vg_dd3d_geom &g, const View3 &v, const float *__restrict__ s,
+                               float2 sz, int k, int nd, float cp, float co, int iz) {
     const float u0 = ufloor_edge(g, 0), v0 = vfloor_edge(g, 0);
     const float idu = 1.0f / g.du, idv = 1.0f / g.dv;
-    Kahan acc;
-    for (int ia = 0; ia < g.na; ++ia) {
-        const View3 v = view3(trig, ia);
-        int k, nd, io, no;
-        if (v.xdrv) { k = ix; nd = g.nx; io = iy; no = g.ny; }
-        else        { k = iy; nd = g.ny; io = ix; no = g.nx; }
-        const float c = cen(g.d_pix, io, no);
-        const float cp = v.po * c, co = v.oo * c;
-        const float2 sz = __ldg(tab + (size_t)ia * nm + io);
-        const float pa = projU(g, v, cp, co, edg(g.d_pix, k, nd));
-        const float pb = projU(g, v, cp, co, edg(g.d_pix, k + 1, nd));
-        const float ulo = fminf(pa, pb), uhi = fmaxf(pa, pb);
-        const float vlo = sz.y * zl0, vhi = sz.y * zr0;
-        const int j0 = max(0, (int)floorf((ulo - u0) * idu)), j1 = min(g.nu - 1, (int)floorf((uhi - u0) * idu));
-        const int q0 = max(0, (int)floorf((vlo - v0) * idv)), q1 = min(g.nv - 1, (int)floorf((vhi - v0) * idv));
-        if (j0 > j1 || q0 > q1) continue;
-        const float *s = sino + (size_t)ia * g.nu * g.nv;
-        float part = 0.f;
-        for (int j = j0; j <= j1; ++j) {
-            const float ou = fminf(uhi, ufloor_edge(g, j + 1)) - fmaxf(ulo, ufloor_edge(g, j));
-            if (ou <= 0.f) continue;
-            float rs = 0.f;
-            for (int q = q0; q <= q1; ++q) {
-                const float ov = fminf(vhi, vfloor_edge(g, q + 1)) - fmaxf(vlo, vfloor_edge(g, q));
-                if (ov > 0.f) rs = fmaf(__ldg(s + (size_t)j * g.nv + q), ov, rs);
-            }
-            part = fmaf(rs, ou, part);
+    const float pa = projU(g, v, cp, co, edg(g.d_pix, k, nd));
+    const float pb = projU(g, v, cp, co, edg(g.d_pix, k + 1, nd));
+    const float ulo = fminf(pa, pb), uhi = fmaxf(pa, pb);
+    const float vlo = sz.y * edg(g.d_pix, iz, g.nz), vhi = sz.y * edg(g.d_pix, iz + 1, g.nz);
+    const int j0 = max(0, (int)floorf((ulo - u0) * idu)), j1 = min(g.nu - 1, (int)floorf((uhi - u0) * idu));
+    const int q0 = max(0, (int)floorf((vlo - v0) * idv)), q1 = min(g.nv - 1, (int)floorf((vhi - v0) * idv));
+    float part = 0.f;
+    for (int j = j0; j <= j1; ++j) {
+        const float ou = fminf(uhi, ufloor_edge(g, j + 1)) - fmaxf(ulo, ufloor_edge(g, j));
+        if (ou <= 0.f) continue;
+        float rs = 0.f;
+        for (int q = q0; q <= q1; ++q) {
+            const float ov = fminf(vhi, vfloor_edge(g, q + 1)) - fmaxf(vlo, vfloor_edge(g, q));
+            if (ov > 0.f) rs = fmaf(__ldg(s + (size_t)j * g.nv + q), ov, rs);
         }
-        acc.add(part * sz.x);
+        part = fmaf(rs, ou, part);
     }
-    vol[((size_t)ix * g.ny + iy) * g.nz + iz] = acc.s / ((float)g.na * g.d_pix);
+    return part * sz.x;
+}
+
+__global__ void __launch_bounds__(256, 2)
+dd3d_bp_kernel(vg_dd3d_geom g, const float *__restrict__ sino, const float4 *__restrict__ vf,
+               const float2 *__restrict__ tab, float *__restrict__ vol) {
+    __shared__ BpTables T;
+    const int z0 = blockIdx.x * BZ, y0 = blockIdx.y * BT, x0 = blockIdx.z * BT;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int iz = z0 + lane, iy = y0 + warp;  // this thread: voxels (x0 + i, iy, iz), i < 8
+    const int nm = g.nx > g.ny ? g.nx : g.ny;
+    const float u0 = ufloor_edge(g, 0), v0 = vfloor_edge(g, 0);
+    const float idu = 1.0f / g.du, idv = 1.0f / g.dv;
+    const int jmax = g.nu - 3, qmax = g.nv - 3;
+    Kahan acc[BT];
+    float grp[BT];
+#pragma unroll
+    for (int i = 0; i < BT; ++i) grp[i] = 0.f;
+    int ngrp = 0;
+    // T.wide[b] == ia + 1 marks view ia for the per-voxel path; writers only
+    // ever store that marker, so no reset races with them
+    if (tid < 2) T.wide[tid] = -1;
+    __syncthreads();
+    for (int ia = 0; ia < g.na; ++ia) {
+        const int b = ia & 1;
+        const View3 v = view_f(vf, ia);
+        const int nd = v.xdrv ? g.nx : g.ny, no = v.xdrv ? g.ny : g.nx;
+        const int k0 = v.xdrv ? x0 : y0, io0 = v.xdrv ? y0 : x0;  // tile origin in (k, io)
+        // v table: thread (line l = warp, slice lane)
+        {
+            const int io = io0 + warp;
+            float4 w = make_float4(0.f, 0.f, 0.f, 0.f);
+            int qb = 0;
+            if (io < no && iz < g.nz) {
+                const float zmag = __ldg(tab + (size_t)ia * nm + io).y;
+                const float vlo = zmag * edg(g.d_pix, iz, g.nz), vhi = zmag * edg(g.d_pix, iz + 1, g.nz);
+                const int qs = (int)floorf((vlo - v0) * idv), qe = (int)floorf((vhi - v0) * idv);
+                if (qe - qs > 2) T.wide[b] = ia + 1;
+                qb = min(max(qs, 0), max(qmax, 0));
+                float ow[3];
+#pragma unroll
+                for (int t = 0; t < 3; ++t) {
+                    const float o = fminf(vhi, vfloor_edge(g, qb + t + 1)) - fmaxf(vlo, vfloor_edge(g, qb + t));
+                    ow[t] = (qb + t < g.nv && o > 0.f) ? o : 0.f;
+                }
+                w = make_float4(ow[0], ow[1], ow[2], 0.f);
+            }
+            T.vw[b][warp][lane] = w;
+            T.vq[b][warp][lane] = qb;
+        }
+        // u table: thread c < 64 owns column (k0 + c % 8, line io0 + c / 8)
+        if (tid < BT * BT) {
+            const int k = k0 + (tid & 7), io = io0 + (tid >> 3);
+            float4 w = make_float4(0.f, 0.f, 0.f, 0.f);
+            int jb = 0;
+            if (k < nd && io < no) {
+                const float c = cen(g.d_pix, io, no);
+                const float cp = v.po * c, co = v.oo * c;
+                const float scale = __ldg(tab + (size_t)ia * nm + io).x;
+                const float pa = projU(g, v, cp, co, edg(g.d_pix, k, nd));
+                const float pb = projU(g, v, cp, co, edg(g.d_pix, k + 1, nd));
+                const float ulo = fminf(pa, pb), uhi = fmaxf(pa, pb);
+                const int js = (int)floorf((ulo - u0) * idu), je = (int)floorf((uhi - u0) * idu);
+                if (je - js > 2) T.wide[b] = ia + 1;
+                jb = min(max(js, 0), max(jmax, 0));
+                float ow[3];
+#pragma unroll
+                for (int t = 0; t < 3; ++t) {
+                    const float o = fminf(uhi, ufloor_edge(g, jb + t + 1)) - fmaxf(ulo, ufloor_edge(g, jb + t));
+                    ow[t] = (jb + t < g.nu && o > 0.f) ? o * scale : 0.f;
+                }
+                w = make_float4(ow[0], ow[1], ow[2], 0.f);
+            }
+            T.uw[b][tid] = w;
+            T.uj[b][tid] = jb;
+        }
+        __syncthreads();
+        const float *s = sino + (size_t)ia * g.nu * g.nv;
+        float part[BT];
+        if (T.wide[b] != ia + 1 && g.nu >= 3 && g.nv >= 3) {
+#pragma unroll
+            for (int i = 0; i < BT; ++i) {
+                // voxel (x0 + i, iy, iz) is column (k, io) = xdrv ? (x, y) : (y, x)
+                const int c = v.xdrv ? (i + BT * warp) : (warp + BT * i);
+                const int l = v.xdrv ? warp : i;
+                const float4 wu = T.uw[b][c];
+                const float4 wv = T.vw[b][l][lane];
+                const float *r = s + (size_t)T.uj[b][c] * g.nv + T.vq[b][l][lane];
+                const float c0 = fmaf(wv.x, __ldg(r), fmaf(wv.y, __ldg(r + 1), wv.z * __ldg(r + 2)));
+                r += g.nv;
+                const float c1 = fmaf(wv.x, __ldg(r), fmaf(wv.y, __ldg(r + 1), wv.z * __ldg(r + 2)));
+                r += g.nv;
+                const float c2 = fmaf(wv.x, __ldg(r), fmaf(wv.y, __ldg(r + 1), wv.z * __ldg(r + 2)));
+                part[i] = fmaf(wu.x, c0, fmaf(wu.y, c1, wu.z * c2));
+            }
+        } else {
+#pragma unroll 1
+            for (int i = 0; i < BT; ++i) {
+                const int ix = x0 + i;
+                part[i] = 0.f;
+                if (ix < g.nx && iy < g.ny && iz < g.nz) {
+                    const int k = v.xdrv ? ix : iy, io = v.xdrv ? iy : ix;
+                    const float c = cen(g.d_pix, io, no);
+                    part[i] = bp_voxel_view(g, v, s, __ldg(tab + (size_t)ia * nm + io), k, nd,
+                                            v.po * c, v.oo * c, iz);
+                }
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < BT; ++i) grp[i] += part[i];
+        if (++ngrp == FT_GROUP) {
+#pragma unroll
+            for (int i = 0; i < BT; ++i) { acc[i].add(grp[i]); grp[i] = 0.f; }
+            ngrp = 0;
+        }
+    }
+    const float f = 1.0f / ((float)g.na * g.d_pix);
+#pragma unroll
+    for (int i = 0; i < BT; ++i) {
+        acc[i].add(grp[i]);
+        const int ix = x0 + i;
+        if (ix < g.nx && iy < g.ny && iz < g.nz)
+            vol[((size_t)ix * g.ny + iy) * g.nz + iz] = acc[i].s * f;
+    }
 }
 
 int check(const vg_dd3d_geom *g) {
@@ -183,9 +494,11 @@ int check(const vg_dd3d_geom *g) {
 }
 
 int launch_prep(const vg_dd3d_geom *g, const double *trig, void *ws, size_t wsb, cudaStream_t st) {
-    VG_REQUIRE(ws && wsb >= ws_bytes(g) && ((uintptr_t)ws & 7) == 0,
+    VG_REQUIRE(ws && wsb >= ws_bytes(g) && ((uintptr_t)ws & 15) == 0,
                "dd3d: workspace of %zu bytes needed (vg_dd3d_workspace_bytes)", ws_bytes(g));
-    dd3d_prep<<<g->na, 256, 0, st>>>(*g, trig, reinterpret_cast<float2 *>(ws));
+    dd3d_prep<<<g->na, 256, 0, st>>>(*g, trig, reinterpret_cast<float2 *>(ws),
+                                     reinterpret_cast<float4 *>(static_cast<char *>(ws) +
+                                                                tab_bytes(g)));
     return launch_status("dd3d_prep");
 }
 
@@ -203,8 +516,8 @@ extern "C" int vg_dd3d_fp(const vg_dd3d_geom *g, const float *vol, const double 
     cudaStream_t st = as_stream(stream);
     s = launch_prep(g, trig, workspace, workspace_bytes, st);
     if (s) return s;
-    dim3 grid(ceil_div(g->nv, 32), ceil_div(g->nu, 8), g->na);
-    dd3d_fp_kernel<<<grid, dim3(32, 8), 0, st>>>(*g, vol, trig,
+    dim3 grid(ceil_div(g->nv, FT_V), ceil_div(g->nu, FT_U), g->na);
+    dd3d_fp_kernel<<<grid, 256, 0, st>>>(*g, vol, trig,
                                                   reinterpret_cast<const float2 *>(workspace), sino);
     return launch_status("dd3d_fp");
 }
@@ -217,8 +530,10 @@ extern "C" int vg_dd3d_bp(const vg_dd3d_geom *g, const float *sino, const double
     cudaStream_t st = as_stream(stream);
     s = launch_prep(g, trig, workspace, workspace_bytes, st);
     if (s) return s;
-    dim3 grid(ceil_div(g->nz, 32), ceil_div(g->ny, 8), g->nx);
-    dd3d_bp_kernel<<<grid, dim3(32, 8), 0, st>>>(*g, sino, trig,
-                                                  reinterpret_cast<const float2 *>(workspace), vol);
+    dim3 grid(ceil_div(g->nz, BZ), ceil_div(g->ny, BT), ceil_div(g->nx, BT));
+    dd3d_bp_kernel<<<grid, 256, 0, st>>>(
+        *g, sino,
+        reinterpret_cast<const float4 *>(static_cast<const char *>(workspace) + tab_bytes(g)),
+        reinterpret_cast<const float2 *>(workspace), vol);
     return launch_status("dd3d_bp");
 }

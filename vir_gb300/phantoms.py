@@ -162,3 +162,22 @@ def rasterize3d(e: Ellipsoids, n, d_pix=1.0, sub=2) -> np.ndarray:
 def ellipsoid_phantom(n=64, n_obj=20, seed=0, d_pix=1.0, vmax=0.02, sub=2):
     e = random_ellipsoids(n_obj, fov_radius=n * d_pix / 2, seed=seed, vmax=vmax)
     return rasterize3d(e, n, d_pix, sub), e
+
+
+def rasterize3d_device(e: Ellipsoids, n, d_pix=1.0, device="cuda"):
+    """Point-sampled (voxel centres) ellipsoid volume built on the GPU with
+    torch, for volumes too large to rasterize on the host (512^3)."""
+    import torch
+    c = d_pix * (torch.arange(n, device=device, dtype=torch.float32) + 0.5 - n / 2)
+    vol = torch.zeros((n, n, n), device=device, dtype=torch.float32)
+    step = 16
+    for z0 in range(0, n, step):
+        X, Y, Z = torch.meshgrid(c, c, c[z0:z0 + step], indexing="ij")
+        P = torch.stack([X, Y, Z], -1)
+        for i in range(e.val.size):
+            R = torch.tensor(e.R[i], device=device, dtype=torch.float32)
+            ctr = torch.tensor(e.c[i], device=device, dtype=torch.float32)
+            ax = torch.tensor(e.ax[i], device=device, dtype=torch.float32)
+            q = ((P - ctr) @ R.T) / ax
+            vol[:, :, z0:z0 + step] += float(e.val[i]) * ((q * q).sum(-1) <= 1.0)
+    return vol
