@@ -120,47 +120,48 @@ __device__ __noinline__ float fp_cell_line(const vg_dd3d_geom &g, const View3 &v
     return part;
 }
 
-// Forward projection, tiled.  Block = (view, FT_U u-cells x FT_V v-cells).
-// For each line io whose shadow meets the tile, the block stages the
-// voxels under its cells (a k x z tile of the line, zero padded) in shared
-// memory, and one thread per cell row / column forms that cell's overlap
-// weights (at most 3 pixels per u-cell and 3 slices per v-cell, the same
-// float expressions as the backprojector).  Each thread then forms its
-// 4 adjacent u-cells x 2 v-cells as sum_a sum_b ou_a ov_b t[k_a][z_b] from
-// shared memory.  Lines whose tile or weights exceed that capacity take
-// the per-cell global-memory path.  Line sums are added in groups of
-// FT_GROUP lines, each group with compensation.
+// Forward projection, tiled.  Block = (view, FT_U u-cells x FT_V v-cells);
+// thread = 4 adjacent u-cells (warp) x 2 v-cells (lane, lane + 32).  For
+// each line io whose shadow meets the tile, the block tabulates in shared
+// memory the overlap weights of its cells: per u-cell the first pixel and
+// 3 u-overlaps times the line scale, per v-cell the first slice and 3
+// v-overlaps (the same float expressions as the backprojector).  Each cell
+// then sums 3 x 3 voxels of the line (L1-cached reads; lanes on
+// consecutive slices).  Lines where a cell overlaps more than 3 pixels or
+// slices take the per-cell global path.  The tables are double-buffered by
+// line parity, so one barrier per line suffices.  Line sums are added in
+// groups of FT_GROUP lines, each group with compensation.
 constexpr int FT_U = 32, FT_V = 64;
-constexpr int FT_KMAX = 48, FT_ZMAX = 96, FT_ZP = FT_ZMAX + 4;
 constexpr int FT_GROUP = 16;
 
-struct FpTile {
-    float t[(FT_KMAX + 2) * FT_ZP];  // volume tile: row = pixel k - kA, column = slice z - zA
-    float4 uw[FT_U];                 // per u-cell: weights of pixels ka, ka+1, ka+2
-    float4 vw[FT_V];                 // per v-cell: weights of slices za, za+1, za+2
-    int uk[FT_U], vz[FT_V];          // ka - kA, za - zA
-    int wide;
+struct FpTables {
+    float4 uw[2][FT_U];  // per u-cell: weights of pixels k, k+1, k+2 (x line scale)
+    int uk[2][FT_U];
+    float4 vw[2][FT_V];  // per v-cell: weights of slices z, z+1, z+2
+    int vz[2][FT_V];
+    int wide[2];
 };
 
 __global__ void __launch_bounds__(256, 2)
-dd3d_fp_kernel(vg_dd3d_geom g, const float *__restrict__ vol, const double *__restrict__ trig,
+dd3d_fp_kernel(vg_dd3d_geom g, const float *__restrict__ vol, const float4 *__restrict__ vf,
                const float2 *__restrict__ tab, float *__restrict__ sino) {
-    __shared__ FpTile S;
+    __shared__ FpTables S;
     const int ia = blockIdx.z;
     const int u0 = blockIdx.y * FT_U, v0 = blockIdx.x * FT_V;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const View3 v = view3(trig, ia);
+    const View3 v = view_f(vf, ia);
     const int nd = v.xdrv ? g.nx : g.ny;
     const int no = v.xdrv ? g.ny : g.nx;
     const int nm = g.nx > g.ny ? g.nx : g.ny;
     const size_t sk = v.xdrv ? (size_t)g.ny * g.nz : (size_t)g.nz;  // stride of k
     const size_t so = v.xdrv ? (size_t)g.nz : (size_t)g.ny * g.nz;  // stride of io
     const float inv_d = 1.0f / g.d_pix;
-    // the tile's outer u edges and their inverse-map denominators
+    const int kmax = nd - 3, zmax = g.nz - 3;
+    // the tile's outer edges and their inverse-map denominators
     const float TUl = ufloor_edge(g, u0), TUr = ufloor_edge(g, min(u0 + FT_U, g.nu));
     const float TVl = vfloor_edge(g, v0), TVr = vfloor_edge(g, min(v0 + FT_V, g.nv));
     const float rTl = 1.0f / (g.DSD * v.pd + TUl * v.od), rTr = 1.0f / (g.DSD * v.pd + TUr * v.od);
-    // weight threads: tid < FT_U owns u-cell u0 + tid, FT_U <= tid < FT_U + FT_V owns v-cell
+    // table threads: tid < FT_U owns u-cell u0 + tid, FT_U <= tid < FT_U + FT_V a v-cell
     const int wu_i = u0 + tid, wv_i = v0 + tid - FT_U;
     const bool is_u = tid < FT_U && wu_i < g.nu;
     const bool is_v = tid >= FT_U && tid < FT_U + FT_V && wv_i < g.nv;
@@ -170,15 +171,17 @@ dd3d_fp_kernel(vg_dd3d_geom g, const float *__restrict__ vol, const double *__re
         crl = 1.0f / (g.DSD * v.pd + cUl * v.od); crr = 1.0f / (g.DSD * v.pd + cUr * v.od);
     }
     if (is_v) { cVl = vfloor_edge(g, wv_i); cVr = vfloor_edge(g, wv_i + 1); }
+    const bool small = nd < 3 || g.nz < 3;
 
     Kahan acc[8];
     float grp[8];
 #pragma unroll
     for (int c = 0; c < 8; ++c) grp[c] = 0.f;
-    int ngrp = 0;
-    // S.wide == io + 1 marks line io for the global path; writers only ever
-    // store that marker, so no reset races with them
-    if (tid == 0) S.wide = -1;
+    int ngrp = 0, nl = 0;
+    // S.wide[b] == io + 1 marks line io for the global path; writers only
+    // ever store that marker, so no reset races with them
+    if (tid < 2) S.wide[tid] = -1;
+    __syncthreads();
     for (int io = 0; io < no; ++io) {
         const float c = cen(g.d_pix, io, no);
         const float cp = v.po * c, co = v.oo * c;
@@ -187,88 +190,70 @@ dd3d_fp_kernel(vg_dd3d_geom g, const float *__restrict__ vol, const double *__re
         const float kr = fmaf(TUr, g.DSO - co, -g.DSD * cp) * rTr * inv_d + 0.5f * nd;
         const int kA = max(0, (int)floorf(fminf(kl, kr)));
         const int kB = min(nd - 1, (int)floorf(fmaxf(kl, kr)));
-        const int zA = max(0, (int)floorf(TVl / (sz.y * g.d_pix) + 0.5f * g.nz));
-        const int zB = min(g.nz - 1, (int)floorf(TVr / (sz.y * g.d_pix) + 0.5f * g.nz));
+        const float izd = 1.0f / (sz.y * g.d_pix);
+        const int zA = max(0, (int)floorf(TVl * izd + 0.5f * g.nz));
+        const int zB = min(g.nz - 1, (int)floorf(TVr * izd + 0.5f * g.nz));
         if (kA > kB || zA > zB) continue;  // block-uniform
-        const int nk = kB - kA + 1, nzt = zB - zA + 1;
-        const bool fits = nk <= FT_KMAX && nzt <= FT_ZMAX;
-        __syncthreads();  // the previous line's reads of S are done
-        if (fits) {
-            const float *base = vol + (size_t)kA * sk + (size_t)io * so + zA;
-            for (int r = warp; r < nk + 2; r += 8)
-                for (int q = lane; q < nzt + 2; q += 32)
-                    S.t[r * FT_ZP + q] = (r < nk && q < nzt) ? __ldg(base + (size_t)r * sk + q) : 0.f;
-        }
-        if (tid == 0 && !fits) S.wide = io + 1;
-        if (is_u || (tid < FT_U)) {
+        const int b = nl++ & 1;
+        if (tid < FT_U) {
             float4 w = make_float4(0.f, 0.f, 0.f, 0.f);
-            int rel = 0;
-            if (is_u && fits) {
+            int kb0 = 0;
+            if (is_u) {
                 const float a = fmaf(cUl, g.DSO - co, -g.DSD * cp) * crl * inv_d + 0.5f * nd;
-                const float b = fmaf(cUr, g.DSO - co, -g.DSD * cp) * crr * inv_d + 0.5f * nd;
-                const int ka = max(kA, (int)floorf(fminf(a, b)));
-                const int kb = min(kB, (int)floorf(fmaxf(a, b)));
-                if (ka <= kb) {
-                    if (kb - ka > 2) {
-                        S.wide = io + 1;
-                    } else {
-                        float pa = projU(g, v, cp, co, edg(g.d_pix, ka, nd));
-                        float ow[3];
+                const float bb = fmaf(cUr, g.DSO - co, -g.DSD * cp) * crr * inv_d + 0.5f * nd;
+                const int ks = (int)floorf(fminf(a, bb)), ke = (int)floorf(fmaxf(a, bb));
+                if (ke - ks > 2 && ke >= 0 && ks < nd) S.wide[b] = io + 1;
+                kb0 = min(max(ks, 0), max(kmax, 0));
+                float pa = projU(g, v, cp, co, edg(g.d_pix, kb0, nd));
+                float ow[3];
 #pragma unroll
-                        for (int t = 0; t < 3; ++t) {
-                            const float pb = projU(g, v, cp, co, edg(g.d_pix, ka + t + 1, nd));
-                            const float o = fminf(fmaxf(pa, pb), cUr) - fmaxf(fminf(pa, pb), cUl);
-                            ow[t] = (ka + t <= kb && o > 0.f) ? o : 0.f;
-                            pa = pb;
-                        }
-                        w = make_float4(ow[0], ow[1], ow[2], 0.f);
-                        rel = ka - kA;
-                    }
+                for (int t = 0; t < 3; ++t) {
+                    const float pb = projU(g, v, cp, co, edg(g.d_pix, kb0 + t + 1, nd));
+                    const float o = fminf(fmaxf(pa, pb), cUr) - fmaxf(fminf(pa, pb), cUl);
+                    ow[t] = (kb0 + t < nd && o > 0.f) ? o * sz.x : 0.f;
+                    pa = pb;
                 }
+                w = make_float4(ow[0], ow[1], ow[2], 0.f);
             }
-            S.uw[tid] = w;
-            S.uk[tid] = rel;
+            S.uw[b][tid] = w;
+            S.uk[b][tid] = kb0;
         } else if (tid < FT_U + FT_V) {
             float4 w = make_float4(0.f, 0.f, 0.f, 0.f);
-            int rel = 0;
-            if (is_v && fits) {
-                const int za = max(zA, (int)floorf(cVl / (sz.y * g.d_pix) + 0.5f * g.nz));
-                const int zb = min(zB, (int)floorf(cVr / (sz.y * g.d_pix) + 0.5f * g.nz));
-                if (za <= zb) {
-                    if (zb - za > 2) {
-                        S.wide = io + 1;
-                    } else {
-                        float ow[3];
+            int zb0 = 0;
+            if (is_v) {
+                const int zs = (int)floorf(cVl * izd + 0.5f * g.nz);
+                const int ze = (int)floorf(cVr * izd + 0.5f * g.nz);
+                if (ze - zs > 2 && ze >= 0 && zs < g.nz) S.wide[b] = io + 1;
+                zb0 = min(max(zs, 0), max(zmax, 0));
+                float ow[3];
 #pragma unroll
-                        for (int t = 0; t < 3; ++t) {
-                            const float zl = sz.y * edg(g.d_pix, za + t, g.nz);
-                            const float zr = sz.y * edg(g.d_pix, za + t + 1, g.nz);
-                            const float o = fminf(zr, cVr) - fmaxf(zl, cVl);
-                            ow[t] = (za + t <= zb && o > 0.f) ? o : 0.f;
-                        }
-                        w = make_float4(ow[0], ow[1], ow[2], 0.f);
-                        rel = za - zA;
-                    }
+                for (int t = 0; t < 3; ++t) {
+                    const float zl = sz.y * edg(g.d_pix, zb0 + t, g.nz);
+                    const float zr = sz.y * edg(g.d_pix, zb0 + t + 1, g.nz);
+                    const float o = fminf(zr, cVr) - fmaxf(zl, cVl);
+                    ow[t] = (zb0 + t < g.nz && o > 0.f) ? o : 0.f;
                 }
+                w = make_float4(ow[0], ow[1], ow[2], 0.f);
             }
-            S.vw[tid - FT_U] = w;
-            S.vz[tid - FT_U] = rel;
+            S.vw[b][tid - FT_U] = w;
+            S.vz[b][tid - FT_U] = zb0;
         }
         __syncthreads();
         float part[8];
-        if (S.wide != io + 1) {
-            const float4 wa = S.vw[lane], wb = S.vw[32 + lane];
-            const int za = S.vz[lane], zb = S.vz[32 + lane];
+        if (S.wide[b] != io + 1 && !small) {
+            const float4 wa = S.vw[b][lane], wb = S.vw[b][32 + lane];
+            const int za = S.vz[b][lane], zb = S.vz[b][32 + lane];
+            const float *line = vol + (size_t)io * so;
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
-                const float4 wu = S.uw[4 * warp + j];
-                const float *r = S.t + S.uk[4 * warp + j] * FT_ZP;
+                const float4 wu = S.uw[b][4 * warp + j];
+                const float *r = line + (size_t)S.uk[b][4 * warp + j] * sk;
                 float ca = 0.f, cb = 0.f;
 #pragma unroll
                 for (int t = 0; t < 3; ++t) {
-                    const float *q = r + t * FT_ZP;
-                    const float sa = fmaf(wa.x, q[za], fmaf(wa.y, q[za + 1], wa.z * q[za + 2]));
-                    const float sb = fmaf(wb.x, q[zb], fmaf(wb.y, q[zb + 1], wb.z * q[zb + 2]));
+                    const float *q = r + t * sk;
+                    const float sa = fmaf(wa.x, __ldg(q + za), fmaf(wa.y, __ldg(q + za + 1), wa.z * __ldg(q + za + 2)));
+                    const float sb = fmaf(wb.x, __ldg(q + zb), fmaf(wb.y, __ldg(q + zb + 1), wb.z * __ldg(q + zb + 2)));
                     const float wt = t == 0 ? wu.x : (t == 1 ? wu.y : wu.z);
                     ca = fmaf(wt, sa, ca);
                     cb = fmaf(wt, sb, cb);
@@ -277,22 +262,22 @@ dd3d_fp_kernel(vg_dd3d_geom g, const float *__restrict__ vol, const double *__re
                 part[2 * j + 1] = cb;
             }
         } else {
-#pragma unroll
+#pragma unroll 1
             for (int j = 0; j < 4; ++j) {
                 const int iu = u0 + 4 * warp + j;
                 const float Ul = ufloor_edge(g, iu), Ur = ufloor_edge(g, iu + 1);
-#pragma unroll
+#pragma unroll 1
                 for (int h = 0; h < 2; ++h) {
                     const int iv = v0 + 32 * h + lane;
                     part[2 * j + h] = (iu < g.nu && iv < g.nv)
-                        ? fp_cell_line(g, v, vol, sk, so, nd, io, cp, co, sz.y, Ul, Ur,
-                                       vfloor_edge(g, iv), vfloor_edge(g, iv + 1))
+                        ? sz.x * fp_cell_line(g, v, vol, sk, so, nd, io, cp, co, sz.y, Ul, Ur,
+                                              vfloor_edge(g, iv), vfloor_edge(g, iv + 1))
                         : 0.f;
                 }
             }
         }
 #pragma unroll
-        for (int q = 0; q < 8; ++q) grp[q] = fmaf(part[q], sz.x, grp[q]);
+        for (int q = 0; q < 8; ++q) grp[q] += part[q];
         if (++ngrp == FT_GROUP) {
 #pragma unroll
             for (int q = 0; q < 8; ++q) { acc[q].add(grp[q]); grp[q] = 0.f; }
@@ -517,8 +502,10 @@ extern "C" int vg_dd3d_fp(const vg_dd3d_geom *g, const float *vol, const double 
     s = launch_prep(g, trig, workspace, workspace_bytes, st);
     if (s) return s;
     dim3 grid(ceil_div(g->nv, FT_V), ceil_div(g->nu, FT_U), g->na);
-    dd3d_fp_kernel<<<grid, 256, 0, st>>>(*g, vol, trig,
-                                                  reinterpret_cast<const float2 *>(workspace), sino);
+    dd3d_fp_kernel<<<grid, 256, 0, st>>>(
+        *g, vol,
+        reinterpret_cast<const float4 *>(static_cast<const char *>(workspace) + tab_bytes(g)),
+        reinterpret_cast<const float2 *>(workspace), sino);
     return launch_status("dd3d_fp");
 }
 
