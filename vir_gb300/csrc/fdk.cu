@@ -60,39 +60,71 @@ __global__ void fdk_transpose_back(vg_dd3d_geom g, const float *__restrict__ in,
     }
 }
 
+// Thread = FZ consecutive slices of one (x, y) column; the u coordinate,
+// 1 / U and the u interpolation are shared by the column's slices.  The
+// view table is converted to float once per block into shared memory.
+constexpr int FZ = 4;
+
 __global__ void __launch_bounds__(256)
 fdk_bp_kernel(vg_dd3d_geom g, const float *__restrict__ q, const double *__restrict__ trig,
               float scale, float *__restrict__ vol) {
-    const int iz = blockIdx.x * 32 + threadIdx.x;
+    extern __shared__ float2 cs[];  // (cos, sin) per view
+    for (int ia = threadIdx.y * 32 + threadIdx.x; ia < g.na; ia += 256)
+        cs[ia] = make_float2((float)__ldg(trig + 2 * ia), (float)__ldg(trig + 2 * ia + 1));
+    __syncthreads();
+    const int zb = (blockIdx.x * 32 + threadIdx.x) * FZ;
     const int iy = blockIdx.y * 8 + threadIdx.y;
     const int ix = blockIdx.z;
-    if (iz >= g.nz || iy >= g.ny) return;
+    if (zb >= g.nz || iy >= g.ny) return;
     const float x = g.d_pix * ((float)ix + 0.5f - 0.5f * g.nx);
     const float y = g.d_pix * ((float)iy + 0.5f - 0.5f * g.ny);
-    const float z = g.d_pix * ((float)iz + 0.5f - 0.5f * g.nz);
+    float z[FZ];
+#pragma unroll
+    for (int t = 0; t < FZ; ++t) z[t] = g.d_pix * ((float)(zb + t) + 0.5f - 0.5f * g.nz);
     const float iu_off = 0.5f * g.nu - 0.5f - g.su, iv_off = 0.5f * g.nv - 0.5f - g.sv;
     const float idu = 1.0f / g.du, idv = 1.0f / g.dv;
-    Kahan acc;
+    Kahan acc[FZ];
     for (int ia = 0; ia < g.na; ++ia) {
-        const float c = (float)__ldg(trig + 2 * ia), s = (float)__ldg(trig + 2 * ia + 1);
+        const float2 t2 = cs[ia];
+        const float c = t2.x, s = t2.y;
         const float d = g.DSO - fmaf(c, x, s * y);
         const float r = 1.0f / d;
         const float p = fmaf(-s, x, c * y);
         const float tu = g.DSD * p * r * idu + iu_off;
-        const float tv = g.DSD * z * r * idv + iv_off;
-        const float fu = floorf(tu), fv = floorf(tv);
-        const int ju = (int)fu, jv = (int)fv;
-        const float au = tu - fu, av = tv - fv;
-        const float *Q = q + (size_t)ia * g.nu * g.nv;
-        auto at = [&](int j, int k) -> float {
-            return (j >= 0 && j < g.nu && k >= 0 && k < g.nv) ? __ldg(Q + (size_t)j * g.nv + k) : 0.f;
-        };
-        const float val = (1.f - au) * ((1.f - av) * at(ju, jv) + av * at(ju, jv + 1)) +
-                          au * ((1.f - av) * at(ju + 1, jv) + av * at(ju + 1, jv + 1));
+        const float fu = floorf(tu);
+        const int ju = (int)fu;
+        const float au = tu - fu;
         const float Ui = g.DSO * r;  // 1 / U
-        acc.add(val * Ui * Ui);
+        const float w = Ui * Ui;
+        const bool uin = ju >= 0 && ju + 1 < g.nu;
+        const float *Qa = q + (size_t)ia * g.nu * g.nv;
+        const float zr = g.DSD * r * idv;
+#pragma unroll
+        for (int t = 0; t < FZ; ++t) {
+            const float tv = fmaf(z[t], zr, iv_off);
+            const float fv = floorf(tv);
+            const int jv = (int)fv;
+            const float av = tv - fv;
+            float q00, q01, q10, q11;
+            if (uin && jv >= 0 && jv + 1 < g.nv) {
+                const float *Q = Qa + (size_t)ju * g.nv + jv;
+                q00 = __ldg(Q); q01 = __ldg(Q + 1);
+                q10 = __ldg(Q + g.nv); q11 = __ldg(Q + g.nv + 1);
+            } else {
+                auto at = [&](int dj, int k) -> float {
+                    const int j = ju + dj;
+                    return (j >= 0 && j < g.nu && k >= 0 && k < g.nv) ? __ldg(Qa + (size_t)j * g.nv + k) : 0.f;
+                };
+                q00 = at(0, jv); q01 = at(0, jv + 1); q10 = at(1, jv); q11 = at(1, jv + 1);
+            }
+            const float val = (1.f - au) * ((1.f - av) * q00 + av * q01) +
+                              au * ((1.f - av) * q10 + av * q11);
+            acc[t].add(val * w);
+        }
     }
-    vol[((size_t)ix * g.ny + iy) * g.nz + iz] = acc.s * scale;
+#pragma unroll
+    for (int t = 0; t < FZ; ++t)
+        if (zb + t < g.nz) vol[((size_t)ix * g.ny + iy) * g.nz + zb + t] = acc[t].s * scale;
 }
 
 int check(const vg_dd3d_geom *g) {
@@ -133,7 +165,14 @@ extern "C" int vg_fdk_bp(const vg_dd3d_geom *g, const float *q, const double *tr
     if (s) return s;
     VG_REQUIRE(q && trig && vol, "fdk_bp: null pointer");
     const float scale = (float)(3.14159265358979323846 / (2.0 * g->na));
-    dim3 grid(ceil_div(g->nz, 32), ceil_div(g->ny, 8), g->nx);
-    fdk_bp_kernel<<<grid, dim3(32, 8), 0, as_stream(stream)>>>(*g, q, trig, scale, vol);
+    const size_t smem = (size_t)g->na * sizeof(float2);
+    VG_REQUIRE(smem <= 200 * 1024, "fdk_bp: more than 25600 views");
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(fdk_bp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
+        if (e != cudaSuccess) return cuda_status(e, "fdk_bp: shared memory attribute");
+    }
+    dim3 grid(ceil_div(g->nz, 32 * FZ), ceil_div(g->ny, 8), g->nx);
+    fdk_bp_kernel<<<grid, dim3(32, 8), smem, as_stream(stream)>>>(*g, q, trig, scale, vol);
     return launch_status("fdk_bp");
 }
