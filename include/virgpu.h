@@ -266,6 +266,43 @@ int vg_dd_square_sirt_iter(const vg_dd_square_geom *g, const float *y,
                            float *x, float *r, void *workspace,
                            size_t workspace_bytes, void *stream);
 
+/* ---- ray-driven (rd.py) and pixel-driven (pd.py) projectors ------------- */
+
+/* Geometry of sys_mat/rd.py and sys_mat/pd.py: kind 0 = parallel 2D
+ * (image nx x ny), 1 = fan 2D (flat detector at DSD, source at DSO),
+ * 2 = circular cone 3D (volume nx x ny x nz, detector nu x nv, v
+ * fastest).  joseph selects the Joseph sampling of rd.py instead of its
+ * Amanatides-Woo walk (ignored by the pixel-driven pair). */
+typedef struct {
+    int nx, ny, nz, na, nu, nv;
+    float du, dv, su, sv, d_pix, DSO, DSD;
+    int kind, joseph;
+} vg_ray_geom;
+
+/* aw_fp_par_2d / aw_fp_fan_2d / aw_fp_cone_3d (rd.py:450, 544, 652; the
+ * kernels rd.py:112-447): one thread per ray.  trig: float64 (cos, sin) of
+ * the float32 angles.  A ray parallel to an axis is clipped to its slab,
+ * and cone rows use nv (the reference's rd.py:52-64 and :688 do neither). */
+int vg_rd_fp(const vg_ray_geom *g, const float *img, const double *trig,
+             float *sino, void *stream);
+
+/* aw_bp_par_2d / aw_bp_fan_2d / aw_bp_cone_3d (rd.py:461, 556, 665):
+ * scatter along each ray (float atomics), scaled img / na / d_pix^2 * du
+ * (2D) or img / na * du * dv (cone). */
+int vg_rd_bp(const vg_ray_geom *g, const float *sino, const double *trig,
+             float *img, void *stream);
+
+/* pd_fp_par_2d / pd_fp_fan_2d / pd_fp_cone_3d (pd.py:130, 238, 354): each
+ * pixel's footprint scattered into the overlapped bins (float atomics),
+ * sino * d_pix.  trig: float64 (cos, sin) of the angles as given. */
+int vg_pd_fp(const vg_ray_geom *g, const float *img, const double *trig,
+             float *sino, void *stream);
+
+/* pd_bp_par_2d / pd_bp_fan_2d / pd_bp_cone_3d (pd.py:138, 246, 363):
+ * gather per pixel / voxel over views, img / na / d_pix * du (* dv). */
+int vg_pd_bp(const vg_ray_geom *g, const float *sino, const double *trig,
+             float *img, void *stream);
+
 /* ---- FDK (cone-beam filtered backprojection) ----------------------------- */
 
 /* vir has no FDK; these three steps build it on the cone geometry above.

@@ -80,6 +80,11 @@ def lib():
                                          ctypes.c_double]
         L.orc_dd_fp_square.argtypes = [_fp, _ip, _dp, _dp]
         L.orc_dd_bp_square.argtypes = [_fp, _ip, _dp, _dp]
+        i, d = ctypes.c_int, ctypes.c_double
+        L.orc_rd_2d.argtypes = [i, i, i, _fp, _dp, i, i, i, i, _dp, _dp, d, d, d, d, d]
+        L.orc_rd_cone.argtypes = [i, i, _fp, _dp, i, i, i, i, i, i, _dp, _dp, d, d, d, d, d, d, d]
+        L.orc_pd_2d.argtypes = [i, i, _fp, _dp, i, i, i, i, _dp, d, d, d, d, d]
+        L.orc_pd_cone.argtypes = [i, _fp, _dp, i, i, i, i, i, i, _dp, d, d, d, d, d, d, d]
         L.orc_list_fp.argtypes = [_fp, _ip, _fp, _ip, ctypes.c_int, _dp]
         L.orc_list_bp.argtypes = [_fp, _ip, _fp, _ip, ctypes.c_int, ctypes.c_int, _dp]
         L.orc_num_threads.restype = ctypes.c_int
@@ -263,6 +268,107 @@ def dd_bp_square(sino, img_shape, DSO, DSD, du=1.0, dv=1.0, dsrc_p=1.0, dsrc_z=1
     out = np.zeros((nx, ny, nz), np.float64)
     lib().orc_dd_bp_square(_ptr(sino, _fp), _ptr(dims, _ip), _ptr(prm, _dp), _ptr(out, _dp))
     return out
+
+
+# --- ray-driven AW / Joseph (sys_mat/rd.py:40-790) --------------------------
+# The angles are cast to float32 as as_float32 does (rd.py:453, 464, ...).
+
+def _rd2(fan, joseph, bp, a, shape, angs, nu, du, su, d_pix, DSO, DSD):
+    a = _f32(a)
+    c, s = trig(angs, np.float32)
+    f = lambda v: float(np.float32(v))
+    nx, ny = shape
+    out = np.zeros((nx, ny) if bp else (c.size, nu), np.float64)
+    lib().orc_rd_2d(fan, int(joseph), bp, _ptr(a, _fp), _ptr(out, _dp), nx, ny, c.size, nu,
+                    _ptr(c, _dp), _ptr(s, _dp), f(du), f(su), f(d_pix), f(DSO), f(DSD))
+    return out
+
+
+def aw_fp_par_2d(img, ang_arr, nu, du=1.0, su=0.0, d_pix=1.0, joseph=False):
+    return _rd2(0, joseph, 0, img, np.shape(img), ang_arr, int(nu), du, su, d_pix, 0.0, 0.0)
+
+
+def aw_bp_par_2d(sino, ang_arr, img_shape, du=1.0, su=0.0, d_pix=1.0, joseph=False):
+    return _rd2(0, joseph, 1, sino, img_shape, ang_arr, np.shape(sino)[1], du, su, d_pix, 0.0, 0.0)
+
+
+def aw_fp_fan_2d(img, ang_arr, nu, DSO, DSD, du=1.0, su=0.0, d_pix=1.0, joseph=False):
+    return _rd2(1, joseph, 0, img, np.shape(img), ang_arr, int(nu), du, su, d_pix, DSO, DSD)
+
+
+def aw_bp_fan_2d(sino, ang_arr, img_shape, DSO, DSD, du=1.0, su=0.0, d_pix=1.0, joseph=False):
+    return _rd2(1, joseph, 1, sino, img_shape, ang_arr, np.shape(sino)[1], du, su, d_pix, DSO, DSD)
+
+
+def _rd3(joseph, bp, a, shape, angs, nu, nv, DSO, DSD, du, dv, su, sv, d_pix):
+    a = _f32(a)
+    c, s = trig(angs, np.float32)
+    f = lambda v: float(np.float32(v))
+    out = np.zeros(tuple(shape) if bp else (c.size, nu, nv), np.float64)
+    lib().orc_rd_cone(int(joseph), bp, _ptr(a, _fp), _ptr(out, _dp), *[int(v) for v in shape],
+                      c.size, nu, nv, _ptr(c, _dp), _ptr(s, _dp), f(du), f(dv), f(su), f(sv),
+                      f(d_pix), f(DSO), f(DSD))
+    return out
+
+
+def aw_fp_cone_3d(img, ang_arr, nu, nv, DSO, DSD, du=1.0, dv=1.0, su=0.0, sv=0.0, d_pix=1.0,
+                  joseph=False):
+    return _rd3(joseph, 0, img, np.shape(img), ang_arr, int(nu), int(nv), DSO, DSD, du, dv, su,
+                sv, d_pix)
+
+
+def aw_bp_cone_3d(sino, ang_arr, img_shape, DSO, DSD, du=1.0, dv=1.0, su=0.0, sv=0.0, d_pix=1.0,
+                  joseph=False):
+    return _rd3(joseph, 1, sino, img_shape, ang_arr, np.shape(sino)[1], np.shape(sino)[2], DSO, DSD,
+                du, dv, su, sv, d_pix)
+
+
+# --- pixel-driven footprints (sys_mat/pd.py:56-480) --------------------------
+# The angles are used as given (pd.py does not cast them).
+
+def _pd2(fan, bp, a, shape, angs, nu, du, su, d_pix, DSO, DSD):
+    a = _f32(a)
+    ang = np.ascontiguousarray(np.atleast_1d(np.asarray(angs)), np.float64)
+    nx, ny = shape
+    out = np.zeros((nx, ny) if bp else (ang.size, nu), np.float64)
+    lib().orc_pd_2d(fan, bp, _ptr(a, _fp), _ptr(out, _dp), nx, ny, ang.size, nu, _ptr(ang, _dp),
+                    float(du), float(su), float(d_pix), float(DSO), float(DSD))
+    return out
+
+
+def pd_fp_par_2d(img, ang_arr, nu, du=1.0, su=0.0, d_pix=1.0):
+    return _pd2(0, 0, img, np.shape(img), ang_arr, int(nu), du, su, d_pix, 0.0, 0.0)
+
+
+def pd_bp_par_2d(sino, ang_arr, img_shape, du=1.0, su=0.0, d_pix=1.0):
+    return _pd2(0, 1, sino, img_shape, ang_arr, np.shape(sino)[1], du, su, d_pix, 0.0, 0.0)
+
+
+def pd_fp_fan_2d(img, ang_arr, nu, DSO, DSD, du=1.0, su=0.0, d_pix=1.0):
+    return _pd2(1, 0, img, np.shape(img), ang_arr, int(nu), du, su, d_pix, DSO, DSD)
+
+
+def pd_bp_fan_2d(sino, ang_arr, img_shape, DSO, DSD, du=1.0, su=0.0, d_pix=1.0):
+    return _pd2(1, 1, sino, img_shape, ang_arr, np.shape(sino)[1], du, su, d_pix, DSO, DSD)
+
+
+def _pd3(bp, a, shape, angs, nu, nv, DSO, DSD, du, dv, su, sv, d_pix):
+    a = _f32(a)
+    ang = np.ascontiguousarray(np.atleast_1d(np.asarray(angs)), np.float64)
+    out = np.zeros(tuple(shape) if bp else (ang.size, nu, nv), np.float64)
+    lib().orc_pd_cone(bp, _ptr(a, _fp), _ptr(out, _dp), *[int(v) for v in shape], ang.size, nu, nv,
+                      _ptr(ang, _dp), float(du), float(dv), float(su), float(sv), float(d_pix),
+                      float(DSO), float(DSD))
+    return out
+
+
+def pd_fp_cone_3d(img, ang_arr, nu, nv, DSO, DSD, du=1.0, dv=1.0, su=0.0, sv=0.0, d_pix=1.0):
+    return _pd3(0, img, np.shape(img), ang_arr, int(nu), int(nv), DSO, DSD, du, dv, su, sv, d_pix)
+
+
+def pd_bp_cone_3d(sino, ang_arr, img_shape, DSO, DSD, du=1.0, dv=1.0, su=0.0, sv=0.0, d_pix=1.0):
+    return _pd3(1, sino, img_shape, ang_arr, np.shape(sino)[1], np.shape(sino)[2], DSO, DSD, du, dv,
+                su, sv, d_pix)
 
 
 # --- separable footprint (sys_mat/sp.py:12-87, fp_2d_par.py:67-125) -------

@@ -867,6 +867,347 @@ void orc_list_bp(const float *sino, const int32_t *ind, const float *len,
         for (int32_t i = off[r]; i < off[r + 1]; i++) x[ind[i]] += (double)sino[r] * len[i];
 }
 
+/* ------------------------------------------------------------------------ */
+/* Ray-driven Amanatides-Woo and Joseph, sys_mat/rd.py:40-790                */
+/* ------------------------------------------------------------------------ */
+
+#define RD_EPS 1e-6 /* rd.py:42 */
+
+/* _img_bounds (rd.py:46-49): boundaries -+ d n / 2, first centre. */
+static void rd_bounds(int n, double d, double *lo, double *hi, double *c0)
+{
+    *lo = -d * n / 2.0; *hi = d * n / 2.0; *c0 = -d * (n / 2.0 - 0.5);
+}
+
+/* _intersect_bounding (rd.py:52-64), with the axis-parallel case fixed: the
+ * reference returns (-inf, inf) for a ray parallel to the slab wherever it
+ * lies, so rays beside the image walk its edge row (the over-count of
+ * axis-aligned views); here such a ray meets the slab only when
+ * r_min <= r0 < r_max. */
+static void rd_bound(double r0, double dr, double lo, double hi, double *t0, double *t1)
+{
+    if (fabs(dr) > RD_EPS) {
+        double a = (lo - r0) / dr, b = (hi - r0) / dr;
+        *t0 = fmin(a, b); *t1 = fmax(a, b);
+    } else if (r0 >= lo && r0 < hi) {
+        *t0 = -INFINITY; *t1 = INFINITY;
+    } else {
+        *t0 = INFINITY; *t1 = -INFINITY;
+    }
+}
+
+/* _calc_ir0 (rd.py:67-74) */
+static int rd_ir0(double org, double hat, double t, double lo, double hi, double d)
+{
+    double r = org + t * hat;
+    r = fmin(fmax(r, lo + RD_EPS), hi - RD_EPS);
+    return (int)floor((r - lo) / d);
+}
+
+/* _fp_step_init (rd.py:77-109) */
+static void rd_step(double r0, int ir, double dr, double lo, double d, int *dir, double *ts,
+                    double *tn)
+{
+    double rn;
+    if (dr > 0) { *dir = 1; rn = lo + (ir + 1) * d; }
+    else { *dir = -1; rn = lo + ir * d; }
+    if (fabs(dr) > RD_EPS) { *ts = d / fabs(dr); *tn = (rn - r0) / dr; }
+    else { *ts = INFINITY; *tn = INFINITY; }
+}
+
+typedef struct { double org[3], hat[3]; } rd_ray;
+
+/* One ray of the 2D (dim 2) or 3D (dim 3) projectors.  joseph = 0: the
+ * Amanatides-Woo walk of _aw_{fp,bp}_traverse_{2d,3d} (rd.py:112-248);
+ * joseph = 1: the 0.5-step sampling of _joseph_{fp,bp}_{2d,3d}
+ * (rd.py:251-447).  bp = 0 returns the line integral of img; bp = 1 adds
+ * s_val times the ray's weights into bimg. */
+static double rd_trace(int dim, int joseph, const rd_ray *R, const float *img, double *bimg,
+                       double s_val, const int *n, double d)
+{
+    double lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0}, c0[3] = {0, 0, 0};
+    double te = -INFINITY, tx = INFINITY;
+    for (int a = 0; a < dim; a++) {
+        double t0, t1;
+        rd_bounds(n[a], d, &lo[a], &hi[a], &c0[a]);
+        rd_bound(R->org[a], R->hat[a], lo[a], hi[a], &t0, &t1);
+        te = fmax(te, t0); tx = fmin(tx, t1);
+    }
+    if (tx <= te) return 0.0;
+    size_t sy = dim == 3 ? (size_t)n[2] : 1, sx = (size_t)n[1] * sy;
+    double acc = 0.0;
+    if (joseph) {
+        const double step = 0.5;
+        for (double t = te; t <= tx; t += step) {
+            double f[3];
+            for (int a = 0; a < dim; a++) f[a] = (R->org[a] + t * R->hat[a] - c0[a]) / d;
+            if (dim == 2 && !bimg) {               /* rd.py:269-289: clamped bilinear */
+                double fx = fmin(fmax(f[0], 0.0), n[0] - 2.0), fy = fmin(fmax(f[1], 0.0), n[1] - 2.0);
+                int ix = (int)fx, iy = (int)fy;
+                double dx = fx - ix, dy = fy - iy;
+                size_t b = ix * sx + iy;
+                acc += (img[b] * (1 - dx) * (1 - dy) + img[b + sx] * dx * (1 - dy) +
+                        img[b + 1] * (1 - dx) * dy + img[b + sx + 1] * dx * dy) * step;
+            } else if (dim == 3 && !bimg) {        /* rd.py:301-350: truncation, interior only */
+                int ix = (int)f[0], iy = (int)f[1], iz = (int)f[2];
+                if (0 <= ix && ix < n[0] - 1 && 0 <= iy && iy < n[1] - 1 && 0 <= iz && iz < n[2] - 1) {
+                    double dx = f[0] - ix, dy = f[1] - iy, dz = f[2] - iz;
+                    size_t b = ix * sx + iy * sy + iz;
+                    double c00 = img[b] + dx * (img[b + sx] - img[b]);
+                    double c10 = img[b + sy] + dx * (img[b + sx + sy] - img[b + sy]);
+                    double c01 = img[b + 1] + dx * (img[b + sx + 1] - img[b + 1]);
+                    double c11 = img[b + sy + 1] + dx * (img[b + sx + sy + 1] - img[b + sy + 1]);
+                    double c0v = c00 + dy * (c10 - c00), c1v = c01 + dy * (c11 - c01);
+                    acc += (c0v + dz * (c1v - c0v)) * step;
+                }
+            } else {                               /* rd.py:357-447: floor, splat in bounds */
+                int i0[3] = {0, 0, 0};
+                double w0[3] = {1, 1, 1};
+                for (int a = 0; a < dim; a++) { i0[a] = (int)floor(f[a]); w0[a] = f[a] - i0[a]; }
+                for (int c = 0; c < (1 << dim); c++) {
+                    double w = s_val * step;
+                    int ok = 1;
+                    size_t off = 0;
+                    for (int a = 0; a < dim; a++) {
+                        int bit = (c >> a) & 1, i = i0[a] + bit;
+                        if (i < 0 || i >= n[a]) ok = 0;
+                        w *= bit ? w0[a] : 1 - w0[a];
+                        off += (size_t)i * (a == 0 ? sx : (a == 1 ? sy : 1));
+                    }
+                    if (ok) bimg[off] += w;
+                }
+            }
+        }
+        return acc;
+    }
+    int ir[3] = {0, 0, 0}, dir[3] = {0, 0, 0};
+    double ts[3] = {INFINITY, INFINITY, INFINITY}, tn[3] = {INFINITY, INFINITY, INFINITY};
+    for (int a = 0; a < dim; a++) {
+        ir[a] = rd_ir0(R->org[a], R->hat[a], te, lo[a], hi[a], d);
+        if (ir[a] < 0) ir[a] = 0;                  /* entry voxel inside the grid */
+        if (ir[a] > n[a] - 1) ir[a] = n[a] - 1;
+        rd_step(R->org[a], ir[a], R->hat[a], lo[a], d, &dir[a], &ts[a], &tn[a]);
+        if (dim == 2) tn[a] = fmax(tn[a], te);     /* rd.py:116-117, 155-156 */
+    }
+    double t = te;
+    /* 2D FP walks while t <= t_exit (rd.py:126), the others while t < t_exit */
+    while (dim == 2 && !bimg ? t <= tx : t < tx) {
+        int out = 0;
+        for (int a = 0; a < dim; a++) out |= ir[a] < 0 || ir[a] >= n[a];
+        if (out) break;
+        int a = 0;
+        if (dim == 2) a = tn[0] <= tn[1] ? 0 : 1;
+        else a = (tn[0] <= tn[1] && tn[0] <= tn[2]) ? 0 : (tn[1] <= tn[2] ? 1 : 2);
+        double tnext = fmin(tn[a], tx);
+        size_t v = ir[0] * sx + ir[1] * sy + (dim == 3 ? (size_t)ir[2] : 0);
+        if (bimg) bimg[v] += s_val * (tnext - t);
+        else acc += img[v] * (tnext - t);
+        t = tnext;
+        tn[a] += ts[a];
+        ir[a] += dir[a];
+    }
+    return acc;
+}
+
+/* aw_p_par_2d / aw_p_fan_2d (rd.py:473-541, 567-649).  bp = 0: in = img
+ * (nx, ny) -> out = sino (na, nu); bp = 1: in = sino -> out = img, scaled
+ * img / na / d_pix / d_pix * du (rd.py:538, 646). */
+void orc_rd_2d(int fan, int joseph, int bp, const float *in, double *out, int nx, int ny,
+               int na, int nu, const double *cosv, const double *sinv, double du, double su,
+               double d_pix, double DSO, double DSD)
+{
+    int n[2] = {nx, ny};
+    if (bp) memset(out, 0, sizeof(double) * (size_t)nx * ny);
+    for (int ia = 0; ia < na; ia++) {
+        double c = cosv[ia], s = sinv[ia];
+        for (int iu = 0; iu < nu; iu++) {
+            double u = du * ((double)iu - (nu / 2.0 - 0.5) + su);
+            rd_ray R;
+            if (fan) {
+                R.org[0] = DSO * c; R.org[1] = DSO * s;
+                double dx = -(DSD - DSO) * c + u * -s - R.org[0];
+                double dy = -(DSD - DSO) * s + u * c - R.org[1];
+                double m = sqrt(dx * dx + dy * dy);
+                R.hat[0] = dx / m; R.hat[1] = dy / m;
+            } else {
+                R.org[0] = u * -s; R.org[1] = u * c;
+                R.hat[0] = c; R.hat[1] = s;
+            }
+            if (bp) rd_trace(2, joseph, &R, NULL, out, in[(size_t)ia * nu + iu], n, d_pix);
+            else out[(size_t)ia * nu + iu] = rd_trace(2, joseph, &R, in, NULL, 0.0, n, d_pix);
+        }
+    }
+    if (bp)
+        for (size_t i = 0; i < (size_t)nx * ny; i++) out[i] = out[i] / na / d_pix / d_pix * du;
+}
+
+/* aw_p_cone_3d (rd.py:678-790).  The AW forward value is scaled by
+ * DSD / sqrt(DSD^2 + u^2 + v^2) (rd.py:782-783); the back projection
+ * returns img / na * du * dv (rd.py:786).  Detector rows are
+ * dv (iv - (nv/2 - 0.5) + sv): the reference writes nu for nv here
+ * (rd.py:688), which shifts the rows whenever nu != nv. */
+void orc_rd_cone(int joseph, int bp, const float *in, double *out, int nx, int ny, int nz,
+                 int na, int nu, int nv, const double *cosv, const double *sinv, double du,
+                 double dv, double su, double sv, double d_pix, double DSO, double DSD)
+{
+    int n[3] = {nx, ny, nz};
+    size_t nvox = (size_t)nx * ny * nz;
+    if (bp) memset(out, 0, sizeof(double) * nvox);
+    for (int ia = 0; ia < na; ia++) {
+        double c = cosv[ia], s = sinv[ia];
+        for (int iv = 0; iv < nv; iv++) {
+            double v = dv * ((double)iv - (nv / 2.0 - 0.5) + sv);
+            for (int iu = 0; iu < nu; iu++) {
+                double u = du * ((double)iu - (nu / 2.0 - 0.5) + su);
+                rd_ray R;
+                R.org[0] = DSO * c; R.org[1] = DSO * s; R.org[2] = 0.0;
+                double vx = -(DSD - DSO) * c + u * -s - R.org[0];
+                double vy = -(DSD - DSO) * s + u * c - R.org[1];
+                double vz = v;
+                double m = sqrt(vx * vx + vy * vy + vz * vz);
+                R.hat[0] = vx / m; R.hat[1] = vy / m; R.hat[2] = vz / m;
+                size_t k = ((size_t)ia * nu + iu) * nv + iv;
+                if (bp) {
+                    rd_trace(3, joseph, &R, NULL, out, in[k], n, d_pix);
+                } else {
+                    double val = rd_trace(3, joseph, &R, in, NULL, 0.0, n, d_pix);
+                    if (!joseph) val *= DSD / sqrt(DSD * DSD + u * u + v * v);
+                    out[k] = val;
+                }
+            }
+        }
+    }
+    if (bp)
+        for (size_t i = 0; i < nvox; i++) out[i] = out[i] / na * du * dv;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Pixel-driven footprints, sys_mat/pd.py:56-480                             */
+/* ------------------------------------------------------------------------ */
+
+/* pd_p_par_2d / pd_p_fan_2d (pd.py:148-235, 256-351): each pixel's four
+ * corners are projected (parallel: p = -s x + c y; fan: DSD p / (DSO - o));
+ * the bins overlapping [p_min, p_max] get value * overlap / du * scale with
+ * scale 1 / (|sin| + |cos|) (parallel) or 1 / (|cos(a+g)| + |sin(a+g)|),
+ * g = atan(u_c / DSD) of the pixel centre (fan).  FP returns sino * d_pix,
+ * BP img / na / d_pix * du.  The reference's fan FP skips zero pixels
+ * without advancing oy_bnd_l (pd.py:335-339), so the centre of the next
+ * pixel, and its scale, come out wrong after every zero; here every pixel
+ * uses its own centre. */
+void orc_pd_2d(int fan, int bp, const float *in, double *out, int nx, int ny, int na, int nu,
+               const double *angs, double du, double su, double d_pix, double DSO, double DSD)
+{
+    size_t npix = (size_t)nx * ny;
+    if (bp) memset(out, 0, sizeof(double) * npix);
+    else memset(out, 0, sizeof(double) * (size_t)na * nu);
+    for (int ia = 0; ia < na; ia++) {
+        double c = cos(angs[ia]), s = sin(angs[ia]);
+        double pscale = 1.0 / (fabs(s) + fabs(c));
+        for (int ix = 0; ix < nx; ix++) {
+            double xl = d_pix * (ix - nx / 2.0), xr = d_pix * (ix + 1 - nx / 2.0);
+            for (int iy = 0; iy < ny; iy++) {
+                double yl = d_pix * (iy - ny / 2.0), yr = d_pix * (iy + 1 - ny / 2.0);
+                double xs[2] = {xl, xr}, ys[2] = {yl, yr}, p[4];
+                double scale = pscale;
+                for (int a = 0; a < 2; a++)
+                    for (int b = 0; b < 2; b++) {
+                        double pp = -s * xs[a] + c * ys[b];
+                        if (fan) pp = DSD * pp / (DSO - (c * xs[a] + s * ys[b]));
+                        p[2 * b + a] = pp;
+                    }
+                if (fan) {
+                    double xc = 0.5 * (xl + xr), yc = 0.5 * (yl + yr);
+                    double uc = DSD * (-s * xc + c * yc) / (DSO - (c * xc + s * yc));
+                    double g = atan(uc / DSD);
+                    scale = 1.0 / (fabs(cos(angs[ia] + g)) + fabs(sin(angs[ia] + g)));
+                }
+                double pmin = fmin(fmin(p[0], p[1]), fmin(p[2], p[3]));
+                double pmax = fmax(fmax(p[0], p[1]), fmax(p[2], p[3]));
+                int iu0 = (int)floor(pmin / du + nu / 2.0 - su); if (iu0 < 0) iu0 = 0;
+                int iu1 = (int)ceil(pmax / du + nu / 2.0 - su); if (iu1 > nu) iu1 = nu;
+                size_t q = (size_t)ix * ny + iy;
+                if (!bp && in[q] == 0.0f) continue;
+                double acc = 0.0;
+                for (int iu = iu0; iu < iu1; iu++) {
+                    double ub0 = du * (iu - nu / 2.0 + su), ub1 = du * (iu + 1 - nu / 2.0 + su);
+                    double l = fmax(pmin, ub0), r = fmin(pmax, ub1);
+                    if (r <= l) continue;
+                    if (bp) acc += in[(size_t)ia * nu + iu] * (r - l) / du * scale;
+                    else out[(size_t)ia * nu + iu] += in[q] * scale * (r - l) / du;
+                }
+                if (bp) out[q] += acc;
+            }
+        }
+    }
+    if (bp) for (size_t i = 0; i < npix; i++) out[i] = out[i] / na / d_pix * du;
+    else for (size_t i = 0; i < (size_t)na * nu; i++) out[i] *= d_pix;
+}
+
+/* pd_p_cone_3d (pd.py:372-480): per column the fan magnification
+ * m = DSD / (DSO - o_c) of its centre projects the four corners to
+ * u = m (p corner); slices to v = m / cos(g) z, g = atan(u_c / DSD); cells
+ * overlapping [u_min, u_max] x [v_min, v_max] get value * du-overlap / du *
+ * dv-overlap / dv / (|sin| + |cos|).  FP returns sino * d_pix, BP
+ * img / na / d_pix * du * dv. */
+void orc_pd_cone(int bp, const float *in, double *out, int nx, int ny, int nz, int na, int nu,
+                 int nv, const double *angs, double du, double dv, double su, double sv,
+                 double d_pix, double DSO, double DSD)
+{
+    size_t nvox = (size_t)nx * ny * nz, nsino = (size_t)na * nu * nv;
+    memset(out, 0, sizeof(double) * (bp ? nvox : nsino));
+    for (int ia = 0; ia < na; ia++) {
+        double c = cos(angs[ia]), s = sin(angs[ia]);
+        double pscale = 1.0 / (fabs(s) + fabs(c));
+        for (int ix = 0; ix < nx; ix++) {
+            double xl = d_pix * (ix - nx / 2.0), xr = d_pix * (ix + 1 - nx / 2.0);
+            for (int iy = 0; iy < ny; iy++) {
+                double yl = d_pix * (iy - ny / 2.0), yr = d_pix * (iy + 1 - ny / 2.0);
+                double xc = 0.5 * (xl + xr), yc = 0.5 * (yl + yr);
+                double oc = c * xc + s * yc;
+                double uc = DSD * (-s * xc + c * yc) / (DSO - oc);
+                double g = atan(uc / DSD);
+                double fm = DSD / (DSO - oc), cm = fm / cos(g);
+                double uu[4] = {fm * (-s * xl + c * yl), fm * (-s * xr + c * yl),
+                                fm * (-s * xl + c * yr), fm * (-s * xr + c * yr)};
+                double umin = fmin(fmin(uu[0], uu[1]), fmin(uu[2], uu[3]));
+                double umax = fmax(fmax(uu[0], uu[1]), fmax(uu[2], uu[3]));
+                int iu0 = (int)floor((umin - du * (-nu / 2.0 + su)) / du) - 1;
+                int iu1 = (int)floor((umax - du * (-nu / 2.0 + su)) / du) + 2;
+                if (iu0 < 0) iu0 = 0;
+                if (iu1 > nu) iu1 = nu;
+                for (int iz = 0; iz < nz; iz++) {
+                    double zl = d_pix * (iz - nz / 2.0), zr = d_pix * (iz + 1 - nz / 2.0);
+                    double vmin = fmin(cm * zl, cm * zr), vmax = fmax(cm * zl, cm * zr);
+                    int iv0 = (int)floor((vmin - dv * (-nv / 2.0 + sv)) / dv) - 1;
+                    int iv1 = (int)floor((vmax - dv * (-nv / 2.0 + sv)) / dv) + 2;
+                    if (iv0 < 0) iv0 = 0;
+                    if (iv1 > nv) iv1 = nv;
+                    size_t q = ((size_t)ix * ny + iy) * nz + iz;
+                    if (!bp && in[q] == 0.0f) continue;
+                    double acc = 0.0;
+                    for (int iv = iv0; iv < iv1; iv++) {
+                        double vl = fmax(vmin, dv * (iv - nv / 2.0 + sv));
+                        double vr = fmin(vmax, dv * (iv + 1 - nv / 2.0 + sv));
+                        if (vr <= vl) continue;
+                        for (int iu = iu0; iu < iu1; iu++) {
+                            double ul = fmax(umin, du * (iu - nu / 2.0 + su));
+                            double ur = fmin(umax, du * (iu + 1 - nu / 2.0 + su));
+                            if (ur <= ul) continue;
+                            size_t k = ((size_t)ia * nu + iu) * nv + iv;
+                            double w = (ur - ul) / du * (vr - vl) / dv;
+                            if (bp) acc += in[k] * w * pscale;
+                            else out[k] += in[q] * pscale * w;
+                        }
+                    }
+                    if (bp) out[q] += acc;
+                }
+            }
+        }
+    }
+    if (bp) for (size_t i = 0; i < nvox; i++) out[i] = out[i] / na / d_pix * du * dv;
+    else for (size_t i = 0; i < nsino; i++) out[i] *= d_pix;
+}
+
 int orc_num_threads(void)
 {
 #ifdef _OPENMP

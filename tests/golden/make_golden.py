@@ -311,6 +311,57 @@ def main():
                               src_prms=np.array(prms[2]), det_prms=np.array(prms[3]),
                               srt_prms=np.array(prms[4]))
 
+    # --- ray-driven (rd.py) and pixel-driven (pd.py) projectors --------------
+    import vir.sys_mat.rd as rdm
+    import vir.sys_mat.pd as pdm
+    rng = np.random.default_rng(24)
+    img6 = (rng.random((16, 12)) + 0.1).astype(np.float32)   # no zeros (pd.py:335-339)
+    a_par6 = np.linspace(0, np.pi, 10, endpoint=False)        # includes 0 and 90 degrees
+    a_fan6 = np.linspace(0, 2 * np.pi, 10, endpoint=False)
+    vol6 = (rng.random((8, 8, 6)) + 0.1).astype(np.float32)
+    a_cone6 = np.linspace(0, 2 * np.pi, 6, endpoint=False)
+    for j, tag in ((False, "aw"), (True, "joseph")):
+        # nu = 10: every ray inside the image; nu = 14: rays beside it at 0 degrees
+        for nu in (10, 14):
+            sino = rdm.aw_fp_par_2d(img6, a_par6, nu, du=1.0, su=0.2, d_pix=1.0, joseph=j)
+            y = rng.random(sino.shape).astype(np.float32)
+            bp = rdm.aw_bp_par_2d(y, a_par6, img6.shape, du=1.0, su=0.2, d_pix=1.0, joseph=j)
+            out[f"rd_par_{tag}_{nu}"] = dict(img=img6, angs=a_par6, nu=np.int32(nu), du=1.0,
+                                             su=0.2, d_pix=1.0, sino=sino, y=y, bp=bp)
+        sino = rdm.aw_fp_fan_2d(img6, a_fan6, 24, 40.0, 80.0, du=1.3, su=0.1, d_pix=1.0, joseph=j)
+        y = rng.random(sino.shape).astype(np.float32)
+        bp = rdm.aw_bp_fan_2d(y, a_fan6, img6.shape, 40.0, 80.0, du=1.3, su=0.1, d_pix=1.0,
+                              joseph=j)
+        out[f"rd_fan_{tag}"] = dict(img=img6, angs=a_fan6, nu=np.int32(24), DSO=40.0, DSD=80.0,
+                                    du=1.3, su=0.1, d_pix=1.0, sino=sino, y=y, bp=bp)
+        # nu == nv: rd.py:688 builds the rows from nu
+        sino = rdm.aw_fp_cone_3d(vol6, a_cone6, 10, 10, 30.0, 60.0, du=1.5, dv=1.5, su=0.1,
+                                 sv=0.2, d_pix=1.0, joseph=j)
+        y = rng.random(sino.shape).astype(np.float32)
+        bp = rdm.aw_bp_cone_3d(y, a_cone6, vol6.shape, 30.0, 60.0, du=1.5, dv=1.5, su=0.1,
+                               sv=0.2, d_pix=1.0, joseph=j)
+        out[f"rd_cone_{tag}"] = dict(vol=vol6, angs=a_cone6, nu=np.int32(10), nv=np.int32(10),
+                                     DSO=30.0, DSD=60.0, du=1.5, dv=1.5, su=0.1, sv=0.2,
+                                     d_pix=1.0, sino=sino, y=y, bp=bp)
+    sino = pdm.pd_fp_par_2d(img6, a_par6, 20, du=1.1, su=0.2, d_pix=1.0)
+    y = rng.random(sino.shape).astype(np.float32)
+    out["pd_par"] = dict(img=img6, angs=a_par6, nu=np.int32(20), du=1.1, su=0.2, d_pix=1.0,
+                         sino=sino, y=y,
+                         bp=pdm.pd_bp_par_2d(y, a_par6, img6.shape, du=1.1, su=0.2, d_pix=1.0))
+    sino = pdm.pd_fp_fan_2d(img6, a_fan6, 30, 40.0, 80.0, du=1.2, su=0.1, d_pix=1.0)
+    y = rng.random(sino.shape).astype(np.float32)
+    out["pd_fan"] = dict(img=img6, angs=a_fan6, nu=np.int32(30), DSO=40.0, DSD=80.0, du=1.2,
+                         su=0.1, d_pix=1.0, sino=sino, y=y,
+                         bp=pdm.pd_bp_fan_2d(y, a_fan6, img6.shape, 40.0, 80.0, du=1.2, su=0.1,
+                                             d_pix=1.0))
+    sino = pdm.pd_fp_cone_3d(vol6, a_cone6, 14, 12, 30.0, 60.0, du=1.3, dv=1.4, su=0.1, sv=0.2,
+                             d_pix=1.0)
+    y = rng.random(sino.shape).astype(np.float32)
+    out["pd_cone"] = dict(vol=vol6, angs=a_cone6, nu=np.int32(14), nv=np.int32(12), DSO=30.0,
+                          DSD=60.0, du=1.3, dv=1.4, su=0.1, sv=0.2, d_pix=1.0, sino=sino, y=y,
+                          bp=pdm.pd_bp_cone_3d(y, a_cone6, vol6.shape, 30.0, 60.0, du=1.3, dv=1.4,
+                                               su=0.1, sv=0.2, d_pix=1.0))
+
     path = os.path.join(HERE, "golden.npz")
     flat = {}
     for k, d in out.items():

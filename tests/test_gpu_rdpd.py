@@ -1,0 +1,139 @@
+"""GPU ray-driven (Amanatides-Woo / Joseph, sys_mat/rd.py) and pixel-driven
+(sys_mat/pd.py) projectors against the reference's golden vectors and the
+FP64 oracle."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-30)
+
+
+def _call(mod, name, g, bp, joseph=None):
+    kw = {k: float(g[k]) for k in ("du", "su", "d_pix", "dv", "sv") if k in g}
+    if joseph is not None:
+        kw["joseph"] = joseph
+    geo = [float(g["DSO"]), float(g["DSD"])] if "DSO" in g else []
+    x = g["vol"] if "vol" in g else g["img"]
+    if bp:
+        return getattr(mod, name)(g["y"], g["angs"], x.shape, *geo, **kw)
+    det = [int(g["nu"])] + ([int(g["nv"])] if "nv" in g else [])
+    return getattr(mod, name)(x, g["angs"], *det, *geo, **kw)
+
+
+@pytest.mark.parametrize("tag,joseph", [("aw", False), ("joseph", True)])
+def test_rd_golden(vg, golden, tag, joseph):
+    from vir_gb300.sys_mat import rd
+    for case, geo in ((f"rd_par_{tag}_10", "par_2d"), (f"rd_fan_{tag}", "fan_2d"),
+                      (f"rd_cone_{tag}", "cone_3d")):
+        g = golden[case]
+        fp = _call(rd, "aw_fp_" + geo, g, False, joseph)
+        assert fp.dtype == np.float32 and fp.shape == g["sino"].shape
+        assert rel(fp, g["sino"]) < 2e-5, case
+        assert rel(_call(rd, "aw_bp_" + geo, g, True, joseph), g["bp"]) < 2e-5, case
+
+
+@pytest.mark.parametrize("tag,joseph", [("aw", False), ("joseph", True)])
+def test_rd_axis_aligned_fix(vg, golden, orc, tag, joseph):
+    from vir_gb300.sys_mat import rd
+    g = golden[f"rd_par_{tag}_14"]
+    fp = _call(rd, "aw_fp_par_2d", g, False, joseph)
+    assert rel(fp[1:], g["sino"][1:]) < 2e-5            # the reference, off axis
+    assert rel(fp, _call(orc, "aw_fp_par_2d", g, False, joseph)) < 2e-5
+
+
+@pytest.mark.parametrize("case", ["pd_par", "pd_fan", "pd_cone"])
+def test_pd_golden(vg, golden, case):
+    from vir_gb300.sys_mat import pd
+    g = golden[case]
+    geo = case.split("_")[1] + ("_3d" if case == "pd_cone" else "_2d")
+    fp = _call(pd, "pd_fp_" + geo, g, False)
+    assert fp.dtype == np.float32 and fp.shape == g["sino"].shape
+    assert rel(fp, g["sino"]) < 2e-5
+    assert rel(_call(pd, "pd_bp_" + geo, g, True), g["bp"]) < 2e-5
+
+
+@pytest.mark.parametrize("joseph", [False, True])
+def test_rd_2d_vs_oracle(vg, orc, joseph):
+    from vir_gb300 import phantoms as ph
+    from vir_gb300.sys_mat import rd
+    img, _ = ph.ellipse_phantom(96, 8, seed=6, d_pix=0.8, vmax=1.0)
+    angs = np.linspace(0, np.pi, 60, endpoint=False)
+    angf = np.linspace(0, 2 * np.pi, 60, endpoint=False)
+    y = np.random.default_rng(8).random((60, 150)).astype(np.float32)
+    # float32 ray parameters: the fan's t runs from the source (|t| ~ DSO = 150),
+    # so its segment lengths carry ~1e-5 absolute rounding, as the reference's do
+    for name, args, tol in (("par_2d", (angs, 150), 2e-5),
+                            ("fan_2d", (angf, 150, 150.0, 300.0), 1e-4)):
+        kw = dict(du=0.9, su=0.3, d_pix=0.8, joseph=joseph)
+        fp = getattr(rd, "aw_fp_" + name)(img, *args, **kw)
+        assert rel(fp, getattr(orc, "aw_fp_" + name)(img, *args, **kw)) < tol, name
+        bargs = (args[0], img.shape) + args[2:]
+        bp = getattr(rd, "aw_bp_" + name)(y, *bargs, **kw)
+        bo = getattr(orc, "aw_bp_" + name)(y, *bargs, **kw)
+        if joseph:
+            # a ray whose length is within rounding of a multiple of the 0.5 step
+            # gains or loses its last sample, which lies on the image edge: the
+            # border pixels differ by up to one splat, the interior does not
+            assert rel(bp[1:-1, 1:-1], bo[1:-1, 1:-1]) < tol, name
+            assert rel(bp, bo) < 1e-2, name
+        else:
+            assert rel(bp, bo) < tol, name
+
+
+@pytest.mark.parametrize("joseph", [False, True])
+def test_rd_cone_vs_oracle(vg, orc, joseph):
+    """nu != nv: the rows come from nv (rd.py:688 uses nu)."""
+    from vir_gb300.sys_mat import rd
+    rng = np.random.default_rng(9)
+    vol = rng.random((20, 18, 14)).astype(np.float32)
+    angs = np.linspace(0, 2 * np.pi, 16, endpoint=False)
+    kw = dict(du=1.2, dv=1.1, su=0.2, sv=-0.3, d_pix=1.0, joseph=joseph)
+    fp = rd.aw_fp_cone_3d(vol, angs, 36, 28, 50.0, 90.0, **kw)
+    assert rel(fp, orc.aw_fp_cone_3d(vol, angs, 36, 28, 50.0, 90.0, **kw)) < 1e-4
+    y = rng.random(fp.shape).astype(np.float32)
+    bp = rd.aw_bp_cone_3d(y, angs, vol.shape, 50.0, 90.0, **kw)
+    assert rel(bp, orc.aw_bp_cone_3d(y, angs, vol.shape, 50.0, 90.0, **kw)) < 1e-4
+
+
+def test_rd_aw_adjoint(vg):
+    """The AW pair is a scaled transpose: BP = A^T y du / (na d_pix^2)."""
+    import torch
+    from vir_gb300.sys_mat import rd
+    g = torch.Generator(device="cuda").manual_seed(2)
+    x = torch.rand((80, 70), device="cuda", generator=g)
+    y = torch.rand((45, 120), device="cuda", generator=g)
+    angs = np.linspace(0, 2 * np.pi, 45, endpoint=False)
+    A = rd.aw_fp_fan_2d(x, angs, 120, 120.0, 250.0, du=1.1, d_pix=1.0)
+    B = rd.aw_bp_fan_2d(y, angs, (80, 70), 120.0, 250.0, du=1.1, d_pix=1.0)
+    f = float(np.float32(1.1))
+    lhs = (A.double() * y.double()).sum().item()
+    rhs = (x.double() * B.double()).sum().item() * 45 / f
+    assert abs(lhs - rhs) / lhs < 1e-5
+
+
+def test_pd_vs_oracle(vg, orc):
+    from vir_gb300 import phantoms as ph
+    from vir_gb300.sys_mat import pd
+    img, _ = ph.ellipse_phantom(64, 6, seed=7, d_pix=1.0, vmax=1.0)
+    angs = np.linspace(0, np.pi, 40, endpoint=False)
+    angf = np.linspace(0, 2 * np.pi, 40, endpoint=False)
+    y = np.random.default_rng(10).random((40, 100)).astype(np.float32)
+    for name, args in (("par_2d", (angs, 100)), ("fan_2d", (angf, 100, 100.0, 200.0))):
+        kw = dict(du=1.1, su=0.2, d_pix=1.0)
+        fp = getattr(pd, "pd_fp_" + name)(img, *args, **kw)
+        assert rel(fp, getattr(orc, "pd_fp_" + name)(img, *args, **kw)) < 2e-5, name
+        bargs = (args[0], img.shape) + args[2:]
+        bp = getattr(pd, "pd_bp_" + name)(y, *bargs, **kw)
+        assert rel(bp, getattr(orc, "pd_bp_" + name)(y, *bargs, **kw)) < 2e-5, name
+    vol = np.random.default_rng(11).random((16, 16, 12)).astype(np.float32)
+    a3 = np.linspace(0, 2 * np.pi, 12, endpoint=False)
+    kw = dict(du=1.2, dv=1.3, su=0.1, sv=0.2, d_pix=1.0)
+    fp = pd.pd_fp_cone_3d(vol, a3, 30, 24, 40.0, 80.0, **kw)
+    assert rel(fp, orc.pd_fp_cone_3d(vol, a3, 30, 24, 40.0, 80.0, **kw)) < 2e-5
+    ys = np.random.default_rng(12).random(fp.shape).astype(np.float32)
+    bp = pd.pd_bp_cone_3d(ys, a3, vol.shape, 40.0, 80.0, **kw)
+    assert rel(bp, orc.pd_bp_cone_3d(ys, a3, vol.shape, 40.0, 80.0, **kw)) < 2e-5

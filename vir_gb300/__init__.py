@@ -30,6 +30,12 @@ _DROP_INS = {
     "sys_mat.sirt_numba": {n: "vir_gb300.sys_mat.sirt_dd:" + n
                            for n in ("sirt", "fast_divide1", "fast_divide2")},
     "sys_mat.sp": {"sf_fp_fan_2d": "vir_gb300.sys_mat.sp:sf_fp_fan_2d"},
+    "sys_mat.rd": {n: "vir_gb300.sys_mat.rd:" + n for n in
+                   ("aw_fp_par_2d", "aw_bp_par_2d", "aw_fp_fan_2d", "aw_bp_fan_2d",
+                    "aw_fp_cone_3d", "aw_bp_cone_3d")},
+    "sys_mat.pd": {n: "vir_gb300.sys_mat.pd:" + n for n in
+                   ("pd_fp_par_2d", "pd_bp_par_2d", "pd_fp_fan_2d", "pd_bp_fan_2d",
+                    "pd_fp_cone_3d", "pd_bp_cone_3d")},
     "sys_mat.fp_2d_par": {n: "vir_gb300.sys_mat.fp_2d_par:" + n
                           for n in ("siddons_fp_2d", "separable_footprint_fp_2d")},
     "filtration": {"filter_sino": "vir_gb300.filtration:filter_sino"},

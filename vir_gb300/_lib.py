@@ -64,6 +64,14 @@ class DDSquareGeom(ctypes.Structure):
                 ("sv", c_float), ("ssrc_p", c_float), ("ssrc_z", c_float), ("d_pix", c_float)]
 
 
+class RayGeom(ctypes.Structure):
+    """vg_ray_geom (include/virgpu.h)."""
+    _fields_ = [("nx", c_int), ("ny", c_int), ("nz", c_int), ("na", c_int), ("nu", c_int),
+                ("nv", c_int), ("du", c_float), ("dv", c_float), ("su", c_float),
+                ("sv", c_float), ("d_pix", c_float), ("DSO", c_float), ("DSD", c_float),
+                ("kind", c_int), ("joseph", c_int)]
+
+
 # name -> argtypes (all return int status)
 _PROTOS = {
     "vg_siddon2d_fp": [c_void_p, c_int, c_int, c_void_p, c_int, c_int, c_double, c_double,
@@ -93,6 +101,10 @@ _PROTOS = {
                         c_void_p],
     "vg_dd_square_sirt_iter": [ctypes.POINTER(DDSquareGeom), c_void_p, c_void_p, c_void_p,
                                c_float, c_void_p, c_void_p, c_void_p, c_size_t, c_void_p],
+    "vg_rd_fp": [ctypes.POINTER(RayGeom), c_void_p, c_void_p, c_void_p, c_void_p],
+    "vg_rd_bp": [ctypes.POINTER(RayGeom), c_void_p, c_void_p, c_void_p, c_void_p],
+    "vg_pd_fp": [ctypes.POINTER(RayGeom), c_void_p, c_void_p, c_void_p, c_void_p],
+    "vg_pd_bp": [ctypes.POINTER(RayGeom), c_void_p, c_void_p, c_void_p, c_void_p],
     "vg_fdk_weight_transpose": [ctypes.POINTER(DD3DGeom), c_void_p, c_void_p, c_void_p],
     "vg_fdk_transpose_back": [ctypes.POINTER(DD3DGeom), c_void_p, c_void_p, c_void_p],
     "vg_fdk_bp": [ctypes.POINTER(DD3DGeom), c_void_p, c_void_p, c_void_p, c_void_p],

@@ -1,0 +1,437 @@
+// Ray-driven (Amanatides-Woo walk, Joseph sampling; sys_mat/rd.py) and
+// pixel-driven footprint (sys_mat/pd.py) projector pairs for the parallel
+// and fan 2D and circular cone 3D geometries.
+//
+// Ray-driven: one thread per ray in float32 with the reference's
+// formulas.  Parallel rays start at u (-sin, cos) with direction
+// (cos, sin) (rd.py:490-499); fan/cone rays run from the source
+// DSO (cos, sin, 0) to the detector point -(DSD - DSO)(cos, sin) +
+// u (-sin, cos) + v z (rd.py:584-603, 701-730); u = du (iu - (nu/2 - 0.5) +
+// su), v the same with nv.  The forward projection gathers along the ray;
+// the back projection (vir's own scatter, rd.py:152-176, 357-447) adds with
+// float atomics, so its summation order is not fixed.  Two defects of the
+// reference are not reproduced: a ray parallel to an axis is clipped to
+// the slab it lies in (the reference's _intersect_bounding never clips
+// it, rd.py:52-64, so rays beside the image walk its edge row), and the
+// cone's detector rows use nv (rd.py:688 uses nu).  Every walk is bounded
+// by an iteration count derived from the volume size.
+//
+// Pixel-driven: the back projection is a gather, one thread per pixel or
+// voxel over all views; the forward projection scatters each pixel's
+// footprint into the 1-4 overlapped bins with float atomics, as the
+// reference's loop does (pd.py:56-127).  The fan scale 1 / (|cos(a + g)| +
+// |sin(a + g)|) with g = atan(u_c / DSD) is evaluated through
+// cos(a + g) = (c - s t) / sqrt(1 + t^2), sin(a + g) = (s + c t) /
+// sqrt(1 + t^2), t = u_c / DSD, and the cone's 1 / cos(g) as sqrt(1 + t^2).
+#include <math.h>
+
+#include "vg_common.cuh"
+
+namespace {
+
+using namespace vg;
+
+constexpr float RD_EPS = 1e-6f;  // rd.py:42
+
+struct Ray {
+    float o[3], h[3];
+};
+
+__device__ __forceinline__ void bounds1(int n, float d, float &lo, float &hi, float &c0) {
+    lo = -d * (float)n / 2.f;
+    hi = d * (float)n / 2.f;
+    c0 = -d * ((float)n / 2.f - 0.5f);
+}
+
+// _intersect_bounding with the axis-parallel ray clipped to its slab
+__device__ __forceinline__ void slab(float r0, float dr, float lo, float hi, float &t0, float &t1) {
+    if (fabsf(dr) > RD_EPS) {
+        const float a = (lo - r0) / dr, b = (hi - r0) / dr;
+        t0 = fminf(a, b);
+        t1 = fmaxf(a, b);
+    } else if (r0 >= lo && r0 < hi) {
+        t0 = -INFINITY;
+        t1 = INFINITY;
+    } else {
+        t0 = INFINITY;
+        t1 = -INFINITY;
+    }
+}
+
+// One ray: returns the line integral (BP = false) or adds s times the
+// ray's weights into bimg (BP = true).  DIM 2 or 3; img is x-major with
+// z fastest.
+template <int DIM, bool JOSEPH, bool BP>
+__device__ float trace(const Ray &R, const float *__restrict__ img, float *__restrict__ bimg,
+                       float s, const int *n, float d) {
+    float lo[3] = {0.f, 0.f, 0.f}, hi[3] = {0.f, 0.f, 0.f}, c0[3] = {0.f, 0.f, 0.f};
+    float te = -INFINITY, tx = INFINITY;
+#pragma unroll
+    for (int a = 0; a < DIM; ++a) {
+        float t0, t1;
+        bounds1(n[a], d, lo[a], hi[a], c0[a]);
+        slab(R.o[a], R.h[a], lo[a], hi[a], t0, t1);
+        te = fmaxf(te, t0);
+        tx = fminf(tx, t1);
+    }
+    if (!(tx > te)) return 0.f;
+    const size_t sy = DIM == 3 ? (size_t)n[2] : 1, sx = (size_t)n[1] * sy;
+    float acc = 0.f;
+    if (JOSEPH) {
+        const float step = 0.5f;
+        // samples at t = te + k / 2 <= tx (the reference's t += step; its float32
+        // running sum drifts from te + k / 2 over a ray, this does not)
+        const int cap = (int)fminf((tx - te) / step, 4.f * (n[0] + n[1] + (DIM == 3 ? n[2] : 0))) + 2;
+        for (int it = 0; it < cap; ++it) {
+            const float t = fmaf((float)it, step, te);
+            if (!(t <= tx)) break;
+            float f[3];
+#pragma unroll
+            for (int a = 0; a < DIM; ++a) f[a] = (R.o[a] + t * R.h[a] - c0[a]) / d;
+            if (!BP && DIM == 2) {  // rd.py:269-289: clamped bilinear
+                const float fx = fminf(fmaxf(f[0], 0.f), n[0] - 2.f);
+                const float fy = fminf(fmaxf(f[1], 0.f), n[1] - 2.f);
+                const int ix = (int)fx, iy = (int)fy;
+                const float dx = fx - ix, dy = fy - iy;
+                const float *b = img + ix * sx + iy;
+                acc += (__ldg(b) * (1 - dx) * (1 - dy) + __ldg(b + sx) * dx * (1 - dy) +
+                        __ldg(b + 1) * (1 - dx) * dy + __ldg(b + sx + 1) * dx * dy) * step;
+            } else if (!BP) {  // rd.py:301-350: truncation, interior cells only
+                const int ix = (int)f[0], iy = (int)f[1], iz = (int)f[2];
+                if (0 <= ix && ix < n[0] - 1 && 0 <= iy && iy < n[1] - 1 && 0 <= iz && iz < n[2] - 1) {
+                    const float dx = f[0] - ix, dy = f[1] - iy, dz = f[2] - iz;
+                    const float *b = img + ix * sx + iy * sy + iz;
+                    const float c00 = __ldg(b) + dx * (__ldg(b + sx) - __ldg(b));
+                    const float c10 = __ldg(b + sy) + dx * (__ldg(b + sx + sy) - __ldg(b + sy));
+                    const float c01 = __ldg(b + 1) + dx * (__ldg(b + sx + 1) - __ldg(b + 1));
+                    const float c11 = __ldg(b + sy + 1) + dx * (__ldg(b + sx + sy + 1) - __ldg(b + sy + 1));
+                    const float c0v = c00 + dy * (c10 - c00), c1v = c01 + dy * (c11 - c01);
+                    acc += (c0v + dz * (c1v - c0v)) * step;
+                }
+            } else {  // rd.py:357-447: floor, splat where in bounds
+                int i0[3] = {0, 0, 0};
+                float w0[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+                for (int a = 0; a < DIM; ++a) {
+                    i0[a] = (int)floorf(f[a]);
+                    w0[a] = f[a] - i0[a];
+                }
+#pragma unroll
+                for (int c = 0; c < (1 << DIM); ++c) {
+                    float w = s * step;
+                    bool ok = true;
+                    size_t off = 0;
+#pragma unroll
+                    for (int a = 0; a < DIM; ++a) {
+                        const int bit = (c >> a) & 1, i = i0[a] + bit;
+                        ok = ok && i >= 0 && i < n[a];
+                        w *= bit ? w0[a] : 1.f - w0[a];
+                        off += (size_t)i * (a == 0 ? sx : (a == 1 ? sy : 1));
+                    }
+                    if (ok) atomicAdd(bimg + off, w);
+                }
+            }
+        }
+        return acc;
+    }
+    int ir[3] = {0, 0, 0}, dir[3] = {0, 0, 0};
+    float ts[3] = {INFINITY, INFINITY, INFINITY}, tn[3] = {INFINITY, INFINITY, INFINITY};
+#pragma unroll
+    for (int a = 0; a < DIM; ++a) {
+        // _calc_ir0 and _fp_step_init (rd.py:67-109)
+        float r = R.o[a] + te * R.h[a];
+        r = fminf(fmaxf(r, lo[a] + RD_EPS), hi[a] - RD_EPS);
+        // entry voxel; r - hi may round to 0 in float32 (hi - eps == hi), so the
+        // index is clamped to the grid (the reference's walk would stop there)
+        ir[a] = min(max((int)floorf((r - lo[a]) / d), 0), n[a] - 1);
+        float rn;
+        if (R.h[a] > 0) { dir[a] = 1; rn = lo[a] + (ir[a] + 1) * d; }
+        else { dir[a] = -1; rn = lo[a] + ir[a] * d; }
+        if (fabsf(R.h[a]) > RD_EPS) { ts[a] = d / fabsf(R.h[a]); tn[a] = (rn - R.o[a]) / R.h[a]; }
+        if (DIM == 2) tn[a] = fmaxf(tn[a], te);  // rd.py:116-117, 155-156
+    }
+    float t = te;
+    const int cap = n[0] + n[1] + (DIM == 3 ? n[2] : 0) + 4;
+    for (int it = 0; it < cap; ++it) {
+        // the 2D forward walks while t <= t_exit (rd.py:126), the others while t < t_exit
+        if (DIM == 2 && !BP ? !(t <= tx) : !(t < tx)) break;
+        bool out = false;
+#pragma unroll
+        for (int a = 0; a < DIM; ++a) out = out || ir[a] < 0 || ir[a] >= n[a];
+        if (out) break;
+        int a;
+        if (DIM == 2) a = tn[0] <= tn[1] ? 0 : 1;
+        else a = (tn[0] <= tn[1] && tn[0] <= tn[2]) ? 0 : (tn[1] <= tn[2] ? 1 : 2);
+        const float tnext = fminf(tn[a], tx);
+        const size_t v = ir[0] * sx + ir[1] * sy + (DIM == 3 ? (size_t)ir[2] : 0);
+        if (BP) atomicAdd(bimg + v, s * (tnext - t));
+        else acc += __ldg(img + v) * (tnext - t);
+        t = tnext;
+        tn[a] += ts[a];
+        ir[a] += dir[a];
+    }
+    return acc;
+}
+
+__device__ __forceinline__ void make_ray(const vg_ray_geom &g, float c, float s, float u, float v,
+                                         Ray &R) {
+    if (g.kind == 0) {
+        R.o[0] = u * -s; R.o[1] = u * c; R.o[2] = 0.f;
+        R.h[0] = c; R.h[1] = s; R.h[2] = 0.f;
+        return;
+    }
+    R.o[0] = g.DSO * c; R.o[1] = g.DSO * s; R.o[2] = 0.f;
+    const float vx = -(g.DSD - g.DSO) * c + u * -s - R.o[0];
+    const float vy = -(g.DSD - g.DSO) * s + u * c - R.o[1];
+    const float vz = g.kind == 2 ? v : 0.f;
+    const float m = sqrtf(vx * vx + vy * vy + vz * vz);
+    R.h[0] = vx / m; R.h[1] = vy / m; R.h[2] = vz / m;
+}
+
+template <int DIM, bool JOSEPH, bool BP>
+__global__ void __launch_bounds__(256)
+rd_kernel(vg_ray_geom g, const double *__restrict__ trig, const float *__restrict__ in,
+          float *__restrict__ out, float bp_scale) {
+    const int iv = DIM == 3 ? (int)(blockIdx.x * blockDim.x + threadIdx.x) : 0;
+    const int iu = DIM == 3 ? (int)blockIdx.y : (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    const int ia = DIM == 3 ? (int)blockIdx.z : (int)blockIdx.y;
+    const int nv = DIM == 3 ? g.nv : 1;
+    if (iu >= g.nu || iv >= nv) return;
+    const float c = (float)__ldg(trig + 2 * ia), s = (float)__ldg(trig + 2 * ia + 1);
+    const float u = g.du * ((float)iu - ((float)g.nu / 2.f - 0.5f) + g.su);
+    const float v = g.dv * ((float)iv - ((float)g.nv / 2.f - 0.5f) + g.sv);
+    Ray R;
+    make_ray(g, c, s, u, v, R);
+    const int n[3] = {g.nx, g.ny, g.nz};
+    const size_t k = ((size_t)ia * g.nu + iu) * nv + iv;
+    if (BP) {
+        trace<DIM, JOSEPH, true>(R, nullptr, out, __ldg(in + k) * bp_scale, n, g.d_pix);
+    } else {
+        float val = trace<DIM, JOSEPH, false>(R, in, nullptr, 0.f, n, g.d_pix);
+        if (DIM == 3 && !JOSEPH) val *= g.DSD / sqrtf(g.DSD * g.DSD + u * u + v * v);  // rd.py:782
+        out[k] = val;
+    }
+}
+
+// ---- pixel-driven ------------------------------------------------------------
+
+struct Foot {
+    float pmin, pmax, scale;  // detector interval and the pixel's weight scale
+    float cm;                 // cone: v magnification
+};
+
+// The pixel's footprint on the detector for view (c, s) (pd.py:186-206,
+// 296-330, 405-445).
+__device__ __forceinline__ Foot footprint(const vg_ray_geom &g, float c, float s, int ix, int iy) {
+    const float xl = g.d_pix * ((float)ix - g.nx / 2.f), xr = g.d_pix * ((float)(ix + 1) - g.nx / 2.f);
+    const float yl = g.d_pix * ((float)iy - g.ny / 2.f), yr = g.d_pix * ((float)(iy + 1) - g.ny / 2.f);
+    Foot f;
+    f.scale = 1.f / (fabsf(s) + fabsf(c));
+    f.cm = 1.f;
+    float p[4];
+    if (g.kind == 0) {
+        p[0] = -s * xl + c * yl; p[1] = -s * xr + c * yl;
+        p[2] = -s * xl + c * yr; p[3] = -s * xr + c * yr;
+    } else {
+        const float xc = 0.5f * (xl + xr), yc = 0.5f * (yl + yr);
+        const float oc = c * xc + s * yc;
+        const float t = (g.DSD * (-s * xc + c * yc) / (g.DSO - oc)) / g.DSD;  // tan g
+        const float sec = sqrtf(1.f + t * t);
+        if (g.kind == 1) {
+            auto pj = [&](float x, float y) { return g.DSD * (-s * x + c * y) / (g.DSO - (c * x + s * y)); };
+            p[0] = pj(xl, yl); p[1] = pj(xr, yl); p[2] = pj(xl, yr); p[3] = pj(xr, yr);
+            f.scale = sec / (fabsf(c - s * t) + fabsf(s + c * t));
+        } else {
+            const float fm = g.DSD / (g.DSO - oc);
+            p[0] = fm * (-s * xl + c * yl); p[1] = fm * (-s * xr + c * yl);
+            p[2] = fm * (-s * xl + c * yr); p[3] = fm * (-s * xr + c * yr);
+            f.cm = fm * sec;
+        }
+    }
+    f.pmin = fminf(fminf(p[0], p[1]), fminf(p[2], p[3]));
+    f.pmax = fmaxf(fmaxf(p[0], p[1]), fmaxf(p[2], p[3]));
+    return f;
+}
+
+__device__ __forceinline__ float ubnd(const vg_ray_geom &g, int k) {
+    return g.du * ((float)k - g.nu / 2.f + g.su);
+}
+__device__ __forceinline__ float vbnd(const vg_ray_geom &g, int k) {
+    return g.dv * ((float)k - g.nv / 2.f + g.sv);
+}
+
+// FP: thread = (view, pixel column); scatters value * scale * overlap / du
+// (* dv overlap / dv) * d_pix.
+__global__ void __launch_bounds__(256)
+pd_fp_kernel(vg_ray_geom g, const double *__restrict__ trig, const float *__restrict__ img,
+             float *__restrict__ sino) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    const int ia = blockIdx.y;
+    if (p >= g.nx * g.ny) return;
+    const int ix = p / g.ny, iy = p - ix * g.ny;
+    const float c = (float)__ldg(trig + 2 * ia), s = (float)__ldg(trig + 2 * ia + 1);
+    const Foot f = footprint(g, c, s, ix, iy);
+    const int iu0 = max(0, (int)floorf((f.pmin - ubnd(g, 0)) / g.du) - 1);
+    const int iu1 = min(g.nu, (int)floorf((f.pmax - ubnd(g, 0)) / g.du) + 2);
+    if (g.kind < 2) {
+        const float val = __ldg(img + p);
+        if (val == 0.f) return;
+        for (int iu = iu0; iu < iu1; ++iu) {
+            const float l = fmaxf(f.pmin, ubnd(g, iu)), r = fminf(f.pmax, ubnd(g, iu + 1));
+            if (r > l) atomicAdd(sino + (size_t)ia * g.nu + iu, val * f.scale * (r - l) / g.du * g.d_pix);
+        }
+        return;
+    }
+    const float *col = img + (size_t)p * g.nz;
+    for (int iz = 0; iz < g.nz; ++iz) {
+        const float val = __ldg(col + iz);
+        if (val == 0.f) continue;
+        const float zl = g.d_pix * ((float)iz - g.nz / 2.f), zr = g.d_pix * ((float)(iz + 1) - g.nz / 2.f);
+        const float vmin = fminf(f.cm * zl, f.cm * zr), vmax = fmaxf(f.cm * zl, f.cm * zr);
+        const int iv0 = max(0, (int)floorf((vmin - vbnd(g, 0)) / g.dv) - 1);
+        const int iv1 = min(g.nv, (int)floorf((vmax - vbnd(g, 0)) / g.dv) + 2);
+        for (int iv = iv0; iv < iv1; ++iv) {
+            const float vl = fmaxf(vmin, vbnd(g, iv)), vr = fminf(vmax, vbnd(g, iv + 1));
+            if (vr <= vl) continue;
+            for (int iu = iu0; iu < iu1; ++iu) {
+                const float ul = fmaxf(f.pmin, ubnd(g, iu)), ur = fminf(f.pmax, ubnd(g, iu + 1));
+                if (ur > ul)
+                    atomicAdd(sino + ((size_t)ia * g.nu + iu) * g.nv + iv,
+                              val * f.scale * ((ur - ul) / g.du * (vr - vl) / g.dv) * g.d_pix);
+            }
+        }
+    }
+}
+
+// BP: thread = pixel / voxel (lanes along z for the cone), gather over views.
+__global__ void __launch_bounds__(256)
+pd_bp_kernel(vg_ray_geom g, const double *__restrict__ trig, const float *__restrict__ sino,
+             float *__restrict__ img, float scale) {
+    const int nz = g.kind == 2 ? g.nz : 1;
+    const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= (size_t)g.nx * g.ny * nz) return;
+    const int iz = (int)(q % nz);
+    const int p = (int)(q / nz), ix = p / g.ny, iy = p - ix * g.ny;
+    const float zl = g.d_pix * ((float)iz - g.nz / 2.f), zr = g.d_pix * ((float)(iz + 1) - g.nz / 2.f);
+    Kahan acc;
+    for (int ia = 0; ia < g.na; ++ia) {
+        const float c = (float)__ldg(trig + 2 * ia), s = (float)__ldg(trig + 2 * ia + 1);
+        const Foot f = footprint(g, c, s, ix, iy);
+        const int iu0 = max(0, (int)floorf((f.pmin - ubnd(g, 0)) / g.du) - 1);
+        const int iu1 = min(g.nu, (int)floorf((f.pmax - ubnd(g, 0)) / g.du) + 2);
+        float part = 0.f;
+        if (g.kind < 2) {
+            const float *row = sino + (size_t)ia * g.nu;
+            for (int iu = iu0; iu < iu1; ++iu) {
+                const float l = fmaxf(f.pmin, ubnd(g, iu)), r = fminf(f.pmax, ubnd(g, iu + 1));
+                if (r > l) part += __ldg(row + iu) * (r - l) / g.du * f.scale;
+            }
+        } else {
+            const float vmin = fminf(f.cm * zl, f.cm * zr), vmax = fmaxf(f.cm * zl, f.cm * zr);
+            const int iv0 = max(0, (int)floorf((vmin - vbnd(g, 0)) / g.dv) - 1);
+            const int iv1 = min(g.nv, (int)floorf((vmax - vbnd(g, 0)) / g.dv) + 2);
+            for (int iv = iv0; iv < iv1; ++iv) {
+                const float vl = fmaxf(vmin, vbnd(g, iv)), vr = fminf(vmax, vbnd(g, iv + 1));
+                if (vr <= vl) continue;
+                for (int iu = iu0; iu < iu1; ++iu) {
+                    const float ul = fmaxf(f.pmin, ubnd(g, iu)), ur = fminf(f.pmax, ubnd(g, iu + 1));
+                    if (ur > ul)
+                        part += __ldg(sino + ((size_t)ia * g.nu + iu) * g.nv + iv) *
+                                ((ur - ul) / g.du * (vr - vl) / g.dv) * f.scale;
+                }
+            }
+        }
+        acc.add(part);
+    }
+    img[q] = acc.s * scale;
+}
+
+int check(const vg_ray_geom *g) {
+    VG_REQUIRE(g, "ray/pixel-driven: null geometry");
+    VG_REQUIRE(g->kind >= 0 && g->kind <= 2, "ray/pixel-driven: kind must be 0 (par), 1 (fan), 2 (cone)");
+    const int nz = g->kind == 2 ? g->nz : 1, nv = g->kind == 2 ? g->nv : 1;
+    VG_REQUIRE(g->nx >= 2 && g->ny >= 2 && nz >= 1 && g->na > 0 && g->nu > 0 && nv > 0,
+               "ray/pixel-driven: sizes must be positive (image at least 2 x 2)");
+    VG_REQUIRE(g->kind < 2 || g->nz >= 2, "ray/pixel-driven: cone volume needs nz >= 2");
+    VG_REQUIRE(g->na < 65536 && g->nu < 65536, "ray/pixel-driven: too many views or bins");
+    VG_REQUIRE((long long)g->nx * g->ny < (1LL << 31), "ray/pixel-driven: image too large");
+    VG_REQUIRE(g->du > 0.f && g->d_pix > 0.f && (g->kind < 2 || g->dv > 0.f),
+               "ray/pixel-driven: pitches must be positive");
+    VG_REQUIRE(g->kind == 0 || (g->DSO > 0.f && g->DSD > 0.f), "ray/pixel-driven: DSO, DSD must be positive");
+    return VG_OK;
+}
+
+template <bool JOSEPH, bool BP>
+void launch_rd(const vg_ray_geom &g, const double *trig, const float *in, float *out, float sc,
+               cudaStream_t st) {
+    if (g.kind == 2) {
+        dim3 grid(ceil_div(g.nv, 128), g.nu, g.na);
+        rd_kernel<3, JOSEPH, BP><<<grid, 128, 0, st>>>(g, trig, in, out, sc);
+    } else {
+        dim3 grid(ceil_div(g.nu, 128), g.na);
+        rd_kernel<2, JOSEPH, BP><<<grid, 128, 0, st>>>(g, trig, in, out, sc);
+    }
+}
+
+size_t img_count(const vg_ray_geom *g) {
+    return (size_t)g->nx * g->ny * (g->kind == 2 ? g->nz : 1);
+}
+size_t sino_count(const vg_ray_geom *g) {
+    return (size_t)g->na * g->nu * (g->kind == 2 ? g->nv : 1);
+}
+
+}  // namespace
+
+extern "C" int vg_rd_fp(const vg_ray_geom *g, const float *img, const double *trig, float *sino,
+                        void *stream) {
+    int s = check(g);
+    if (s) return s;
+    VG_REQUIRE(img && trig && sino, "rd_fp: null pointer");
+    cudaStream_t st = as_stream(stream);
+    if (g->joseph) launch_rd<true, false>(*g, trig, img, sino, 1.f, st);
+    else launch_rd<false, false>(*g, trig, img, sino, 1.f, st);
+    return launch_status("rd_fp");
+}
+
+extern "C" int vg_rd_bp(const vg_ray_geom *g, const float *sino, const double *trig, float *img,
+                        void *stream) {
+    int s = check(g);
+    if (s) return s;
+    VG_REQUIRE(img && trig && sino, "rd_bp: null pointer");
+    cudaStream_t st = as_stream(stream);
+    cudaError_t e = cudaMemsetAsync(img, 0, img_count(g) * sizeof(float), st);
+    if (e != cudaSuccess) return cuda_status(e, "rd_bp: clear");
+    // img / na / d_pix^2 * du (rd.py:538, 646); cone img / na * du * dv (rd.py:786)
+    const float sc = g->kind == 2 ? g->du * g->dv / (float)g->na
+                                  : g->du / ((float)g->na * g->d_pix * g->d_pix);
+    if (g->joseph) launch_rd<true, true>(*g, trig, sino, img, sc, st);
+    else launch_rd<false, true>(*g, trig, sino, img, sc, st);
+    return launch_status("rd_bp");
+}
+
+extern "C" int vg_pd_fp(const vg_ray_geom *g, const float *img, const double *trig, float *sino,
+                        void *stream) {
+    int s = check(g);
+    if (s) return s;
+    VG_REQUIRE(img && trig && sino, "pd_fp: null pointer");
+    cudaStream_t st = as_stream(stream);
+    cudaError_t e = cudaMemsetAsync(sino, 0, sino_count(g) * sizeof(float), st);
+    if (e != cudaSuccess) return cuda_status(e, "pd_fp: clear");
+    dim3 grid(ceil_div((long long)g->nx * g->ny, 256), g->na);
+    pd_fp_kernel<<<grid, 256, 0, st>>>(*g, trig, img, sino);
+    return launch_status("pd_fp");
+}
+
+extern "C" int vg_pd_bp(const vg_ray_geom *g, const float *sino, const double *trig, float *img,
+                        void *stream) {
+    int s = check(g);
+    if (s) return s;
+    VG_REQUIRE(img && trig && sino, "pd_bp: null pointer");
+    // img / na / d_pix * du (pd.py:232); cone * dv (pd.py:479)
+    float sc = g->du / ((float)g->na * g->d_pix);
+    if (g->kind == 2) sc *= g->dv;
+    const long long n = (long long)img_count(g);
+    VG_REQUIRE(ceil_div(n, 256) < 2147483647LL, "pd_bp: volume too large");
+    pd_bp_kernel<<<ceil_div(n, 256), 256, 0, as_stream(stream)>>>(*g, trig, sino, img, sc);
+    return launch_status("pd_bp");
+}
