@@ -303,6 +303,24 @@ int vg_pd_fp(const vg_ray_geom *g, const float *img, const double *trig,
 int vg_pd_bp(const vg_ray_geom *g, const float *sino, const double *trig,
              float *img, void *stream);
 
+/* ---- TV-regularised primal-dual solver (tv.py) ---------------------------- */
+
+/* The fused steps of the preconditioned primal-dual loop of tv.py:262-294
+ * for an (nx, ny) image; the projector calls between them are the
+ * caller's.  Gradient and divergence are periodic (np.roll, tv.py:207-224).
+ *   vg_tv_dual:     z += sigma_z grad(u_bar); z <- z / max(1, |z|) per pixel
+ *                   (tv.py:284-285; the projection pyT computes for 2 x 1
+ *                   pairs, tv.py:98-184); z is (2, nx, ny).
+ *   vg_tv_residual: q += sigma_q (Ax - g); q /= (1 + sigma_q lam) (:287-288).
+ *   vg_tv_primal:   u += tau (div z - At q); u_bar = u + theta (u - u_prev)
+ *                   (:291-294). */
+int vg_tv_dual(const float *u_bar, float *z, int nx, int ny, float sigma_z,
+               void *stream);
+int vg_tv_residual(float *q, const float *ax, const float *g, const float *sigma_q,
+                   float lam, size_t n, void *stream);
+int vg_tv_primal(float *u, float *u_bar, const float *z, const float *atq,
+                 const float *tau, float theta, int nx, int ny, void *stream);
+
 /* ---- FDK (cone-beam filtered backprojection) ----------------------------- */
 
 /* vir has no FDK; these three steps build it on the cone geometry above.

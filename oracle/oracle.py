@@ -516,3 +516,56 @@ def sirt(sino, fp, bp, img_shape, gamma=1.0, iters=100, x0=1e-5, W_sino=None, W_
         upd = np.where(W_img != 0.0, upd / np.where(W_img != 0.0, W_img, 1.0), upd)
         x = x + gamma * upd
     return x
+
+
+# --- TV primal-dual (tv.py:98-294), numpy float64 -----------------------------
+
+def tv_grad(x):
+    """tv.py:207-211"""
+    x = np.asarray(x, np.float64)
+    return np.stack([np.roll(x, -1, 0) - x, np.roll(x, -1, 1) - x])
+
+
+def tv_div(z):
+    """tv.py:220-224"""
+    z = np.asarray(z, np.float64)
+    return (z[0] - np.roll(z[0], 1, 0)) + (z[1] - np.roll(z[1], 1, 1))
+
+
+def tv_grad_abs(x):
+    """tv.py:200-204"""
+    x = np.asarray(x, np.float64)
+    return np.stack([x + np.roll(x, -1, 0), x + np.roll(x, -1, 1)])
+
+
+def tv_div_abs(z):
+    """tv.py:214-218"""
+    z = np.asarray(z, np.float64)
+    return (z[0] + np.roll(z[0], 1, 0)) + (z[1] + np.roll(z[1], 1, 1))
+
+
+def tv_project(AA):
+    """pyT (tv.py:98-184) for 2 x 1 pairs: the largest singular value is |a|,
+    the other 0, so the projection is a / max(1, |a|)."""
+    AA = np.asarray(AA, np.float64)
+    return AA / np.maximum(1.0, np.sqrt(AA[0] ** 2 + AA[1] ** 2))
+
+
+def tv_pdhg(g, fp, bp, img_shape, lam=1.0, theta=1.0, iters=100):
+    """The solver loop of tv.py:262-294 (sigma_q = 0 where A 1 = 0)."""
+    g = np.asarray(g, np.float64)
+    A1 = fp(np.ones(img_shape, np.float32))
+    sigma_z = 1.0 / tv_grad_abs(np.ones(img_shape))
+    sigma_q = np.where(A1 != 0, 1.0 / np.where(A1 != 0, A1, 1.0), 0.0)
+    tau = 1.0 / (bp(np.ones(g.shape, np.float32)) + tv_div_abs(np.ones((2,) + tuple(img_shape))))
+    u = np.zeros(img_shape)
+    ub = np.zeros(img_shape)
+    z = np.zeros((2,) + tuple(img_shape))
+    q = np.zeros(g.shape)
+    for _ in range(iters):
+        z = tv_project(z + sigma_z * tv_grad(ub))
+        q = (q + sigma_q * (fp(ub.astype(np.float32)) - g)) / (1 + sigma_q * lam)
+        u_prev = u
+        u = u + tau * (tv_div(z) - bp(q.astype(np.float32)))
+        ub = u + theta * (u - u_prev)
+    return u

@@ -362,6 +362,20 @@ def main():
                           bp=pdm.pd_bp_cone_3d(y, a_cone6, vol6.shape, 30.0, 60.0, du=1.3, dv=1.4,
                                                su=0.1, sv=0.2, d_pix=1.0))
 
+    # --- TV helpers (tv.py:98-224, executed from source: tv.py imports skimage
+    # and a module absent from the tree at import) --------------------------
+    fns = function_from_source(os.path.join(ref, "tv.py"),
+                               ["pyT", "grad", "div", "grad_abs", "div_abs"])
+    rng = np.random.default_rng(25)
+    x = rng.normal(size=(9, 7))
+    zz = rng.normal(size=(2, 9, 7))
+    AA = rng.normal(size=(2, 9, 7))
+    AA[:, 0, 0] = [0.3, 0.0]     # a single non-zero component, inside the ball
+    AA[:, 0, 1] = [0.0, -2.5]    # a single non-zero component, outside the ball
+    out["tv_ops"] = dict(x=x, z=zz, AA=AA, grad=fns["grad"](x), div=fns["div"](zz),
+                         grad_abs=fns["grad_abs"](x), div_abs=fns["div_abs"](zz),
+                         pyT=fns["pyT"](AA.copy()))
+
     path = os.path.join(HERE, "golden.npz")
     flat = {}
     for k, d in out.items():

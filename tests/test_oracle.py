@@ -251,3 +251,17 @@ def test_pd(golden, orc, case):
     geo = case.split("_")[1] + ("_3d" if case == "pd_cone" else "_2d")
     assert rel(_rd_call(orc, "pd_fp_" + geo, g, False), g["sino"]) < 1e-5
     assert rel(_rd_call(orc, "pd_bp_" + geo, g, True), g["bp"]) < 1e-5
+
+
+def test_tv_ops(golden, orc):
+    """grad / div / grad_abs / div_abs / pyT of tv.py:98-224 (reference source)."""
+    g = golden["tv_ops"]
+    assert np.allclose(orc.tv_grad(g["x"]), g["grad"], rtol=0, atol=1e-12)
+    assert np.allclose(orc.tv_div(g["z"]), g["div"], rtol=0, atol=1e-12)
+    assert np.allclose(orc.tv_grad_abs(g["x"]), g["grad_abs"], rtol=0, atol=1e-12)
+    assert np.allclose(orc.tv_div_abs(g["z"]), g["div_abs"], rtol=0, atol=1e-12)
+    assert np.allclose(orc.tv_project(g["AA"]), g["pyT"], rtol=0, atol=1e-12)
+    # div is the negative adjoint of grad
+    rng = np.random.default_rng(0)
+    x, z = rng.normal(size=(9, 7)), rng.normal(size=(2, 9, 7))
+    assert abs((orc.tv_grad(x) * z).sum() + (x * orc.tv_div(z)).sum()) < 1e-10

@@ -105,6 +105,10 @@ _PROTOS = {
     "vg_rd_bp": [ctypes.POINTER(RayGeom), c_void_p, c_void_p, c_void_p, c_void_p],
     "vg_pd_fp": [ctypes.POINTER(RayGeom), c_void_p, c_void_p, c_void_p, c_void_p],
     "vg_pd_bp": [ctypes.POINTER(RayGeom), c_void_p, c_void_p, c_void_p, c_void_p],
+    "vg_tv_dual": [c_void_p, c_void_p, c_int, c_int, c_float, c_void_p],
+    "vg_tv_residual": [c_void_p, c_void_p, c_void_p, c_void_p, c_float, c_size_t, c_void_p],
+    "vg_tv_primal": [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_float, c_int, c_int,
+                     c_void_p],
     "vg_fdk_weight_transpose": [ctypes.POINTER(DD3DGeom), c_void_p, c_void_p, c_void_p],
     "vg_fdk_transpose_back": [ctypes.POINTER(DD3DGeom), c_void_p, c_void_p, c_void_p],
     "vg_fdk_bp": [ctypes.POINTER(DD3DGeom), c_void_p, c_void_p, c_void_p, c_void_p],
