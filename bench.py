@@ -275,6 +275,8 @@ def run_workload(args):
                           dict(du=2.61381, dv=2.61381, dsrc_p=.48, dsrc_z=.48, su=0.0,
                                sv=158.13554, ssrc_p=0.0, ssrc_z=-74.4, d_pix=.96))}
         out = {}
+        if args.kernels_only:  # profiling aid: the script-size case only
+            cases = {"script": cases["script"]}
         for name, (n, nz, nu, nv, nsp, nsz, DSO, DSD, kw) in cases.items():
             e = ph.random_ellipsoids(10, fov_radius=n * kw["d_pix"] / 2, seed=2028)
             x = ph.rasterize3d_device(e, n, kw["d_pix"], device=dev)
