@@ -367,6 +367,18 @@ int vg_sf2d_bp(const vg_sf2d_geom *g, const float *sino, const double *trig,
 /* out (cols, rows) = transpose of in (rows, cols). */
 int vg_transpose(const float *in, int rows, int cols, float *out, void *stream);
 
+/* Ordered compaction of the non-zero entries of a float array of n < 2^31
+ * (the voxel lists of the Siddon list algebra: siddon.py rays_ave and
+ * list2array produce them by np.unique / accumulation).  Blocks of
+ * 1024 entries: vg_count_nonzero writes each block's count
+ * (vg_compact_blocks(n) ints); the caller forms first[b] = the exclusive
+ * prefix sum (int64); vg_compact_nonzero then writes the indices and values
+ * of the non-zeros in increasing index order. */
+int vg_compact_blocks(long long n);
+int vg_count_nonzero(const float *v, long long n, int *counts, void *stream);
+int vg_compact_nonzero(const float *v, long long n, const long long *first, int *idx,
+                       float *val, void *stream);
+
 /* Ramp filtering of each sinogram row as a linear convolution with the
  * spatial kernel of the padded rFFT filter (filtration.filter_sino,
  * filtration.py:238-309): out[r, i] = sum_j in[r, j] * taps[i - j + nu - 1]

@@ -311,6 +311,40 @@ def main():
                               src_prms=np.array(prms[2]), det_prms=np.array(prms[3]),
                               srt_prms=np.array(prms[4]))
 
+    # --- Siddon list algebra (siddon.py:12-633) on the cone fixture's lists ---
+    import copy
+    d = out["siddons_cone"]
+    nP = (12, 10, 6)
+    sdl = sd.siddons(d["src"], d["trg"], nP, (1.0, 0.8, 1.2))
+
+    def cat(lst):
+        """object array of unraveled rays -> counts and concatenated X, Y, Z, L"""
+        cnt = np.array([0 if r is None else len(r[0]) for r in lst.flat], np.int32)
+        parts = [r for r in lst.flat if r is not None]
+        if not parts:
+            return dict(cnt=cnt)
+        return dict(cnt=cnt, X=np.concatenate([r[0] for r in parts]).astype(np.int64),
+                    Y=np.concatenate([r[1] for r in parts]).astype(np.int64),
+                    Z=np.concatenate([r[2] for r in parts]).astype(np.int64),
+                    L=np.concatenate([r[3] for r in parts]).astype(np.float32))
+
+    la = dict(l2a=sd.list2array(sdl, nP), shape=np.array(sdl.shape, np.int32))
+    ave = sd.rays_ave(sdl, nPixels=nP)
+    la.update(ave_x=ave[0], ave_y=ave[1], ave_z=ave[2], ave_l=ave[3])
+    for tag, val in (("axave", sd.list_ave(sdl, nPixels=nP, axis=(2,))),
+                     ("wave", sd.list_weight_ave(sdl, np.linspace(0.2, 1.0, sdl.shape[2]),
+                                                 nPixels=nP, axis=(2,))),
+                     ("conv", sd.list_convole(sdl, np.array([0.25, 0.5, 0.25]), nPixels=nP,
+                                              axis=(2,))),
+                     ("flip", sd.list_flip(copy.deepcopy(sdl), x=5, z=2)),
+                     ("shift", sd.list_index_shift(copy.deepcopy(sdl), (1, -2, 3))),
+                     ("del", sd.list_del_ind(copy.deepcopy(sdl), np.arange(2, 9), np.arange(0, 6),
+                                             np.arange(1, 5)))):
+        for k, v in cat(val).items():
+            la[f"{tag}_{k}"] = v
+    la["weights"] = np.linspace(0.2, 1.0, sdl.shape[2])
+    out["list_algebra"] = la
+
     # --- ray-driven (rd.py) and pixel-driven (pd.py) projectors --------------
     import vir.sys_mat.rd as rdm
     import vir.sys_mat.pd as pdm

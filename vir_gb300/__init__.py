@@ -39,7 +39,13 @@ _DROP_INS = {
     "sys_mat.fp_2d_par": {n: "vir_gb300.sys_mat.fp_2d_par:" + n
                           for n in ("siddons_fp_2d", "separable_footprint_fp_2d")},
     "filtration": {"filter_sino": "vir_gb300.filtration:filter_sino"},
-    "sys_mat.siddon": {"siddons": "vir_gb300.sys_mat.siddon:siddons"},
+    "sys_mat.siddon": {n: "vir_gb300.sys_mat.siddon:" + n for n in
+                       ("siddons", "list2array", "list2array_iter_ray", "list_count_elem",
+                        "list_flatten", "list_ravel", "list_unravel", "ray_ravel", "ray_unravel",
+                        "list_index_shift", "ray_index_shift", "list_del_ind", "list_flip",
+                        "ray_flip", "ray_boundary", "rays_ave", "list_ave", "rays_weight_ave",
+                        "list_weight_ave", "list_convole")},
+    "mpct": {"list_ctypes_object": "vir_gb300.mpct:list_ctypes_object"},
     "projection.proj": {n: "vir_gb300.projection.proj:" + n for n in ("sd_f_proj", "sd_b_proj")},
     "projection.proj_ctype": {n: "vir_gb300.projection.proj_ctype:" + n
                               for n in ("sd_f_proj_c", "sd_b_proj_c")},

@@ -115,6 +115,8 @@ _PROTOS = {
     "vg_sf2d_fp": [ctypes.POINTER(SF2DGeom), c_void_p, c_void_p, c_void_p, c_void_p, c_void_p],
     "vg_sf2d_bp": [ctypes.POINTER(SF2DGeom), c_void_p, c_void_p, c_void_p, c_void_p],
     "vg_transpose": [c_void_p, c_int, c_int, c_void_p, c_void_p],
+    "vg_count_nonzero": [c_void_p, ctypes.c_longlong, c_void_p, c_void_p],
+    "vg_compact_nonzero": [c_void_p, ctypes.c_longlong, c_void_p, c_void_p, c_void_p, c_void_p],
     "vg_filter_rows": [c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p],
 }
 
@@ -152,6 +154,8 @@ def load(build_if_missing: bool = True):
         L.vg_dd3d_workspace_bytes.restype = c_size_t
         L.vg_dd_square_workspace_bytes.argtypes = [ctypes.POINTER(DDSquareGeom)]
         L.vg_dd_square_workspace_bytes.restype = c_size_t
+        L.vg_compact_blocks.argtypes = [ctypes.c_longlong]
+        L.vg_compact_blocks.restype = c_int
         L.vg_list_bp_workspace_bytes.argtypes = [c_int]
         L.vg_list_bp_workspace_bytes.restype = c_size_t
         L.vg_dd2d_noalloc_scratch_bytes.argtypes = []
@@ -174,7 +178,7 @@ def exported_symbols():
                             "vg_dd2d_workspace_bytes", "vg_dd2d_noalloc_scratch_bytes",
                             "vg_dd2d_fp_variants", "vg_dd2d_fp_default_variant",
                             "vg_list_bp_workspace_bytes", "vg_dd3d_workspace_bytes",
-                            "vg_dd_square_workspace_bytes"]
+                            "vg_dd_square_workspace_bytes", "vg_compact_blocks"]
 
 
 def dd_square_workspace(g, dev):

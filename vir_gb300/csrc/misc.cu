@@ -110,7 +110,82 @@ filter_rows_kernel(const float *__restrict__ in, int rows, int nu, const float *
     }
 }
 
+// Ordered stream compaction of the non-zero entries of a float array, in two
+// launches around a scan of per-block counts: CP_ITEMS entries per block.
+constexpr int CP_THREADS = 256, CP_PER = 4, CP_ITEMS = CP_THREADS * CP_PER;
+
+__global__ void __launch_bounds__(CP_THREADS)
+count_nonzero_kernel(const float *__restrict__ v, long long n, int *__restrict__ counts) {
+    __shared__ int wsum[CP_THREADS / 32];
+    const long long base = (long long)blockIdx.x * CP_ITEMS + (long long)threadIdx.x * CP_PER;
+    int c = 0;
+#pragma unroll
+    for (int i = 0; i < CP_PER; ++i) c += (base + i < n && v[base + i] != 0.f) ? 1 : 0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
+    if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = c;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int t = 0;
+        for (int w = 0; w < CP_THREADS / 32; ++w) t += wsum[w];
+        counts[blockIdx.x] = t;
+    }
+}
+
+// first[b]: number of non-zeros before block b (exclusive scan of counts)
+__global__ void __launch_bounds__(CP_THREADS)
+compact_nonzero_kernel(const float *__restrict__ v, long long n, const long long *__restrict__ first,
+                       int *__restrict__ idx, float *__restrict__ val) {
+    __shared__ int wsum[CP_THREADS / 32];
+    const long long base = (long long)blockIdx.x * CP_ITEMS + (long long)threadIdx.x * CP_PER;
+    float x[CP_PER];
+    int c = 0;
+#pragma unroll
+    for (int i = 0; i < CP_PER; ++i) {
+        x[i] = base + i < n ? v[base + i] : 0.f;
+        c += x[i] != 0.f ? 1 : 0;
+    }
+    // exclusive scan of c over the block (warp shuffles, then warp totals)
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int inc = c;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += t;
+    }
+    if (lane == 31) wsum[warp] = inc;
+    __syncthreads();
+    int before = 0;
+    for (int w = 0; w < warp; ++w) before += wsum[w];
+    long long pos = first[blockIdx.x] + before + inc - c;
+#pragma unroll
+    for (int i = 0; i < CP_PER; ++i)
+        if (x[i] != 0.f) {
+            idx[pos] = (int)(base + i);
+            val[pos] = x[i];
+            ++pos;
+        }
+}
+
 }  // namespace
+
+extern "C" int vg_compact_blocks(long long n) { return (int)((n + CP_ITEMS - 1) / CP_ITEMS); }
+
+extern "C" int vg_count_nonzero(const float *v, long long n, int *counts, void *stream) {
+    VG_REQUIRE(v && counts, "count_nonzero: null pointer");
+    VG_REQUIRE(n > 0 && n < (1LL << 31), "count_nonzero: size out of range");
+    count_nonzero_kernel<<<vg_compact_blocks(n), CP_THREADS, 0, as_stream(stream)>>>(v, n, counts);
+    return launch_status("count_nonzero");
+}
+
+extern "C" int vg_compact_nonzero(const float *v, long long n, const long long *first, int *idx,
+                                  float *val, void *stream) {
+    VG_REQUIRE(v && first && idx && val, "compact_nonzero: null pointer");
+    VG_REQUIRE(n > 0 && n < (1LL << 31), "compact_nonzero: size out of range");
+    compact_nonzero_kernel<<<vg_compact_blocks(n), CP_THREADS, 0, as_stream(stream)>>>(v, n, first,
+                                                                                      idx, val);
+    return launch_status("compact_nonzero");
+}
 
 extern "C" int vg_transpose(const float *in, int rows, int cols, float *out, void *stream) {
     VG_REQUIRE(in && out, "transpose: null pointer");

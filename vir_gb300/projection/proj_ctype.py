@@ -30,6 +30,8 @@ def _as_array(ptr, n, ctype, dtype):
 
 
 def _csr_from_structs(sdlist_c, nrays, ravel, dims):
+    # mpct.list_ctypes_object(flat=True) hands over ctypes.byref(array)
+    sdlist_c = getattr(sdlist_c, "_obj", sdlist_c)
     counts = np.zeros(nrays + 1, np.int64)
     inds, lens = [], []
     nX, nY, nZ = dims
