@@ -62,6 +62,21 @@ int vg_siddon2d_bp(const float *sino, int na, int n_dets, const double *trig,
                    int nx, int ny, double d_det, double d_pix, float *img,
                    void *stream);
 
+/* The same back projection in scatter form: every ray of a chunk of views
+ * retraces its segments exactly as vg_siddon2d_fp does and writes y * length
+ * into a (view, pixel) slot reserved for it (ray index mod S, S above the
+ * number of rays one pixel can meet in a view), then a gather pass sums the
+ * slots per pixel in a fixed order.  Deterministic; the segments and lengths
+ * are the forward projector's.  Views are processed in chunks that fit the
+ * caller's workspace (vg_siddon2d_bp_workspace_bytes: up to 256 MiB, at
+ * least one view). */
+size_t vg_siddon2d_bp_workspace_bytes(int nx, int ny, int na, double d_det,
+                                      double d_pix);
+int vg_siddon2d_bp_scatter(const float *sino, int na, int n_dets,
+                           const double *trig, int nx, int ny, double d_det,
+                           double d_pix, float *img, void *workspace,
+                           size_t workspace_bytes, void *stream);
+
 /* Per-ray trace of vg_siddon2d_fp's path (no image): segment count, an
  * order-sensitive 64-bit hash of the voxel indices (h = (h ^ (idx + C1)) *
  * C2, FNV-style, h0 = 0xCBF29CE484222325) and the FP64 sum of lengths, for

@@ -65,13 +65,14 @@ def test_siddon_fp_bp_vs_oracle(vg, orc, shape, n_dets, d_det, d_pix, na, span):
     fo = orc.siddons_fp_2d(img, angs, n_dets, d_det, d_pix)
     assert rel(fp, fo) < 2e-6
     y = rng.random(fp.shape).astype(np.float32)
-    bp = fp_2d_par.siddons_bp_2d(y, angs, shape, d_det, d_pix)
     bo = orc.siddons_bp_2d(y, angs, shape, d_det, d_pix)
-    assert rel(bp, bo) < 2e-6
-    # adjoint (dot-product) test of the GPU pair
-    lhs = (fp.astype(np.float64) * y).sum()
-    rhs = (img.astype(np.float64) * bp).sum()
-    assert abs(lhs - rhs) / abs(lhs) < 1e-6
+    for method in ("scatter", "gather"):
+        bp = fp_2d_par.siddons_bp_2d(y, angs, shape, d_det, d_pix, method=method)
+        assert rel(bp, bo) < 2e-6, method
+        # adjoint (dot-product) test of the GPU pair
+        lhs = (fp.astype(np.float64) * y).sum()
+        rhs = (img.astype(np.float64) * bp).sum()
+        assert abs(lhs - rhs) / abs(lhs) < 1e-6, method
 
 
 # --- distance-driven 2D ---------------------------------------------------------

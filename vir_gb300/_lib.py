@@ -80,6 +80,8 @@ _PROTOS = {
                        c_void_p, c_void_p],
     "vg_siddon2d_trace": [c_int, c_int, c_void_p, c_int, c_int, c_double, c_double, c_void_p,
                           c_void_p, c_void_p, c_void_p],
+    "vg_siddon2d_bp_scatter": [c_void_p, c_int, c_int, c_void_p, c_int, c_int, c_double,
+                               c_double, c_void_p, c_void_p, c_size_t, c_void_p],
     "vg_siddons_count": [ctypes.POINTER(SiddonRays), c_void_p, c_void_p, c_void_p],
     "vg_siddons_fill": [ctypes.POINTER(SiddonRays), c_void_p, c_void_p, c_void_p, c_void_p],
     "vg_list_fp": [c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_int, c_void_p],
@@ -156,6 +158,8 @@ def load(build_if_missing: bool = True):
         L.vg_dd_square_workspace_bytes.restype = c_size_t
         L.vg_compact_blocks.argtypes = [ctypes.c_longlong]
         L.vg_compact_blocks.restype = c_int
+        L.vg_siddon2d_bp_workspace_bytes.argtypes = [c_int, c_int, c_int, c_double, c_double]
+        L.vg_siddon2d_bp_workspace_bytes.restype = c_size_t
         L.vg_list_bp_workspace_bytes.argtypes = [c_int]
         L.vg_list_bp_workspace_bytes.restype = c_size_t
         L.vg_dd2d_noalloc_scratch_bytes.argtypes = []
@@ -178,7 +182,8 @@ def exported_symbols():
                             "vg_dd2d_workspace_bytes", "vg_dd2d_noalloc_scratch_bytes",
                             "vg_dd2d_fp_variants", "vg_dd2d_fp_default_variant",
                             "vg_list_bp_workspace_bytes", "vg_dd3d_workspace_bytes",
-                            "vg_dd_square_workspace_bytes", "vg_compact_blocks"]
+                            "vg_dd_square_workspace_bytes", "vg_compact_blocks",
+                            "vg_siddon2d_bp_workspace_bytes"]
 
 
 def dd_square_workspace(g, dev):

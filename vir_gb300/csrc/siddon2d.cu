@@ -87,13 +87,27 @@ __device__ __forceinline__ unsigned long long trace_mix(unsigned long long h, un
     return (h ^ (v + 0x9E3779B97F4A7C15ull)) * 0x100000001B3ull;
 }
 
-template <bool TRACE>
+// Scatter form of the back projection: each ray of views [ia0, ia0 + nvc)
+// writes y * length into a per-(view, pixel) slot reserved for it,
+// slot = ray mod S, where S exceeds the number of rays that can cross one
+// pixel in one view; a gather pass then sums the slots.
+struct Slots {
+    const float *y;  // sinogram (na, n_dets)
+    float *buf;      // [nvc][nx * ny][S], zeroed
+    int S, ia0;
+};
+
+// MODE 0: line integrals; 1: trace (count, hash, length); 2: slot scatter.
+template <int MODE>
 __global__ void
 siddon2d_fp_kernel(SidGeom g, const float *__restrict__ img, const double *__restrict__ trig,
-                   int na, float *__restrict__ sino, Trace tr) {
+                   int na, float *__restrict__ sino, Trace tr, Slots sl) {
+    constexpr bool TRACE = MODE == 1;
     int k = blockIdx.x * blockDim.x + threadIdx.x;
-    int ia = blockIdx.y;
+    int ia = blockIdx.y + sl.ia0;
     if (k >= g.n_dets || ia >= na) return;
+    const float yv = MODE == 2 ? __ldg(sl.y + (size_t)ia * g.n_dets + k) : 0.f;
+    float *slot = MODE == 2 ? sl.buf + (size_t)blockIdx.y * g.nx * g.ny * sl.S + k % sl.S : nullptr;
     double dx = trig[2 * ia], dy = trig[2 * ia + 1];
     Ray r = ray_setup(g, k, dx, dy);
     Kahan acc;
@@ -141,6 +155,8 @@ siddon2d_fp_kernel(SidGeom g, const float *__restrict__ img, const double *__res
                         ++tcount;
                         thash = trace_mix(thash, pix);
                         tlen = d_add(tlen, d_sub(tn, tprev));
+                    } else if (MODE == 2) {
+                        slot[pix * sl.S] += __fmul_rn(yv, (float)d_sub(tn, tprev));
                     } else {
                         float w = (float)d_sub(tn, tprev);
                         acc.add(__fmul_rn(__ldg(img + pix), w));
@@ -155,9 +171,26 @@ siddon2d_fp_kernel(SidGeom g, const float *__restrict__ img, const double *__res
         tr.count[o] = tcount;
         tr.hash[o] = thash;
         tr.len[o] = tlen;
-    } else {
+    } else if (MODE == 0) {
         sino[o] = acc.s;
     }
+}
+
+// Gather of the slot buffer: pixel sums over the chunk's views and slots in
+// a fixed order, added to img (first chunk: written).
+__global__ void __launch_bounds__(256)
+siddon2d_slot_gather(const float *__restrict__ buf, int npix, int S, int nvc, int first,
+                     float *__restrict__ img) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npix) return;
+    Kahan acc;
+    for (int v = 0; v < nvc; ++v) {
+        const float *b = buf + ((size_t)v * npix + p) * S;
+        float part = 0.f;
+        for (int s = 0; s < S; ++s) part += __ldg(b + s);
+        acc.add(part);
+    }
+    img[p] = first ? acc.s : img[p] + acc.s;
 }
 
 // Gather-form adjoint.  For pixel (ix, iy) and view ia, the candidate rays
@@ -259,7 +292,8 @@ extern "C" int vg_siddon2d_fp(const float *img, int nx, int ny, const double *tr
     VG_REQUIRE(na > 0 && na < 65536, "siddon2d_fp: na out of range");
     VG_REQUIRE(img && trig && sino, "siddon2d_fp: null pointer");
     dim3 grid(ceil_div(n_dets, 128), na);
-    siddon2d_fp_kernel<false><<<grid, 128, 0, as_stream(stream)>>>(g, img, trig, na, sino, Trace{});
+    siddon2d_fp_kernel<0><<<grid, 128, 0, as_stream(stream)>>>(g, img, trig, na, sino, Trace{},
+                                                              Slots{nullptr, nullptr, 1, 0});
     return launch_status("siddon2d_fp");
 }
 
@@ -272,8 +306,9 @@ extern "C" int vg_siddon2d_trace(int nx, int ny, const double *trig, int na, int
     VG_REQUIRE(na > 0 && na < 65536, "siddon2d_trace: na out of range");
     VG_REQUIRE(trig && count && hash && len, "siddon2d_trace: null pointer");
     dim3 grid(ceil_div(n_dets, 128), na);
-    siddon2d_fp_kernel<true><<<grid, 128, 0, as_stream(stream)>>>(g, nullptr, trig, na, nullptr,
-                                                                 Trace{count, hash, len});
+    siddon2d_fp_kernel<1><<<grid, 128, 0, as_stream(stream)>>>(g, nullptr, trig, na, nullptr,
+                                                              Trace{count, hash, len},
+                                                              Slots{nullptr, nullptr, 1, 0});
     return launch_status("siddon2d_trace");
 }
 
@@ -288,4 +323,55 @@ extern "C" int vg_siddon2d_bp(const float *sino, int na, int n_dets, const doubl
     dim3 grid(ceil_div(ny, 256), nx);
     siddon2d_bp_kernel<<<grid, 256, 0, as_stream(stream)>>>(g, sino, trig, na, img);
     return launch_status("siddon2d_bp");
+}
+
+// Slots per (view, pixel): more than the rays one pixel can meet in a view
+// (its projected width d_pix (|cos| + |sin|) <= d_pix sqrt 2 spans at most
+// floor(d_pix sqrt 2 / d_det) + 1 bin centres).
+static int siddon_slots(double d_pix, double d_det) {
+    return (int)floor(d_pix * 1.4142135623730951 / d_det) + 2;
+}
+
+extern "C" size_t vg_siddon2d_bp_workspace_bytes(int nx, int ny, int na, double d_det,
+                                                 double d_pix) {
+    if (nx <= 0 || ny <= 0 || na <= 0 || !(d_det > 0) || !(d_pix > 0)) return 0;
+    const size_t per_view = (size_t)nx * ny * siddon_slots(d_pix, d_det) * sizeof(float);
+    size_t views = ((size_t)256 << 20) / per_view;
+    if (views < 1) views = 1;
+    if (views > (size_t)na) views = na;
+    return views * per_view;
+}
+
+extern "C" int vg_siddon2d_bp_scatter(const float *sino, int na, int n_dets, const double *trig,
+                                      int nx, int ny, double d_det, double d_pix, float *img,
+                                      void *workspace, size_t workspace_bytes, void *stream) {
+    SidGeom g;
+    int st = make_geom(g, nx, ny, n_dets, d_det, d_pix);
+    if (st) return st;
+    VG_REQUIRE(na > 0 && na < 65536, "siddon2d_bp_scatter: na out of range");
+    VG_REQUIRE((long long)nx * ny < (1LL << 31), "siddon2d_bp_scatter: image too large");
+    VG_REQUIRE(img && trig && sino && workspace, "siddon2d_bp_scatter: null pointer");
+    const int S = siddon_slots(d_pix, d_det);
+    const size_t per_view = (size_t)nx * ny * S * sizeof(float);
+    VG_REQUIRE(workspace_bytes >= per_view,
+               "siddon2d_bp_scatter: workspace of at least %zu bytes needed", per_view);
+    VG_REQUIRE(((uintptr_t)workspace & 3) == 0, "siddon2d_bp_scatter: workspace misaligned");
+    const int nvc = (int)(workspace_bytes / per_view < (size_t)na ? workspace_bytes / per_view : na);
+    cudaStream_t s = as_stream(stream);
+    float *buf = static_cast<float *>(workspace);
+    const int npix = nx * ny;
+    for (int ia0 = 0; ia0 < na; ia0 += nvc) {
+        const int nv = na - ia0 < nvc ? na - ia0 : nvc;
+        cudaError_t e = cudaMemsetAsync(buf, 0, (size_t)nv * per_view, s);
+        if (e != cudaSuccess) return cuda_status(e, "siddon2d_bp_scatter: clear");
+        dim3 grid(ceil_div(n_dets, 128), nv);
+        siddon2d_fp_kernel<2><<<grid, 128, 0, s>>>(g, nullptr, trig, na, nullptr, Trace{},
+                                                     Slots{sino, buf, S, ia0});
+        st = launch_status("siddon2d_bp_scatter");
+        if (st) return st;
+        siddon2d_slot_gather<<<ceil_div(npix, 256), 256, 0, s>>>(buf, npix, S, nv, ia0 == 0, img);
+        st = launch_status("siddon2d_slot_gather");
+        if (st) return st;
+    }
+    return VG_OK;
 }
