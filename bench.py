@@ -232,6 +232,47 @@ def _roof(units, ms, peak):
             "algorithmic_bytes_per_launch": 4.0 * units}
 
 
+def storage_error(probs, dev, n_check=2, iters=50):
+    """Final-iterate error against the FP64 oracle's SIRT, relative
+    (||x - x64|| / ||x64||), for FP32 storage (the batched kernels) and for
+    BF16 storage with FP32 arithmetic: y, the residual and the iterate are
+    rounded to bfloat16 wherever they are stored, which gives the values a
+    bf16 store / load pair would.  The smallest problems of the set are used
+    so the oracle finishes in seconds."""
+    import torch
+    from oracle import oracle as orc
+    from vir_gb300.reconstruction import SIRT2D
+    order = sorted(range(len(probs)), key=lambda i: probs[i]["img_shape"][0] * probs[i]["sino"].shape[0])
+    bf = lambda t: t.to(torch.bfloat16).to(torch.float32)
+    out = []
+    for i in order[:n_check]:
+        p = probs[i]
+        kw = dict(du=p["du"], d_pix=p["d_pix"])
+        if p["geom"] == "fan":
+            fp = lambda x: orc.dd_fp_fan_2d(x, p["ang_arr"], p["sino"].shape[1], p["DSO"], p["DSD"], **kw)
+            bp = lambda y: orc.dd_bp_fan_2d(y, p["ang_arr"], p["img_shape"], p["DSO"], p["DSD"], **kw)
+        else:
+            fp = lambda x: orc.dd_fp_par_2d(x, p["ang_arr"], p["sino"].shape[1], **kw)
+            bp = lambda y: orc.dd_bp_par_2d(y, p["ang_arr"], p["img_shape"], **kw)
+        x64 = orc.sirt(p["sino"], fp, bp, p["img_shape"], iters=iters)
+        s = SIRT2D(device=dev, **p)
+        x32 = s.run(iters - 1, graph=False).cpu().numpy()
+        yb = bf(s.y)
+        x = bf(torch.full_like(s.x, float(np.float32(1e-5))))
+        for _ in range(iters - 1):
+            est = s.fp(x)
+            r = bf(torch.where(s.inv_ws != 0, (yb - est) * s.inv_ws, est))
+            upd = s.bp(r)
+            x = bf(x + s.gamma * torch.where(s.inv_wi != 0, upd * s.inv_wi, upd))
+        xb = x.cpu().numpy()
+        nrm = np.linalg.norm(x64)
+        out.append({"problem": i, "side": int(p["img_shape"][0]), "views": int(p["sino"].shape[0]),
+                    "geom": p["geom"], "updates": iters - 1,
+                    "fp32_rel": float(np.linalg.norm(x32 - x64) / nrm),
+                    "bf16_storage_rel": float(np.linalg.norm(xb - x64) / nrm)})
+    return out
+
+
 def run_workload(args):
     """One JSON line for a configuration other than the default C2 line:
     per-kernel CUDA-event times (median of --steps after --warmup), GUPS and
@@ -313,7 +354,8 @@ def run_workload(args):
         line.update({"metric": "batched SIRT iter/s (50 updates x 64 problems)",
                      "graph_ms": res["graph"], "plain_ms": res["plain"],
                      "speedup_vs_plain": res["plain"] / res["graph"],
-                     "fwd_back_gups_graph": 2 * 50 * units / (res["graph"] / 1e3) / 1e9})
+                     "fwd_back_gups_graph": 2 * 50 * units / (res["graph"] / 1e3) / 1e9,
+                     "storage_error": storage_error(probs, dev)})
         print(json.dumps(line), flush=True)
         return 0
     if args.kernels_only:
