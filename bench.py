@@ -127,6 +127,21 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def job_rate(local_ms, world, units_per_rank, dist=None, dev=None):
+    """Whole-job rate of independent replicas: every rank processes
+    units_per_rank units; the job takes the slowest rank's time (max over
+    ranks through the process group when there is one).  Returns (max_ms,
+    world * units_per_rank / max seconds)."""
+    total_ms = float(local_ms)
+    if dist is not None and world > 1:
+        import torch
+        t = torch.tensor([total_ms], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+        dist.barrier()
+    return total_ms, world * units_per_rank / (total_ms / 1e3)
+
+
 def dist_info():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -437,14 +452,7 @@ def main():
             ev[i][1].record(stream)
         torch.cuda.synchronize(dev)
     step_ms = [a.elapsed_time(b) for a, b in ev]
-    total_ms = sum(step_ms)
-    if world > 1:
-        t = torch.tensor([total_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-        if world > 1:
-            dist.barrier()
-    value = world * K * U / (total_ms / 1e3)
+    total_ms, value = job_rate(sum(step_ms), world, K * U, dist if world > 1 else None, dev)
     x_final = sirt.x.detach().cpu().numpy()
     rmse = float(np.sqrt(np.mean((x_final - img) ** 2)))
 
