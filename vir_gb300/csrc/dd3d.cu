@@ -248,9 +248,14 @@ dd3d_fp_kernel(vg_dd3d_geom g, const float *__restrict__ vol, const float4 *__re
             for (int j = 0; j < 4; ++j) {
                 const float4 wu = S.uw[b][4 * warp + j];
                 const float *r = line + (size_t)S.uk[b][4 * warp + j] * sk;
+                // trailing pixel rows with zero weight are skipped (the u-cell,
+                // hence the branch, is the same for the whole warp; a zero row
+                // before a weighted one, at the volume's far edge, is kept)
+                const int nrow = wu.z != 0.f ? 3 : (wu.y != 0.f ? 2 : 1);
                 float ca = 0.f, cb = 0.f;
 #pragma unroll
                 for (int t = 0; t < 3; ++t) {
+                    if (t >= nrow) break;
                     const float *q = r + t * sk;
                     const float sa = fmaf(wa.x, __ldg(q + za), fmaf(wa.y, __ldg(q + za + 1), wa.z * __ldg(q + za + 2)));
                     const float sb = fmaf(wb.x, __ldg(q + zb), fmaf(wb.y, __ldg(q + zb + 1), wb.z * __ldg(q + zb + 2)));
@@ -427,12 +432,21 @@ dd3d_bp_kernel(vg_dd3d_geom g, const float *__restrict__ sino, const float4 *__r
                 const float4 wu = T.uw[b][c];
                 const float4 wv = T.vw[b][l][lane];
                 const float *r = s + (size_t)T.uj[b][c] * g.nv + T.vq[b][l][lane];
-                const float c0 = fmaf(wv.x, __ldg(r), fmaf(wv.y, __ldg(r + 1), wv.z * __ldg(r + 2)));
-                r += g.nv;
-                const float c1 = fmaf(wv.x, __ldg(r), fmaf(wv.y, __ldg(r + 1), wv.z * __ldg(r + 2)));
-                r += g.nv;
-                const float c2 = fmaf(wv.x, __ldg(r), fmaf(wv.y, __ldg(r + 1), wv.z * __ldg(r + 2)));
-                part[i] = fmaf(wu.x, c0, fmaf(wu.y, c1, wu.z * c2));
+                // trailing cell rows with zero weight are skipped (the column,
+                // hence the branch, is the same for the whole warp; a zero row
+                // before a weighted one, at the detector's far edge, is kept)
+                const int nrow = wu.z != 0.f ? 3 : (wu.y != 0.f ? 2 : 1);
+                float acc3 = wu.x * fmaf(wv.x, __ldg(r), fmaf(wv.y, __ldg(r + 1), wv.z * __ldg(r + 2)));
+                if (nrow > 1) {
+                    r += g.nv;
+                    acc3 = fmaf(wu.y, fmaf(wv.x, __ldg(r), fmaf(wv.y, __ldg(r + 1), wv.z * __ldg(r + 2))), acc3);
+                    if (nrow > 2) {
+                        r += g.nv;
+                        acc3 = fmaf(wu.z, fmaf(wv.x, __ldg(r), fmaf(wv.y, __ldg(r + 1), wv.z * __ldg(r + 2))),
+                                    acc3);
+                    }
+                }
+                part[i] = acc3;
             }
         } else {
 #pragma unroll 1
