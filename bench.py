@@ -241,6 +241,22 @@ def _event_ms(fn, reps, stream):
     return statistics.median(out)
 
 
+def orc_mod():
+    from oracle import oracle
+    return oracle
+
+
+def _cpu_port_ms(fp, bp):
+    """The FP64 C restatement of the same pair on all host threads, once."""
+    t0 = time.perf_counter()
+    fp()
+    t1 = time.perf_counter()
+    bp()
+    t2 = time.perf_counter()
+    return {"fp_ms": (t1 - t0) * 1e3, "bp_ms": (t2 - t1) * 1e3, "cores": orc_mod().num_threads(),
+            "kind": "port"}
+
+
 def _roof(units, ms, peak):
     gbs = 4.0 * units / (ms / 1e3) / 1e9
     return {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
@@ -312,6 +328,9 @@ def run_workload(args):
         fp = lambda: f2.siddons_fp_2d(x, angs, 367, 1.0, 1.0)
         bp = lambda: f2.siddons_bp_2d(y, angs, (256, 256), 1.0, 1.0)
         units = 180 * 256 * 256
+        yh = y.cpu().numpy()
+        line["cpu_port"] = _cpu_port_ms(lambda: orc_mod().siddons_fp_2d(img, angs, 367, 1.0, 1.0),
+                                        lambda: orc_mod().siddons_bp_2d(yh, angs, (256, 256), 1.0, 1.0))
     elif wl in ("c4", "c5"):
         n, na, nu, nv, dp, du = ((512, 720, 1024, 768, 0.5, 0.8) if wl == "c4"
                                  else (256, 360, 512, 384, 1.0, 1.6))
@@ -350,6 +369,11 @@ def run_workload(args):
                          "fwd_back_gups": 2 * units / ((t_fp + t_bp) / 1e3) / 1e9,
                          "roofline_fp": _roof(units, t_fp, peak),
                          "roofline_bp": _roof(units, t_bp, peak)}
+            if name == "script":
+                xh, yh = x.cpu().numpy(), y.cpu().numpy()
+                out[name]["cpu_port"] = _cpu_port_ms(
+                    lambda: orc_mod().dd_fp_square(xh, nu, nv, nsp, nsz, DSO, DSD, **kw),
+                    lambda: orc_mod().dd_bp_square(yh, (n, n, nz), DSO, DSD, **kw))
             del x, y
             torch.cuda.empty_cache()
         if not args.kernels_only:

@@ -236,3 +236,44 @@ def test_sirt_vs_oracle(vg, orc, geom):
         r_gpu = np.sqrt(np.mean((x - img) ** 2))
         r_orc = np.sqrt(np.mean((xo - img) ** 2))
         assert abs(r_gpu - r_orc) / r_orc < 1e-4
+
+
+@pytest.mark.parametrize("fan", [False, True])
+@pytest.mark.parametrize("shape,nu,na,su", [
+    ((37, 53), 71, 1, 0.3),      # ragged image, a single view
+    ((1, 29), 40, 9, -0.5),      # one-pixel-wide image
+    ((64, 64), 24, 12, 2.0),     # detector narrower than the image, shifted
+    ((48, 40), 700, 7, 0.0),     # detector much wider than the image
+])
+def test_dd_edge_cases_vs_oracle(vg, orc, fan, shape, nu, na, su):
+    from vir_gb300.sys_mat import dd
+    rng = np.random.default_rng(11)
+    img = rng.random(shape).astype(np.float32)
+    angs = np.linspace(0.1, 0.1 + 2 * np.pi, na, endpoint=False)
+    y = rng.random((na, nu)).astype(np.float32)
+    kw = dict(du=0.9, su=su, d_pix=1.1)
+    if fan:
+        geo = (120.0, 240.0)
+        fp, fo = dd.dd_fp_fan_2d(img, angs, nu, *geo, **kw), orc.dd_fp_fan_2d(img, angs, nu, *geo, **kw)
+        bp = dd.dd_bp_fan_2d(y, angs, shape, *geo, **kw)
+        bo = orc.dd_bp_fan_2d(y, angs, shape, *geo, **kw)
+    else:
+        fp, fo = dd.dd_fp_par_2d(img, angs, nu, **kw), orc.dd_fp_par_2d(img, angs, nu, **kw)
+        bp, bo = dd.dd_bp_par_2d(y, angs, shape, **kw), orc.dd_bp_par_2d(y, angs, shape, **kw)
+    assert fp.shape == (na, nu) and bp.shape == shape
+    assert rel(fp, fo) < 1e-4
+    assert rel(bp, bo) < 1e-4
+
+
+def test_zero_and_empty_inputs(vg):
+    """Zero images project to zero; an object outside every ray gives zeros;
+    no views is an argument error, not a silent empty result."""
+    from vir_gb300 import VirGpuError
+    from vir_gb300.sys_mat import dd, fp_2d_par
+    angs = np.linspace(0, np.pi, 8, endpoint=False)
+    assert not np.any(dd.dd_fp_par_2d(np.zeros((16, 16), np.float32), angs, 20))
+    assert not np.any(fp_2d_par.siddons_fp_2d(np.zeros((16, 16), np.float32), angs, 20))
+    # detector far off to the side: no overlap anywhere
+    assert not np.any(dd.dd_fp_par_2d(np.ones((16, 16), np.float32), angs, 10, su=100.0))
+    with pytest.raises((VirGpuError, ValueError)):
+        dd.dd_fp_par_2d(np.ones((16, 16), np.float32), np.zeros(0), 20)

@@ -120,3 +120,20 @@ def test_cone_c5_scale_properties(vg):
     d = float(np.float32(1.6))
     rhs = (x.double() * B.double()).sum().item() * na * 1.0 / (d * d)
     assert abs(lhs - rhs) / lhs < 1e-5
+
+
+def test_cone_wide_detector_vs_oracle(vg, orc):
+    """A detector reaching beyond DSD from the centre contains the pole of the
+    inverse edge map (rays parallel to the pixel lines) for some views."""
+    from vir_gb300.sys_mat import dd
+    rng = np.random.default_rng(13)
+    vol = rng.random((12, 12, 10)).astype(np.float32)
+    angs = np.linspace(0.05, 0.05 + 2 * np.pi, 16, endpoint=False)
+    kw = dict(du=1.5, dv=1.2, su=0.0, sv=0.0, d_pix=1.0)
+    fp = dd.dd_fp_cone_3d(vol, angs, 110, 24, 30.0, 50.0, **kw)
+    fo = orc.dd_fp_cone_3d(vol, angs, 110, 24, 30.0, 50.0, **kw)
+    assert rel(fp, fo) < 5e-5
+    y = rng.random(fp.shape).astype(np.float32)
+    bp = dd.dd_bp_cone_3d(y, angs, vol.shape, 30.0, 50.0, **kw)
+    bo = orc.dd_bp_cone_3d(y, angs, vol.shape, 30.0, 50.0, **kw)
+    assert rel(bp, bo) < 5e-5

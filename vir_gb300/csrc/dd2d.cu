@@ -153,7 +153,7 @@ __host__ __device__ inline int fp_line_entries(int nd) { return pad_idx(nd + 1) 
 
 // mode 0: out = FP;  mode 1 (SIRT residual): out = (y - FP) * inv_w, or FP
 // where inv_w == 0.
-template <bool FAN, int FP_WARPS, int FP_MAXB>
+template <bool FAN, int FP_WARPS, int FP_MAXB, bool GUARD>
 #ifndef VG_FP_MINB8
 #define VG_FP_MINB8 2
 #endif
@@ -178,6 +178,19 @@ dd2d_fp_kernel(vg_dd2d_geom g, const float *__restrict__ img, const float *__res
     const int jbase = blockIdx.x * FP_BINS;
     const int nb = min(FP_BINS, g.nu - jbase);  // bins of this block
     const float half = 0.5f * (float)nd;
+    // The inverse edge map has a pole at U* = -DSD pd / od (rays parallel to
+    // the lines).  It lies outside every line's shadow, but a detector wider
+    // than 2 DSD can reach it (|U*| >= DSD since |pd| >= |od|): then the
+    // GUARD instantiation runs, and a block whose bins contain the pole
+    // evaluates F directly as 0 before the line's first projected edge and
+    // the line total after its last, instead of trusting the inverse map
+    // beyond the pole.
+    bool guard = false;
+    if (GUARD && FAN && v.od != 0.f) {
+        const float Up = -g.DSD * v.pd / v.od;
+        const float Ua = det_edge(g, jbase), Ub = det_edge(g, jbase + nb);
+        guard = Up >= fminf(Ua, Ub) && Up <= fmaxf(Ua, Ub);
+    }
 
     // line-independent factor of the inverse map at every bin edge:
     // sweep index s(U) = (U a_l - b_l) C(U) + nd/2
@@ -198,6 +211,12 @@ dd2d_fp_kernel(vg_dd2d_geom g, const float *__restrict__ img, const float *__res
         const Line Lg = line_geo<FAN>(g, v, centre_coord(g.d_pix, io, no));
         const float la = FAN ? g.DSO - Lg.co : 1.f;       // inverse map numerator U la - lb
         const float lb = FAN ? g.DSD * Lg.cp : Lg.cp;
+        // the line's first and last projected edges in sweep order (guard only)
+        float Pf = 0.f, Pl = 0.f;
+        if (guard) {
+            Pf = proj<FAN>(g, v, Lg.cp, Lg.co, edge_coord(g.d_pix, rev ? nd : 0, nd));
+            Pl = proj<FAN>(g, v, Lg.cp, Lg.co, edge_coord(g.d_pix, rev ? 0 : nd, nd));
+        }
         const float *row = base + (size_t)io * nd;
         __syncwarp();  // previous line's reads are done
         // stage (P, S, V) of the line: lanes own FP_SEG consecutive pixels
@@ -261,7 +280,8 @@ dd2d_fp_kernel(vg_dd2d_geom g, const float *__restrict__ img, const float *__res
         for (int i = 0; i <= FP_MAXB; ++i) {
             const int e = min(lane + 32 * i, nb);  // edges past nb repeat the last one
             const float2 uc = make_float2(det_edge(g, jbase + e), Cs[lane + 32 * i]);
-            const float sidx = fmaf(fmaf(uc.x, la, -lb), uc.y, half);
+            float sidx = fmaf(fmaf(uc.x, la, -lb), uc.y, half);
+            if (guard) sidx = uc.x <= Pf ? -1.f : (uc.x >= Pl ? (float)nd : sidx);
             // slot of pixel floor(sidx): sentinel below the line, closing edge above
             const int k = (int)floorf(fminf(fmaxf(sidx, -1.f), (float)nd)) + 1;
             const float2 t = E[pad_idx(k)];
@@ -530,16 +550,21 @@ int launch_fp_t(const vg_dd2d_geom *g, const float *img, const float *imgT, cons
     const size_t red = (size_t)W * 32 * B * sizeof(float);
     if (smem < red) smem = red;
     VG_REQUIRE(smem <= 200 * 1024, "dd2d_fp: image side too large for this tile variant");
-    static size_t attr = 0;  // per instantiation: largest dynamic smem already allowed
-    if (smem > 48 * 1024 && smem > attr) {
-        cudaError_t e = cudaFuncSetAttribute(dd2d_fp_kernel<FAN, W, B>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    // the inverse map's pole can reach the detector only when it extends
+    // beyond DSD from the centre
+    const float ext = fmaxf(fabsf(g->du * (0.f - 0.5f * g->nu + g->su)),
+                            fabsf(g->du * ((float)g->nu - 0.5f * g->nu + g->su)));
+    const bool guard = FAN && ext >= g->DSD;
+    auto kern = guard ? dd2d_fp_kernel<FAN, W, B, true> : dd2d_fp_kernel<FAN, W, B, false>;
+    static size_t attr[2] = {0, 0};  // per instantiation: largest dynamic smem already allowed
+    if (smem > 48 * 1024 && smem > attr[guard]) {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
         if (e != cudaSuccess) return cuda_status(e, "dd2d_fp: shared memory attribute");
-        attr = smem;
+        attr[guard] = smem;
     }
     dim3 grid(ceil_div(g->nu, 32 * B), g->na);
-    dd2d_fp_kernel<FAN, W, B><<<grid, W * 32, smem, st>>>(*g, img, imgT, trig, out, mode, y,
-                                                         inv_w);
+    kern<<<grid, W * 32, smem, st>>>(*g, img, imgT, trig, out, mode, y, inv_w);
     return launch_status("dd2d_fp");
 }
 

@@ -39,6 +39,16 @@ __device__ __forceinline__ View3 view3(const double *trig, int ia) {
 __device__ __forceinline__ float cen(float d, int i, int n) { return d * ((float)i + 0.5f - 0.5f * n); }
 __device__ __forceinline__ float edg(float d, int i, int n) { return d * ((float)i - 0.5f * n); }
 
+// Pole of the inverse edge map (u of rays parallel to the lines): whether it
+// lies in [a, b].  It is outside every line's shadow, but a detector that
+// reaches DSD from the centre can contain it; ranges found through the
+// inverse map are then not trusted on an interval holding it.
+__device__ __forceinline__ bool pole_in(const vg_dd3d_geom &g, const View3 &v, float a, float b) {
+    if (v.od == 0.f) return false;
+    const float Up = -g.DSD * v.pd / v.od;
+    return Up >= fminf(a, b) && Up <= fmaxf(a, b);
+}
+
 __device__ __forceinline__ float projU(const vg_dd3d_geom &g, const View3 &v, float cp, float co,
                                        float b) {
     return __fdividef(g.DSD * fmaf(v.pd, b, cp), g.DSO - fmaf(v.od, b, co));
@@ -95,8 +105,9 @@ __device__ __noinline__ float fp_cell_line(const vg_dd3d_geom &g, const View3 &v
     const float rl = 1.0f / (g.DSD * v.pd + Ul * v.od), rr = 1.0f / (g.DSD * v.pd + Ur * v.od);
     const float kl = fmaf(Ul, g.DSO - co, -g.DSD * cp) * rl * inv_d + 0.5f * nd;
     const float kr = fmaf(Ur, g.DSO - co, -g.DSD * cp) * rr * inv_d + 0.5f * nd;
-    const int k0 = max(0, (int)floorf(fminf(kl, kr)));
-    const int k1 = min(nd - 1, (int)floorf(fmaxf(kl, kr)));
+    const bool pole = pole_in(g, v, Ul, Ur);
+    const int k0 = pole ? 0 : max(0, (int)floorf(fminf(kl, kr)));
+    const int k1 = pole ? nd - 1 : min(nd - 1, (int)floorf(fmaxf(kl, kr)));
     const float izl = Vl / (zmag * g.d_pix) + 0.5f * g.nz;
     const float izr = Vr / (zmag * g.d_pix) + 0.5f * g.nz;
     const int z0 = max(0, (int)floorf(izl)), z1 = min(g.nz - 1, (int)floorf(izr));
@@ -161,6 +172,7 @@ dd3d_fp_kernel(vg_dd3d_geom g, const float *__restrict__ vol, const float4 *__re
     const float TUl = ufloor_edge(g, u0), TUr = ufloor_edge(g, min(u0 + FT_U, g.nu));
     const float TVl = vfloor_edge(g, v0), TVr = vfloor_edge(g, min(v0 + FT_V, g.nv));
     const float rTl = 1.0f / (g.DSD * v.pd + TUl * v.od), rTr = 1.0f / (g.DSD * v.pd + TUr * v.od);
+    const bool tile_pole = pole_in(g, v, TUl, TUr);
     // table threads: tid < FT_U owns u-cell u0 + tid, FT_U <= tid < FT_U + FT_V a v-cell
     const int wu_i = u0 + tid, wv_i = v0 + tid - FT_U;
     const bool is_u = tid < FT_U && wu_i < g.nu;
@@ -171,6 +183,7 @@ dd3d_fp_kernel(vg_dd3d_geom g, const float *__restrict__ vol, const float4 *__re
         crl = 1.0f / (g.DSD * v.pd + cUl * v.od); crr = 1.0f / (g.DSD * v.pd + cUr * v.od);
     }
     if (is_v) { cVl = vfloor_edge(g, wv_i); cVr = vfloor_edge(g, wv_i + 1); }
+    const bool cell_pole = is_u && pole_in(g, v, cUl, cUr);
     const bool small = nd < 3 || g.nz < 3;
 
     Kahan acc[8];
@@ -188,8 +201,8 @@ dd3d_fp_kernel(vg_dd3d_geom g, const float *__restrict__ vol, const float4 *__re
         const float2 sz = __ldg(tab + (size_t)ia * nm + io);
         const float kl = fmaf(TUl, g.DSO - co, -g.DSD * cp) * rTl * inv_d + 0.5f * nd;
         const float kr = fmaf(TUr, g.DSO - co, -g.DSD * cp) * rTr * inv_d + 0.5f * nd;
-        const int kA = max(0, (int)floorf(fminf(kl, kr)));
-        const int kB = min(nd - 1, (int)floorf(fmaxf(kl, kr)));
+        const int kA = tile_pole ? 0 : max(0, (int)floorf(fminf(kl, kr)));
+        const int kB = tile_pole ? nd - 1 : min(nd - 1, (int)floorf(fmaxf(kl, kr)));
         const float izd = 1.0f / (sz.y * g.d_pix);
         const int zA = max(0, (int)floorf(TVl * izd + 0.5f * g.nz));
         const int zB = min(g.nz - 1, (int)floorf(TVr * izd + 0.5f * g.nz));
@@ -202,7 +215,7 @@ dd3d_fp_kernel(vg_dd3d_geom g, const float *__restrict__ vol, const float4 *__re
                 const float a = fmaf(cUl, g.DSO - co, -g.DSD * cp) * crl * inv_d + 0.5f * nd;
                 const float bb = fmaf(cUr, g.DSO - co, -g.DSD * cp) * crr * inv_d + 0.5f * nd;
                 const int ks = (int)floorf(fminf(a, bb)), ke = (int)floorf(fmaxf(a, bb));
-                if (ke - ks > 2 && ke >= 0 && ks < nd) S.wide[b] = io + 1;
+                if ((ke - ks > 2 && ke >= 0 && ks < nd) || cell_pole) S.wide[b] = io + 1;
                 kb0 = min(max(ks, 0), max(kmax, 0));
                 float pa = projU(g, v, cp, co, edg(g.d_pix, kb0, nd));
                 float ow[3];
