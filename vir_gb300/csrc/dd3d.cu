@@ -360,7 +360,7 @@ __device__ float bp_voxel_view(const vg_dd3d_geom &g, const View3 &v, const floa
     return part * sz.x;
 }
 
-__global__ void __launch_bounds__(256, 2)
+__global__ void __launch_bounds__(256, 3)
 dd3d_bp_kernel(vg_dd3d_geom g, const float *__restrict__ sino, const float4 *__restrict__ vf,
                const float2 *__restrict__ tab, float *__restrict__ vol) {
     __shared__ BpTables T;
