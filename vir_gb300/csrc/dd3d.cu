@@ -141,7 +141,7 @@ __device__ __noinline__ float fp_cell_line(const vg_dd3d_geom &g, const View3 &v
 // consecutive slices).  Lines where a cell overlaps more than 3 pixels or
 // slices take the per-cell global path.  The tables are double-buffered by
 // line parity, so one barrier per line suffices.  Line sums are added in
-// groups of FT_GROUP lines, each group with compensation.
+// groups of FT_GROUP lines and the group sums in a second running sum.
 constexpr int FT_U = 32, FT_V = 64;
 constexpr int FT_GROUP = 16;
 
@@ -153,7 +153,7 @@ struct FpTables {
     int wide[2];
 };
 
-__global__ void __launch_bounds__(256, 2)
+__global__ void __launch_bounds__(256, 3)
 dd3d_fp_kernel(vg_dd3d_geom g, const float *__restrict__ vol, const float4 *__restrict__ vf,
                const float2 *__restrict__ tab, float *__restrict__ sino) {
     __shared__ FpTables S;
@@ -186,10 +186,9 @@ dd3d_fp_kernel(vg_dd3d_geom g, const float *__restrict__ vol, const float4 *__re
     const bool cell_pole = is_u && pole_in(g, v, cUl, cUr);
     const bool small = nd < 3 || g.nz < 3;
 
-    Kahan acc[8];
-    float grp[8];
+    float acc[8], grp[8];
 #pragma unroll
-    for (int c = 0; c < 8; ++c) grp[c] = 0.f;
+    for (int c = 0; c < 8; ++c) acc[c] = grp[c] = 0.f;
     int ngrp = 0, nl = 0;
     // S.wide[b] == io + 1 marks line io for the global path; writers only
     // ever store that marker, so no reset races with them
@@ -298,7 +297,7 @@ dd3d_fp_kernel(vg_dd3d_geom g, const float *__restrict__ vol, const float4 *__re
         for (int q = 0; q < 8; ++q) grp[q] += part[q];
         if (++ngrp == FT_GROUP) {
 #pragma unroll
-            for (int q = 0; q < 8; ++q) { acc[q].add(grp[q]); grp[q] = 0.f; }
+            for (int q = 0; q < 8; ++q) { acc[q] += grp[q]; grp[q] = 0.f; }
             ngrp = 0;
         }
     }
@@ -309,9 +308,9 @@ dd3d_fp_kernel(vg_dd3d_geom g, const float *__restrict__ vol, const float4 *__re
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
             const int iv = v0 + 32 * h + lane;
-            acc[2 * j + h].add(grp[2 * j + h]);
+            acc[2 * j + h] += grp[2 * j + h];
             if (iu < g.nu && iv < g.nv)
-                sino[((size_t)ia * g.nu + iu) * g.nv + iv] = acc[2 * j + h].s * f;
+                sino[((size_t)ia * g.nu + iu) * g.nv + iv] = acc[2 * j + h] * f;
         }
     }
 }
