@@ -46,3 +46,38 @@ def test_argument_errors_without_gpu():
     st = L.vg_dd2d_fp(ctypes.byref(g), None, None, None, None, None)
     assert st == 1
     assert b"positive" in L.vg_last_error()
+
+
+def test_drop_in_table_resolves_and_installs():
+    """Every vir function named in the drop-in table exists here, and
+    install_into replaces it in an imported vir package (a stand-in tree of
+    empty modules, so no GPU and no vir import are needed)."""
+    import importlib
+    import sys
+    import types
+    import vir_gb300
+    for mod, fns in vir_gb300._DROP_INS.items():
+        for name, spec in fns.items():
+            m, a = spec.split(":")
+            assert callable(getattr(importlib.import_module(m), a)), spec
+    root = types.ModuleType("fakevir")
+    made = {"fakevir": root}
+    for mod in vir_gb300._DROP_INS:
+        parts = mod.split(".")
+        for i in range(1, len(parts) + 1):
+            full = "fakevir." + ".".join(parts[:i])
+            if full not in made:
+                made[full] = types.ModuleType(full)
+    saved = {k: sys.modules.get(k) for k in made}
+    sys.modules.update(made)
+    try:
+        done = vir_gb300.install_into(root)
+        assert len(done) == sum(len(f) for f in vir_gb300._DROP_INS.values())
+        from vir_gb300.sys_mat import dd
+        assert made["fakevir.sys_mat.dd"].dd_fp_fan_2d is dd.dd_fp_fan_2d
+    finally:
+        for k, v in saved.items():
+            if v is None:
+                sys.modules.pop(k, None)
+            else:
+                sys.modules[k] = v
