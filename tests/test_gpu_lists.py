@@ -101,3 +101,19 @@ def test_ctypes_list_entry_points(vg, golden):
     ph = np.zeros(c["phantom"].shape, np.float32)
     proj_ctype.sd_b_proj_c(ph, c["y"].copy(), rays)
     assert np.abs(ph - c["bp"]).max() <= 2e-6 * np.abs(c["bp"]).max()
+
+
+def test_numba_list_entry_points(vg, golden):
+    """proj_numba / proj_cuda drop-ins (CSR in, in-place or new sinogram)."""
+    from vir_gb300.projection import proj_numba
+    d = golden["siddons_cone"]
+    c = golden["list_c"]
+    nr = d["off"].size - 1
+    ref = c["sino"].astype(np.float64)
+    for fn in (proj_numba.sd_f_proj_numba, proj_numba.sd_f_proj_numba_p,
+               proj_numba.sd_f_proj_numba_g):
+        s = fn(c["phantom"], (d["ind"], d["len"], d["off"]), (nr,))
+        assert s.dtype == np.float32 and np.abs(s - ref).max() <= 2e-6 * np.abs(ref).max()
+    out = np.zeros(nr, np.float32)
+    proj_numba.fast_forward_project_p(c["phantom"].ravel(), d["ind"], d["len"], d["off"], out)
+    assert np.abs(out - ref).max() <= 2e-6 * np.abs(ref).max()

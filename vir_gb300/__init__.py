@@ -49,6 +49,10 @@ _DROP_INS = {
     "projection.proj": {n: "vir_gb300.projection.proj:" + n for n in ("sd_f_proj", "sd_b_proj")},
     "projection.proj_ctype": {n: "vir_gb300.projection.proj_ctype:" + n
                               for n in ("sd_f_proj_c", "sd_b_proj_c")},
+    "projection.proj_numba": {n: "vir_gb300.projection.proj_numba:" + n
+                              for n in ("fast_forward_project", "fast_forward_project_p",
+                                        "sd_f_proj_numba", "sd_f_proj_numba_p")},
+    "projection.proj_cuda": {"sd_f_proj_numba_g": "vir_gb300.projection.proj_numba:sd_f_proj_numba_g"},
 }
 
 
