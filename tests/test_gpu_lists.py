@@ -117,3 +117,18 @@ def test_numba_list_entry_points(vg, golden):
     out = np.zeros(nr, np.float32)
     proj_numba.fast_forward_project_p(c["phantom"].ravel(), d["ind"], d["len"], d["off"], out)
     assert np.abs(out - ref).max() <= 2e-6 * np.abs(ref).max()
+
+
+def test_mp_list_entry_points(vg, golden):
+    """proj_mp drop-ins on an unraveled object-array list."""
+    from vir_gb300.projection import proj_mp
+    from vir_gb300.sys_mat import siddon as sd
+    d, c = golden["siddons_cone"], golden["list_c"]
+    nP = tuple(int(v) for v in d["nPixels"])
+    sdl = sd.siddons(d["src"], d["trg"], nP, tuple(d["dPixels"]))
+    s = proj_mp.mp_sd_f_proj(c["phantom"], sdl)
+    assert s.shape == sdl.shape
+    ref = c["sino"].reshape(sdl.shape).astype(np.float64)
+    assert np.abs(s - ref).max() <= 2e-6 * np.abs(ref).max()
+    b = proj_mp.mpc_sd_b_proj(c["y"].reshape(sdl.shape), sdl, nP)
+    assert np.abs(b - c["bp"]).max() <= 2e-6 * np.abs(c["bp"]).max()
