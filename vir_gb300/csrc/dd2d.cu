@@ -9,18 +9,16 @@
 // with P_k the projection of driving edge k on line io.  Here each thread
 // owns output elements and gathers their terms; no atomics, deterministic.
 //
-//  FP (dd2d_fp_kernel): one block per view (x a bin range).  Orthogonal lines
-//    are processed in chunks: the block first projects every driving edge of
-//    the chunk's lines into shared memory (one division per edge, shared by
-//    all bins) and stages the lines' pixels pre-multiplied by the line scale;
-//    then each thread walks its bins down the chunk, keeping per bin the
-//    index of the pixel under its left edge (it moves by at most a step from
-//    one line to the next), and sums the 1-3 overlapping pixels.
-//  BP (dd2d_bp_kernel): one block per 64x16 pixel tile (2x2 per thread).  Views are processed
-//    in chunks: the block projects the tile's driving edges for every view of
-//    the chunk into shared memory (one division per edge, shared by the two
-//    pixels on either side) with the line scales; then each thread sums, per
-//    view, the 1-3 bins overlapped by its pixel's projected interval.
+//  FP (dd2d_fp_kernel): one block per view (x a bin range), one warp per
+//    orthogonal line at a time.  The warp projects the line's driving edges
+//    (one division per edge), stages the running integral of its pixels in
+//    shared memory, and every lane evaluates that integral at the left edges
+//    of its bins through the inverse edge map; a bin's term is the
+//    difference of the integral at its two edges.
+//  BP (dd2d_bp_kernel): one block per 64x16 pixel tile (2x2 per thread).  A
+//    per-view table holds the running integral of the sinogram row; each
+//    thread projects its patch's driving edges (three per line, shared by
+//    neighbouring pixels) and takes differences of the table at them.
 //
 // Geometry per dd.py:
 //  - driving axis X when |sin| >= |cos| (dd.py:478, 532);
@@ -157,13 +155,14 @@ template <bool FAN, int FP_WARPS, int FP_MAXB, bool GUARD>
 #ifndef VG_FP_MINB8
 #define VG_FP_MINB8 2
 #endif
-__global__ void __launch_bounds__(FP_WARPS * 32, (FP_MAXB > 24 ? 1 : (FP_WARPS >= 8 ? VG_FP_MINB8 : 16 / FP_WARPS)))
+// (the guarded variants of the 24-bin tiles give up occupancy rather than spill)
+__global__ void __launch_bounds__(FP_WARPS * 32, ((FP_MAXB > 24 || (GUARD && FP_MAXB == 24)) ? 1 : (FP_WARPS >= 8 ? VG_FP_MINB8 : 16 / FP_WARPS)))
 dd2d_fp_kernel(vg_dd2d_geom g, const float *__restrict__ img, const float *__restrict__ imgT,
                const double *__restrict__ trig, float *__restrict__ out, int mode,
                const float *__restrict__ y, const float *__restrict__ inv_w) {
     constexpr int FP_BINS = 32 * FP_MAXB;  // bins per block
     extern __shared__ float2 smem2[];
-    __shared__ float Cs[FP_BINS + 32];  // per bin edge C(U); entries past nb repeat nb
+    __shared__ float2 UC[FP_BINS + 32];  // per bin edge (U, C(U)); entries past nb repeat nb
     const int ia = blockIdx.y;
     const ViewGeo v = view_geo(trig, ia);
     const int nd = v.xdrv ? g.nx : g.ny;
@@ -198,7 +197,7 @@ dd2d_fp_kernel(vg_dd2d_geom g, const float *__restrict__ img, const float *__res
         const float sig = (rev ? -1.f : 1.f) / g.d_pix;
         for (int e = threadIdx.x; e < FP_BINS + 32; e += FP_WARPS * 32) {
             const float U = det_edge(g, jbase + min(e, nb));
-            Cs[e] = FAN ? sig / (g.DSD * v.pd + U * v.od) : sig / v.pd;
+            UC[e] = make_float2(U, FAN ? sig / (g.DSD * v.pd + U * v.od) : sig / v.pd);
         }
     }
     __syncthreads();
@@ -222,14 +221,26 @@ dd2d_fp_kernel(vg_dd2d_geom g, const float *__restrict__ img, const float *__res
         // stage (P, S, V) of the line: lanes own FP_SEG consecutive pixels
         // (edge coordinate b0 + i db along a lane's segment)
         const float db = rev ? -g.d_pix : g.d_pix;
+        // along the segment the projection's numerator and denominator are
+        // affine in the edge number i: P_i = (n0 + i dn) / (d0 + i dd)
+        const float dn = (FAN ? g.DSD : 1.f) * v.pd * db;
+        const float dd = -v.od * db;
         float carry = 0.f;
         for (int r0 = 0; r0 < nd; r0 += 32 * FP_SEG) {
             const int m0 = r0 + lane * FP_SEG;
             const float b0 = edge_coord(g.d_pix, rev ? nd - m0 : m0, nd);
+            const float n0 = (FAN ? g.DSD : 1.f) * fmaf(v.pd, b0, Lg.cp);
+            const float d0 = g.DSO - fmaf(v.od, b0, Lg.co);
             float Pv[FP_SEG + 1], q[FP_SEG];
 #pragma unroll
-            for (int i = 0; i <= FP_SEG; ++i)
-                Pv[i] = proj<FAN>(g, v, Lg.cp, Lg.co, fmaf((float)i, db, b0));
+            for (int i = 0; i <= FP_SEG; ++i) {
+                const float num = fmaf((float)i, dn, n0);
+#if VG_FAST_DIV
+                Pv[i] = FAN ? __fdividef(num, fmaf((float)i, dd, d0)) : num;
+#else
+                Pv[i] = FAN ? num / fmaf((float)i, dd, d0) : num;
+#endif
+            }
             // pixels m0 .. m0 + FP_SEG - 1 (sweep order): four 16-byte loads when
             // the segment is whole and aligned, else element by element
             float tot = 0.f;
@@ -278,20 +289,22 @@ dd2d_fp_kernel(vg_dd2d_geom g, const float *__restrict__ img, const float *__res
         float Fl[FP_MAXB + 1];
 #pragma unroll
         for (int i = 0; i <= FP_MAXB; ++i) {
-            const int e = min(lane + 32 * i, nb);  // edges past nb repeat the last one
-            const float2 uc = make_float2(det_edge(g, jbase + e), Cs[lane + 32 * i]);
+            const float2 uc = UC[lane + 32 * i];  // edges past nb repeat the last one
             float sidx = fmaf(fmaf(uc.x, la, -lb), uc.y, half);
             if (guard) sidx = uc.x <= Pf ? -1.f : (uc.x >= Pl ? (float)nd : sidx);
-            // slot of pixel floor(sidx): sentinel below the line, closing edge above
-            const int k = (int)floorf(fminf(fmaxf(sidx, -1.f), (float)nd)) + 1;
+            // slot of pixel floor(sidx): sentinel below the line, closing edge
+            // above (the conversion saturates, so the clamp also bounds +-inf)
+            const int k = min(max(__float2int_rd(sidx), -1), nd) + 1;
             const float2 t = E[pad_idx(k)];
             Fl[i] = fmaf(t.y, uc.x, t.x);
         }
+        // right edge of bin lane + 32 i: lane + 1's left edge, or for lane 31
+        // lane 0's next one -- one rotation of (lane 0 ? Fl[i + 1] : Fl[i])
+        const int src = (lane + 1) & 31;
 #pragma unroll
         for (int i = 0; i < FP_MAXB; ++i) {
-            const float nxt = __shfl_down_sync(0xffffffffu, Fl[i], 1);
-            const float wrap = __shfl_sync(0xffffffffu, Fl[i + 1], 0);
-            acc[i] += ((lane == 31) ? wrap : nxt) - Fl[i];
+            const float r = __shfl_sync(0xffffffffu, lane == 0 ? Fl[i + 1] : Fl[i], src);
+            acc[i] += r - Fl[i];
         }
     }
 
@@ -321,12 +334,14 @@ dd2d_fp_kernel(vg_dd2d_geom g, const float *__restrict__ img, const float *__res
 //
 // For one view, let G(u) be the running integral of the sinogram row as a
 // piecewise-constant function of u (bin j spans [U_j, U_j+1]):
-//     G(u) = T_j + du sino_j (u - U_j)/du,  j = floor((u - U_0)/du),  T_j = du sum_{i<j} sino_i.
+//     G(u) = T_j + du sino_j (t - j),  t = (u - U_0)/du,  j = floor(t),  T_j = du sum_{i<j} sino_i.
 // A pixel whose driving edges project to lo <= hi receives
 // scale(line) * (G(hi) - G(lo)) from the view -- the sum of sino * overlap *
 // scale that vir's merge distributes.  dd2d_bp_prep writes, per view, the
-// table (T_j, du sino_j) (prefix accumulated in FP64) and the line scales;
-// the main kernel evaluates G at the two projected edges of each pixel.
+// table (T_j - j du sino_j, du sino_j) (prefix accumulated in FP64), so that
+// G = x_j + y_j t, and the line scales signed by the direction in which the
+// line's edges project; the main kernel evaluates G at the two projected
+// edges of each pixel.
 // ---------------------------------------------------------------------------
 
 #ifndef VG_BP_TY
@@ -347,16 +362,22 @@ constexpr int BP_TX = VG_BP_TX;  // pixels along x (threadIdx.y)
 constexpr int BP_VC = (BP_TY * BP_TX < 128) ? BP_TY * BP_TX : 128;  // views staged per chunk
 
 struct BpWork {
-    float2 *ts;  // [na][nu + 1]: (T_j, du * sino_j)
-    float *scl;  // [na][max(nx, ny)]: line scale for the view's driving axis
+    float2 *ts;  // [na][nu + 1]: (T_j - j du sino_j, du sino_j)
+    float *scl;  // [na][scl_stride]: signed line scale for the view's driving axis
 };
+
+// scale rows hold max(nx, ny) lines, padded to an even count so that a
+// pixel patch reads its two lines as one 8-byte load
+__host__ __device__ inline int scl_stride(const vg_dd2d_geom &g) {
+    const int nm = g.nx > g.ny ? g.nx : g.ny;
+    return nm + (nm & 1);
+}
 
 size_t bp_ws_ts_bytes(const vg_dd2d_geom *g) {
     return ((size_t)g->na * (g->nu + 1) * sizeof(float2) + 255) & ~(size_t)255;
 }
 size_t bp_ws_bytes(const vg_dd2d_geom *g) {
-    int nm = g->nx > g->ny ? g->nx : g->ny;
-    return bp_ws_ts_bytes(g) + (((size_t)g->na * nm * sizeof(float) + 255) & ~(size_t)255);
+    return bp_ws_ts_bytes(g) + (((size_t)g->na * scl_stride(*g) * sizeof(float) + 255) & ~(size_t)255);
 }
 BpWork bp_ws(const vg_dd2d_geom *g, void *ws) {
     BpWork w;
@@ -397,25 +418,41 @@ dd2d_bp_prep(vg_dd2d_geom g, const float *__restrict__ sino, const double *__res
         const int j = j0 + i;
         if (j < g.nu) {
             const float sv = __ldg(row + j);
-            ts[j] = make_float2((float)(run * du), g.du * sv);
+            ts[j] = make_float2((float)((run - (double)j * (double)sv) * du), g.du * sv);
             run += (double)sv;
         }
     }
     if (threadIdx.x == 255) ts[g.nu] = make_float2((float)(run * du), 0.f);
-    // line scales of this view
+    // line scales of this view, negated for lines whose edges project in
+    // decreasing order (the pixel's interval is then [P(b+1), P(b)])
     const ViewGeo v = view_geo(trig, ia);
     const int no = v.xdrv ? g.ny : g.nx;
-    const int nm = g.nx > g.ny ? g.nx : g.ny;
-    for (int io = threadIdx.x; io < no; io += 256)
-        w.scl[(size_t)ia * nm + io] = line_geo<FAN>(g, v, centre_coord(g.d_pix, io, no)).scl;
+    const int nd = v.xdrv ? g.nx : g.ny;
+    for (int io = threadIdx.x; io < no; io += 256) {
+        const Line L = line_geo<FAN>(g, v, centre_coord(g.d_pix, io, no));
+        const float P0 = proj<FAN>(g, v, L.cp, L.co, edge_coord(g.d_pix, 0, nd));
+        const float P1 = proj<FAN>(g, v, L.cp, L.co, edge_coord(g.d_pix, nd, nd));
+        w.scl[(size_t)ia * scl_stride(g) + io] = P1 >= P0 ? L.scl : -L.scl;
+    }
+}
+
+__device__ __forceinline__ float rcp_approx(float x) {
+#if VG_FAST_DIV
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+#else
+    return 1.0f / x;
+#endif
 }
 
 __device__ __forceinline__ float bp_G(const float2 *__restrict__ ts, int nu, float t) {
-    // t: position in bins from U_0
-    const float tc = fminf(fmaxf(t, 0.f), (float)nu);
-    const int j = min((int)tc, nu - 1);
+    // t: position in bins from U_0.  Before U_0 entry 0 gives x_0 = 0; past
+    // U_nu entry nu holds (T_nu, 0); the conversion saturates.
+    const float tc = fmaxf(t, 0.f);
+    const int j = min(__float2int_rz(tc), nu);
     const float2 e = __ldg(ts + j);
-    return fmaf(e.y, tc - (float)j, e.x);
+    return fmaf(e.y, tc, e.x);
 }
 
 // Each thread owns a 2x2 pixel patch.  A view drives along x (X-driven) or y:
@@ -429,15 +466,18 @@ __global__ void __launch_bounds__(BP_TY * BP_TX, VG_BP_MINB)
 dd2d_bp_kernel(vg_dd2d_geom g, BpWork w, const double *__restrict__ trig,
                float *__restrict__ img, int mode, const float *__restrict__ inv_w, float gamma,
                float *__restrict__ xT) {
-    __shared__ float4 Vs[BP_VC];  // (pd, od, po, oo)
+    // per view: fan (DSD pd/du, -od, DSD po/du, -oo), parallel (pd/du, 0, po/du, 0):
+    // an edge b on the line through cen lands at bin position
+    //   t = (x b + z cen) / (DSO + y b + w cen) + t0   (fan)
+    //   t = x b + z cen + t0                           (parallel)
+    __shared__ float4 Vs[BP_VC];
     __shared__ int Xs[BP_VC];
     const int tid = threadIdx.y * BP_TY + threadIdx.x;
     const int iy = blockIdx.x * (2 * BP_TY) + 2 * threadIdx.x;  // patch origin
     const int ix = blockIdx.y * (2 * BP_TX) + 2 * threadIdx.y;
     const bool inside = iy < g.ny && ix < g.nx;
-    const int nm = g.nx > g.ny ? g.nx : g.ny;
-    const float u0 = det_edge(g, 0);
-    const float inv_du = 1.0f / g.du;
+    const int sstr = scl_stride(g);
+    const float t0 = -det_edge(g, 0) / g.du;
     const float bx = edge_coord(g.d_pix, ix, g.nx), by = edge_coord(g.d_pix, iy, g.ny);
     const float cx0 = bx + 0.5f * g.d_pix, cy0 = by + 0.5f * g.d_pix;
     const float2 *ts_all = w.ts;
@@ -447,7 +487,9 @@ dd2d_bp_kernel(vg_dd2d_geom g, BpWork w, const double *__restrict__ trig,
         __syncthreads();
         if (tid < nv) {
             const ViewGeo v = view_geo(trig, a0 + tid);
-            Vs[tid] = make_float4(v.pd, v.od, v.po, v.oo);
+            const float k = (FAN ? g.DSD : 1.f) / g.du;
+            Vs[tid] = FAN ? make_float4(k * v.pd, -v.od, k * v.po, -v.oo)
+                          : make_float4(k * v.pd, 0.f, k * v.po, 0.f);
             Xs[tid] = v.xdrv;
         }
         __syncthreads();
@@ -462,34 +504,25 @@ dd2d_bp_kernel(vg_dd2d_geom g, BpWork w, const double *__restrict__ trig,
             const int io0 = xd ? iy : ix;
             const int no = xd ? g.ny : g.nx;
             const float2 *ts = ts_all + (size_t)(a0 + vi) * (g.nu + 1);
-            const float *sc = w.scl + (size_t)(a0 + vi) * nm;
+            // signed scales of lines io0 and io0 + 1 (io0 is even; rows padded)
+            const float2 sc2 = __ldg(reinterpret_cast<const float2 *>(w.scl + (size_t)(a0 + vi) * sstr + io0));
             float cL[2][2];  // [line][position along the driving axis]
 #pragma unroll
             for (int L = 0; L < 2; ++L) {
                 const float cen = c0 + (float)L * g.d_pix;
-                const float cp = q.z * cen;
-                float P[3];
+                const float nc = FAN ? q.z * cen : fmaf(q.z, cen, t0);
+                const float dc = fmaf(q.w, cen, g.DSO);
+                float G[3];
 #pragma unroll
                 for (int e = 0; e < 3; ++e) {
                     const float b = fmaf((float)e, g.d_pix, b0);
-                    float p = fmaf(q.x, b, cp);
-                    if (FAN) {
-                        const float den = g.DSO - fmaf(q.y, b, q.w * cen);
-#if VG_FAST_DIV
-                        p = __fdividef(g.DSD * p, den);
-#else
-                        p = g.DSD * p / den;
-#endif
-                    }
-                    P[e] = p;
+                    const float t = FAN ? fmaf(fmaf(q.x, b, nc), rcp_approx(fmaf(q.y, b, dc)), t0)
+                                        : fmaf(q.x, b, nc);
+                    G[e] = bp_G(ts, g.nu, t);
                 }
-                const float G0 = bp_G(ts, g.nu, (P[0] - u0) * inv_du);
-                const float G1 = bp_G(ts, g.nu, (P[1] - u0) * inv_du);
-                const float G2 = bp_G(ts, g.nu, (P[2] - u0) * inv_du);
-                const float sgn = (P[2] >= P[0]) ? 1.f : -1.f;  // monotone line
-                const float s = (io0 + L < no) ? __ldg(sc + io0 + L) * sgn : 0.f;
-                cL[L][0] = (G1 - G0) * s;
-                cL[L][1] = (G2 - G1) * s;
+                const float s = (io0 + L < no) ? (L ? sc2.y : sc2.x) : 0.f;
+                cL[L][0] = (G[1] - G[0]) * s;
+                cL[L][1] = (G[2] - G[1]) * s;
             }
             // X-driven: line = y offset, position = x offset; Y-driven: the transpose
             part[0][0] += cL[0][0];
