@@ -153,6 +153,41 @@ struct FpTables {
     int wide[2];
 };
 
+// One line's share of a thread's 4 u-cells x 2 v-cells: 1-3 pixel rows
+// (trailing rows with zero weight are skipped; the u-cell, hence the branch,
+// is the same for the whole warp; a zero row before a weighted one, at the
+// volume's far edge, is kept) x NV slices.
+template <int NV>
+__device__ __forceinline__ void fp_cells(const float4 *uw, const int *uk, const float *line,
+                                         size_t sk, float4 wa, float4 wb, int za, int zb,
+                                         float part[8]) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const float4 wu = uw[j];
+        const float *r = line + (size_t)uk[j] * sk;
+        const int nrow = wu.z != 0.f ? 3 : (wu.y != 0.f ? 2 : 1);
+        float ca = 0.f, cb = 0.f;
+#pragma unroll
+        for (int t = 0; t < 3; ++t) {
+            if (t >= nrow) break;
+            const float *q = r + t * sk;
+            float sa, sb;
+            if (NV == 3) {
+                sa = fmaf(wa.x, __ldg(q + za), fmaf(wa.y, __ldg(q + za + 1), wa.z * __ldg(q + za + 2)));
+                sb = fmaf(wb.x, __ldg(q + zb), fmaf(wb.y, __ldg(q + zb + 1), wb.z * __ldg(q + zb + 2)));
+            } else {
+                sa = fmaf(wa.x, __ldg(q + za), wa.y * __ldg(q + za + 1));
+                sb = fmaf(wb.x, __ldg(q + zb), wb.y * __ldg(q + zb + 1));
+            }
+            const float wt = t == 0 ? wu.x : (t == 1 ? wu.y : wu.z);
+            ca = fmaf(wt, sa, ca);
+            cb = fmaf(wt, sb, cb);
+        }
+        part[2 * j] = ca;
+        part[2 * j + 1] = cb;
+    }
+}
+
 __global__ void __launch_bounds__(256, 3)
 dd3d_fp_kernel(vg_dd3d_geom g, const float *__restrict__ vol, const float4 *__restrict__ vf,
                const float2 *__restrict__ tab, float *__restrict__ sino) {
@@ -256,28 +291,12 @@ dd3d_fp_kernel(vg_dd3d_geom g, const float *__restrict__ vol, const float4 *__re
             const float4 wa = S.vw[b][lane], wb = S.vw[b][32 + lane];
             const int za = S.vz[b][lane], zb = S.vz[b][32 + lane];
             const float *line = vol + (size_t)io * so;
-#pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                const float4 wu = S.uw[b][4 * warp + j];
-                const float *r = line + (size_t)S.uk[b][4 * warp + j] * sk;
-                // trailing pixel rows with zero weight are skipped (the u-cell,
-                // hence the branch, is the same for the whole warp; a zero row
-                // before a weighted one, at the volume's far edge, is kept)
-                const int nrow = wu.z != 0.f ? 3 : (wu.y != 0.f ? 2 : 1);
-                float ca = 0.f, cb = 0.f;
-#pragma unroll
-                for (int t = 0; t < 3; ++t) {
-                    if (t >= nrow) break;
-                    const float *q = r + t * sk;
-                    const float sa = fmaf(wa.x, __ldg(q + za), fmaf(wa.y, __ldg(q + za + 1), wa.z * __ldg(q + za + 2)));
-                    const float sb = fmaf(wb.x, __ldg(q + zb), fmaf(wb.y, __ldg(q + zb + 1), wb.z * __ldg(q + zb + 2)));
-                    const float wt = t == 0 ? wu.x : (t == 1 ? wu.y : wu.z);
-                    ca = fmaf(wt, sa, ca);
-                    cb = fmaf(wt, sb, cb);
-                }
-                part[2 * j] = ca;
-                part[2 * j + 1] = cb;
-            }
+            // when no cell of the warp weights a third slice (slices project
+            // at least a cell high), the third read and its zero term go
+            if (__all_sync(0xffffffffu, wa.z == 0.f && wb.z == 0.f))
+                fp_cells<2>(S.uw[b] + 4 * warp, S.uk[b] + 4 * warp, line, sk, wa, wb, za, zb, part);
+            else
+                fp_cells<3>(S.uw[b] + 4 * warp, S.uk[b] + 4 * warp, line, sk, wa, wb, za, zb, part);
         } else {
 #pragma unroll 1
             for (int j = 0; j < 4; ++j) {
