@@ -220,6 +220,10 @@ EXTRA = {
           "720 views over 2pi, 1024x768 detector at 0.8 mm, DSO 600 mm, DSD 1100 mm",
     "c5": "3D cone DD FP + BP: 256^3 volume of 20 random ellipsoids, 1 mm voxels, 360 views "
           "over 2pi, 512x384 detector at 1.6 mm, DSO 600 mm, DSD 1100 mm",
+    "bh": "beam-hardening pre-correction of a 720 x 1024 x 768 float32 logged sinogram (the "
+          "C4 detector): water polynomial with np.polyfit coefficients (float64 result) and with "
+          "Python-float coefficients (float32 result), 1000-entry spectrum table (interp1d), "
+          "4001-entry lookup table (np.interp); each result in numpy's dtype, bit for bit",
     "square": "translational square geometry DD FP + BP (dd_fp_square / dd_bp_square) at the "
               "reference's SIRT-script size (64^3, 96x10 sources, 129x64 cells) and at its "
               "nice.py size (250^3, 650x10 sources, 961x121 cells)",
@@ -380,6 +384,50 @@ def run_workload(args):
             line["cases"] = out
             print(json.dumps(line), flush=True)
         return 0
+    elif wl == "bh":
+        from vir_gb300 import beamhard as bh
+        na, nu, nv = 720, 1024, 768
+        g = torch.Generator(device=dev).manual_seed(5)
+        li = torch.rand((na, nu, nv), device=dev, generator=g) * 7.0
+        e = np.arange(20.0, 121.0)
+        cnt = np.exp(-0.5 * ((e - 62.0) / 18.0) ** 2)
+        water = lambda m, x: 0.17 + 2500.0 * np.asarray(x, np.float64) ** -3.0  # synthetic
+        ae = float(water("H2O", [np.average(e, weights=cnt)])[0])
+        coefs = np.polyfit(np.linspace(0, 10, 50), np.linspace(0, 10, 50) ** 1.1, 2)
+        lut = 1.0 + 0.05 * np.sin(np.linspace(0, 3, 4001))
+        pyc = [float(c) for c in coefs]
+        runs = {"poly": lambda: bh.beamhard_cor(li, coefs, 0.2),
+                "poly_f32": lambda: bh.beamhard_cor(li, pyc, 0.2),
+                "table": lambda: bh.beamhard_cor_table(li, e, cnt, None, ae, mixatten=water),
+                "lut": lambda: bh.beamhard_cor2(li, lut, 0.2)}
+        n = li.numel()
+        out = {}
+        sample = li[:8].cpu().numpy()  # 1/90 of the sinogram for the CPU path
+        orc = orc_mod()
+        cpu = {"poly": lambda: orc.bh_poly(sample, coefs, 0.2),
+               "poly_f32": lambda: orc.bh_poly(sample, pyc, 0.2),
+               "table": lambda: orc.bh_table(sample, e, cnt, ae, water("H2O", e)),
+               "lut": lambda: orc.bh_lut(sample, lut, 0.2)}
+        for k, fn in runs.items():
+            nbytes = (8.0 if k == "poly_f32" else 12.0) * n  # float32 in; float32 / float64 out
+            ms = _event_ms(fn, reps, stream)
+            gbs = nbytes / (ms / 1e3) / 1e9
+            t0 = time.perf_counter()
+            cpu[k]()
+            cpu_ms = (time.perf_counter() - t0) * 1e3 * (n / sample.size)
+            out[k] = {"ms": ms, "gsamples_per_s": n / (ms / 1e3) / 1e9,
+                      # float64 results replay numpy's float64 arithmetic: the FP64 pipe,
+                      # not HBM, bounds those cases; the HBM fraction is shown beside it
+                      "roofline": {"bound": "hbm" if k == "poly_f32" else "fp64 pipe",
+                                   "achieved": gbs, "peak": peak, "unit": "GB/s",
+                                   "frac": gbs / peak, "bytes_per_launch": nbytes},
+                      "cpu_numpy_ms_full_size": cpu_ms}
+        line.update({"cases": out, "cpu_baseline": {
+            "kind": "port", "cores": 1,
+            "sample": "the oracle's numpy/scipy restatement of beamhard.py:16-47 and "
+                      "beamhard_test.py:26-27 on 8 of 720 views, scaled to the full sinogram"}})
+        print(json.dumps(line), flush=True)
+        return 0
     elif wl == "c3":
         from vir_gb300.batched import BatchedSIRT2D
         from vir_gb300.workloads import batched_problems
@@ -408,9 +456,23 @@ def run_workload(args):
                  "fwd_back_gups": 2 * units / ((t_fp + t_bp) / 1e3) / 1e9,
                  "roofline_fp": _roof(units, t_fp, peak), "roofline_bp": _roof(units, t_bp, peak)})
     if wl == "c4":
+        from vir_gb300 import autograd as ag
         from vir_gb300 import reconstruction as rc
         line["kernel_ms"]["fdk"] = _event_ms(
             lambda: rc.fdk(y, angs, (n, n, n), 600.0, 1100.0, du=du, dv=du, d_pix=dp), 1, stream)
+        # 20 SIRT iterations of vir's rule (19 updates, weights included) on the cone pair
+        geom = ag.ConeGeom(tuple(angs), (n, n, n), nu, nv, 600.0, 1100.0, **kw)
+        out = {}
+
+        def sirt20():
+            out["x"] = ag.sirt(y, geom, iters=20)
+
+        t_sirt = _event_ms(sirt20, 1, stream)
+        rmse = float(torch.sqrt(torch.mean((out["x"] - x) ** 2)))
+        line["sirt"] = {"iters": 20, "updates": 19, "ms": t_sirt,
+                        "iter_per_s": 19 / (t_sirt / 1e3), "rmse_vs_phantom": rmse,
+                        "path": "unfused: projector calls + torch elementwise ops, W_sino/W_img "
+                                "computed inside the timed call"}
     print(json.dumps(line), flush=True)
     return 0
 

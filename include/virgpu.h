@@ -404,6 +404,33 @@ int vg_compact_nonzero(const float *v, long long n, const long long *first, int 
 int vg_filter_rows(const float *in, int rows, int nu, const float *taps,
                    const float *row_weight, float *out, void *stream);
 
+/* Beam-hardening pre-correction of logged sinograms (processing/beamhard.py),
+ * elementwise over n values; `in` and `out` are float32 or float64
+ * (in_f64 / out_f64), computed as numpy computes the reference's
+ * expressions, every operation separately rounded.
+ *   vg_bh_poly: out = mu ((c0 t^2 + c1 t) + c2), t = in / mu -- beamhard_cor
+ *     (beamhard.py:39-47).  Bit i of f32mask makes step i float32 (else
+ *     float64), as numpy's promotion of the caller's types decides: 0 t and
+ *     t^2, 1 c0 t^2, 2 c1 t, 3 the sum with c2, 4 the product with mu.
+ *   vg_bh_interp: piecewise-linear lookup in a table of m (2..VG_BH_MAX_TABLE)
+ *     increasing abscissae: seg holds m rows (x_k, y_k, s_k, 0) of float64
+ *     (16-byte aligned) with s_k = (y_k+1 - y_k) / (x_k+1 - x_k) (0 for the
+ *     last row); keys the m search keys: x_k as float64, or (key_f32, float32
+ *     samples only) x_k rounded to float32 toward -inf for mode 0 and toward
+ *     +inf for modes 1 / 2.
+ *     mode 0: scipy interp1d 'linear' on in.clip(0), as beamhard_cor_table
+ *       (beamhard.py:16-36); values outside [x_0, x_m-1] are added to
+ *       *n_outside (a device counter, may be NULL; interp1d raises for them).
+ *     mode 1 / 2: out = in * np.interp(in / mu, x, y), the lookup-table
+ *       correction of tests/Test_Beamhard/beamhard_test.py:26-27, with the
+ *       division in float32 (1) or float64 (2). */
+#define VG_BH_MAX_TABLE 4096
+int vg_bh_poly(const void *in, int in_f64, void *out, int out_f64, size_t n, double mu,
+               double c0, double c1, double c2, int f32mask, void *stream);
+int vg_bh_interp(const void *in, int in_f64, void *out, int out_f64, size_t n, const double *seg,
+                 const void *keys, int key_f32, int m, int mode, double mu,
+                 unsigned long long *n_outside, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -569,3 +569,51 @@ def tv_pdhg(g, fp, bp, img_shape, lam=1.0, theta=1.0, iters=100):
         u = u + tau * (tv_div(z) - bp(q.astype(np.float32)))
         ub = u + theta * (u - u_prev)
     return u
+
+
+# ---- beam-hardening pre-correction (processing/beamhard.py) ------------------
+# The reference's corrections are numpy / scipy expressions; restated here as
+# the checker, with numpy's own types (float32 sinograms stay float32 where
+# the reference's expression keeps them so).
+
+def bh_poly(line_ints, coefs, mu):
+    """beamhard_cor (beamhard.py:39-47): mu (c0 t^2 + c1 t + c2), t = x / mu."""
+    t = np.asarray(line_ints) / mu
+    return mu * (coefs[0] * t ** 2 + coefs[1] * t + coefs[2])
+
+
+def bh_spectrum_table(energies, counts, atten_eff, attens):
+    """The interp1d table of beamhard_cor_table (beamhard.py:30-34):
+    (x, y) = (polyenergetic, monoenergetic) water line integrals of 1000
+    thicknesses in [0, 80]."""
+    pl = np.linspace(0, 80, 1000)
+    pp = -1.0 * np.log(np.sum(counts * np.exp(-1.0 * np.outer(pl, attens)), axis=1)
+                       / np.sum(counts)) / atten_eff
+    return pp * atten_eff, pl * atten_eff
+
+
+def bh_table(line_ints, energies, counts, atten_eff, attens):
+    """beamhard_cor_table (beamhard.py:16-36): linear interp1d of the table
+    at line_ints.clip(0); raises ValueError outside the table as interp1d."""
+    from scipy import interpolate
+    x, y = bh_spectrum_table(energies, counts, atten_eff, attens)
+    return interpolate.interp1d(x, y)(np.asarray(line_ints).clip(0))
+
+
+def bh_lut(line_ints, coefs, mu):
+    """Lookup-table correction of tests/Test_Beamhard/beamhard_test.py:26-27."""
+    li = np.asarray(line_ints)
+    return li * np.interp(li / mu, np.linspace(0, 40, 4001), coefs)
+
+
+def bh_sphere_fan_coefs(energies, counts, gammas, src_iso, atten_eff, attens):
+    """beamhard_coefs2's fan branch (beamhard.py:50-78): chord lengths of a
+    centred sphere of radius 20 (intersection_sino.py:105-121 at view 0) for
+    the first 256 of 512 fan angles, polyenergetic path lengths, quadratic fit."""
+    r = 20.0
+    xi = src_iso * np.sin(gammas)
+    f = r ** 2 * (np.cos(gammas) ** 2 + np.sin(gammas) ** 2)
+    pl = ((2. * r ** 2 / f) * np.sqrt((f - xi ** 2).clip(0)))[:256]
+    pp = -1.0 * np.log(np.sum(counts * np.exp(-1.0 * np.outer(pl, attens)), axis=1)
+                       / np.sum(counts)) / atten_eff
+    return np.polyfit(pp, pl, 2)

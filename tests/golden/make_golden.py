@@ -410,6 +410,65 @@ def main():
                          grad_abs=fns["grad_abs"](x), div_abs=fns["div_abs"](zz),
                          pyT=fns["pyT"](AA.copy()))
 
+    # --- beam-hardening pre-correction (processing/beamhard.py) -------------
+    # beamhard.py imports three modules outside the tree at import: the
+    # X-ray attenuation database xcompy (stubbed with a synthetic water curve,
+    # mu(E) = 0.17 + 2500 E^-3 per cm, stated here as synthetic), vir's
+    # intersection_sino under the name `intersection` (its plotting imports
+    # are stubbed when matplotlib is absent), and a projector module
+    # `projection` that the fixtures below do not call.
+    if "matplotlib" not in sys.modules:  # intersection_sino.py:13-14, plotting only
+        mpl = types.ModuleType("matplotlib")
+        mpl.pyplot = types.ModuleType("matplotlib.pyplot")
+        sys.modules["matplotlib"] = mpl
+        sys.modules["matplotlib.pyplot"] = mpl.pyplot
+        tk = types.ModuleType("mpl_toolkits")
+        tk.mplot3d = types.ModuleType("mpl_toolkits.mplot3d")
+        tk.mplot3d.Axes3D = object
+        sys.modules["mpl_toolkits"] = tk
+        sys.modules["mpl_toolkits.mplot3d"] = tk.mplot3d
+    import vir.intersection_sino as inter_mod
+    from vir.core import core_funcs as cf
+
+    def mixatten(material, energies):
+        e = np.asarray(energies, np.float64)
+        return 0.17 + 2500.0 * e ** -3.0
+
+    sys.modules["intersection"] = inter_mod
+    sys.modules["projection"] = types.ModuleType("projection")
+    xc = types.ModuleType("xcompy")
+    xc.mixatten = mixatten
+    sys.modules["xcompy"] = xc
+    sys.path.insert(0, os.path.join(ref, "processing"))
+    import beamhard as bhm
+    energies = np.arange(20.0, 121.0)
+    counts = np.exp(-0.5 * ((energies - 62.0) / 18.0) ** 2) * 1e6
+    atten_eff = float(mixatten("H2O", [np.average(energies, weights=counts)])[0])
+    rng = np.random.default_rng(26)
+    li = (rng.random((6, 50)) * 8.0).astype(np.float32)
+    li[0, :5] = [0.0, 1e-7, 3.5, 7.999, 0.25]
+    coefs = np.polyfit(np.linspace(0, 10, 50), np.linspace(0, 10, 50) ** 1.1, 2)
+    mu = 0.2
+    out["bh_poly"] = dict(line_ints=li, coefs=coefs, mu=mu,
+                          cor_f64coefs=bhm.beamhard_cor(li, coefs, mu),
+                          cor_pycoefs=bhm.beamhard_cor(li, [float(c) for c in coefs], mu),
+                          cor_f64mu=bhm.beamhard_cor(li, coefs, np.float64(mu)),
+                          cor_f64in=bhm.beamhard_cor(li.astype(np.float64), coefs, mu))
+    li_t = (rng.random((5, 40)) * 6.5 - 0.5).astype(np.float32)  # some negatives: clipped
+    out["bh_table"] = dict(line_ints=li_t, energies=energies, counts=counts, atten_eff=atten_eff,
+                           attens=mixatten("H2O", energies),
+                           cor=bhm.beamhard_cor_table(li_t, energies, counts, None, atten_eff))
+    g_fan = cf.Geom(nViews=16, fan_angle=0.6, src_iso=60.0, src_det=107.255)
+    out["bh_coefs2_fan"] = dict(energies=energies, counts=counts, atten_eff=atten_eff,
+                                fan_angle=0.6, src_iso=60.0, src_det=107.255,
+                                coefs=bhm.beamhard_coefs2(energies, counts, g_fan, atten_eff))
+    lut = function_from_source(os.path.join(ref, "tests", "Test_Beamhard", "beamhard_test.py"),
+                               ["beamhard_cor2"])["beamhard_cor2"]
+    coefs_tb = 1.0 + 0.05 * np.sin(np.linspace(0, 3, 4001))
+    li_l = (rng.random((4, 30)) * 9.0).astype(np.float32)
+    li_l[0, :4] = [0.0, 8.0, 8.2, 8.0000005]   # on, at and past the table's end (mu 0.2: 40)
+    out["bh_lut"] = dict(line_ints=li_l, coefs=coefs_tb, mu=0.2, cor=lut(li_l, coefs_tb, 0.2))
+
     path = os.path.join(HERE, "golden.npz")
     flat = {}
     for k, d in out.items():

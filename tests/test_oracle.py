@@ -265,3 +265,75 @@ def test_tv_ops(golden, orc):
     rng = np.random.default_rng(0)
     x, z = rng.normal(size=(9, 7)), rng.normal(size=(2, 9, 7))
     assert abs((orc.tv_grad(x) * z).sum() + (x * orc.tv_div(z)).sum()) < 1e-10
+
+
+def _water(e):
+    """The synthetic water attenuation curve of the beam-hardening fixtures."""
+    return 0.17 + 2500.0 * np.asarray(e, np.float64) ** -3.0
+
+
+def test_beamhard_oracle(golden, orc):
+    p = golden["bh_poly"]
+    li, coefs, mu = p["line_ints"], p["coefs"], float(p["mu"])
+    assert np.array_equal(orc.bh_poly(li, coefs, mu), p["cor_f64coefs"])
+    assert np.array_equal(orc.bh_poly(li, [float(c) for c in coefs], mu), p["cor_pycoefs"])
+    assert np.array_equal(orc.bh_poly(li, coefs, np.float64(mu)), p["cor_f64mu"])
+    t = golden["bh_table"]
+    assert np.array_equal(orc.bh_table(t["line_ints"], t["energies"], t["counts"],
+                                       float(t["atten_eff"]), t["attens"]), t["cor"])
+    lut = golden["bh_lut"]
+    assert np.array_equal(orc.bh_lut(lut["line_ints"], lut["coefs"], float(lut["mu"])), lut["cor"])
+    c = golden["bh_coefs2_fan"]
+    n = 512
+    gam = np.linspace(-n + 1, n - 1, n) * (float(c["fan_angle"]) / n) / 2.0
+    co = orc.bh_sphere_fan_coefs(c["energies"], c["counts"], gam, float(c["src_iso"]),
+                                 float(c["atten_eff"]), _water(c["energies"]))
+    assert np.allclose(co, c["coefs"], rtol=1e-12, atol=0)
+
+
+def test_beamhard_host_logic(golden):
+    """The host side of vir_gb300.beamhard (no device): numpy's step types for
+    the polynomial, the interp1d table, the sphere fits and the water tub."""
+    from types import SimpleNamespace
+    from vir_gb300 import beamhard as bh
+    assert bh._poly_types(np.float32, np.array([0.1, 0.2, 0.3]), 0.2) == (1, np.float64)
+    assert bh._poly_types(np.float32, [0.1, 0.2, 0.3], 0.2) == (31, np.float32)
+    assert bh._poly_types(np.float32, np.array([0.1, 0.2, 0.3]), np.float64(0.2))[0] == 0
+    assert bh._poly_types(np.float64, [0.1, 0.2, 0.3], 0.2) == (0, np.float64)
+    c = golden["bh_coefs2_fan"]
+    n = 512
+    g = SimpleNamespace(geom="Fan beam", src_iso=float(c["src_iso"]),
+                        gammas=lambda k: np.linspace(-k + 1, k - 1, k) * (float(c["fan_angle"]) / k) / 2.0)
+    co = bh.beamhard_coefs2(c["energies"], c["counts"], g, float(c["atten_eff"]),
+                            mixatten=lambda m, e: _water(e))
+    assert np.allclose(co, c["coefs"], rtol=1e-12, atol=0)
+    with pytest.raises(ValueError):
+        bh.beamhard_coefs2(c["energies"], c["counts"], g, float(c["atten_eff"]))
+    t = golden["bh_table"]
+    x, y = bh.spectrum_table(t["energies"], t["counts"], float(t["atten_eff"]), t["attens"])
+    assert np.all(np.diff(x) > 0) and x[0] == 0.0 and y[-1] == 80 * float(t["atten_eff"])
+    tub = bh.water_tub_phantom(64, 1.0, 20)
+    ii, jj = np.indices((64, 64))
+    assert np.array_equal(tub, (ii - 32) ** 2 + (jj - 32) ** 2 < 400)
+
+
+def test_beamhard_float32_search_keys():
+    """The lookup kernel searches float32 keys (x rounded toward -inf for
+    searchsorted 'left', toward +inf for 'right'); for float32 samples that
+    finds numpy's float64 index exactly, on and beside every key."""
+    import torch
+    from vir_gb300 import beamhard as bh
+    rng = np.random.default_rng(0)
+    x = np.sort(rng.random(2000) * 10)
+    x[:5] = [0, 0.5, 1.0, 2.0, 3.0]
+    y = rng.random(2000)
+    xf = x.astype(np.float32)
+    v = np.concatenate([(rng.random(100000) * 10).astype(np.float32), xf,
+                        np.nextafter(xf, np.float32(np.inf)), np.nextafter(xf, np.float32(-np.inf))])
+    for up, side in ((False, "left"), (True, "right")):
+        seg, keys = bh._interp_table(x, y, torch.device("cpu"), True, up)
+        k = keys.numpy()
+        assert k.dtype == np.float32
+        assert np.array_equal(np.searchsorted(k, v, side), np.searchsorted(x, v.astype(np.float64), side))
+        s = seg.numpy()
+        assert np.array_equal(s[:-1, 2], (y[1:] - y[:-1]) / (x[1:] - x[:-1])) and s[-1, 2] == 0
