@@ -224,6 +224,11 @@ EXTRA = {
           "C4 detector): water polynomial with np.polyfit coefficients (float64 result) and with "
           "Python-float coefficients (float32 result), 1000-entry spectrum table (interp1d), "
           "4001-entry lookup table (np.interp); each result in numpy's dtype, bit for bit",
+    "helical": "helical rebinning front-end: 1440 helical views (2 rotations, 64 rows x 1024 "
+               "columns, 16 rows per rotation of table travel) rebinned to 720 axial angles x "
+               "128 slices (sino_hel2axl), the axial sinogram resampled back to the helical views "
+               "(sino_axl2hel), and a 128^3 phantom projected over 180 helical views "
+               "(forward_project_phantom)",
     "square": "translational square geometry DD FP + BP (dd_fp_square / dd_bp_square) at the "
               "reference's SIRT-script size (64^3, 96x10 sources, 129x64 cells) and at its "
               "nice.py size (250^3, 650x10 sources, 961x121 cells)",
@@ -426,6 +431,74 @@ def run_workload(args):
             "kind": "port", "cores": 1,
             "sample": "the oracle's numpy/scipy restatement of beamhard.py:16-47 and "
                       "beamhard_test.py:26-27 on 8 of 720 views, scaled to the full sinogram"}})
+        print(json.dumps(line), flush=True)
+        return 0
+    elif wl == "helical":
+        from vir_gb300 import _core
+        from vir_gb300 import trajectory as tr
+        from vir_gb300._lib import call
+        g = torch.Generator(device=dev).manual_seed(6)
+        nvh, nr, nc = 1440, 64, 1024
+        G = tr.Geom(nViews=nvh, coverage=4 * np.pi, zTran=16.0)
+        sinoH = torch.rand((nvh, nr, nc), device=dev, generator=g)
+        angs = np.linspace(0, 2 * np.pi, 720, endpoint=False)
+        Z = np.linspace(-15.5, 15.5, 128)
+        pp, wp, pn, wn = tr._tables(G, [Z] * angs.size, angs, nr)
+        shape = (angs.size, Z.size, nc)
+        out = {}
+        ms = _event_ms(lambda: (tr._gather(sinoH, pp, wp, shape), tr._gather(sinoH, pn, wn, shape)),
+                       reps, stream)
+        n_out = 2 * angs.size * Z.size * nc
+        t0 = time.perf_counter()
+        tr.sino_hel2axl(sinoH, G, angs, Z)
+        torch.cuda.synchronize()
+        call_ms = (time.perf_counter() - t0) * 1e3
+        gbs = 12.0 * n_out / (ms / 1e3) / 1e9  # two float32 rows read, one written per sample
+        hs = sinoH[:, :, :64].cpu().numpy()   # 1/16 of the columns for the CPU path
+        t0 = time.perf_counter()
+        orc_mod().rebin_rows(hs, pp, wp, shape[:2] + (64,))
+        orc_mod().rebin_rows(hs, pn, wn, shape[:2] + (64,))
+        cpu_ms = (time.perf_counter() - t0) * 1e3 * nc / 64
+        out["hel2axl"] = {"kernel_ms": ms, "call_ms": call_ms, "gsamples_per_s": n_out / ms / 1e6,
+                          "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s",
+                                       "frac": gbs / peak, "bytes_per_launch": 12.0 * n_out},
+                          "cpu_numpy_ms_full_size": cpu_ms}
+        sinoA = torch.rand((720, 128, nc), device=dev, generator=g)
+        vH = np.linspace(0, 4 * np.pi, nvh, endpoint=False)
+        idx, zz, wrap, _ = tr.axl2hel_index(720, 128, nr, vH, 720, 0.5)  # 32 rows per rotation
+        ti, tz, tw = (torch.from_numpy(np.ascontiguousarray(v)).to(dev) for v in (idx, zz, wrap))
+        res = torch.empty((nvh, nr, nc), device=dev)
+        ms = _event_ms(lambda: call("vg_axl2hel", _core.ptr(sinoA), 720, 128, nc, _core.ptr(ti),
+                                    _core.ptr(tz), _core.ptr(tw), nvh, nr, _core.ptr(res),
+                                    _core.stream(dev)), reps, stream)
+        n_h = nvh * nr * nc
+        gbs = 20.0 * n_h / (ms / 1e3) / 1e9  # four float32 neighbours read, one written
+        sa = sinoA[:, :, :64].cpu().numpy()
+        t0 = time.perf_counter()
+        orc_mod().axl2hel(sa, idx[:90], zz[:90], wrap[:90], nr)
+        cpu_ms = (time.perf_counter() - t0) * 1e3 * (nc / 64) * (nvh / 90)
+        out["axl2hel"] = {"kernel_ms": ms, "gsamples_per_s": n_h / ms / 1e6,
+                          "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s",
+                                       "frac": gbs / peak, "bytes_per_launch": 20.0 * n_h},
+                          "cpu_scipy_ms_full_size": cpu_ms}
+        ph = torch.rand((128, 128, 128), device=dev, generator=g)
+        vws = np.linspace(0, 2 * np.pi, 180, endpoint=False)
+        zs = np.linspace(-8, 8, 180)
+        ms = _event_ms(lambda: tr.forward_project_phantom(ph, vws, None, None, zs), reps, stream)
+        n_s = 180 * 128 ** 3
+        php = ph.cpu().numpy()
+        t0 = time.perf_counter()
+        orc_mod().rotsum_fp(php, tr.view_matrices(php.shape, vws[:2], zs[:2]))
+        cpu_ms = (time.perf_counter() - t0) * 1e3 * 90
+        out["fp_phantom"] = {"kernel_ms": ms, "gsamples_per_s": n_s / ms / 1e6,
+                             "note": "trilinear samples (8 L1/L2 reads each) summed along y; "
+                                     "bound by the gathers, not by HBM",
+                             "cpu_scipy_ms_full_size": cpu_ms}
+        line.update({"cases": out, "cpu_baseline": {
+            "kind": "port", "cores": 1,
+            "sample": "the oracle's numpy / scipy.ndimage restatement of trajectory.py on 1/16 of "
+                      "the columns (hel2axl), 90 of 1440 views x 1/16 of the columns (axl2hel), "
+                      "2 of 180 views (fp_phantom), scaled to the full workload"}})
         print(json.dumps(line), flush=True)
         return 0
     elif wl == "c3":

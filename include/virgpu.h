@@ -431,6 +431,35 @@ int vg_bh_interp(const void *in, int in_f64, void *out, int out_f64, size_t n, c
                  const void *keys, int key_f32, int m, int mode, double mu,
                  unsigned long long *n_outside, void *stream);
 
+/* Helical rebinning front-end (trajectory.py).
+ *   vg_rebin_rows: n_out output rows of n_cols, row o = float32(src[v0, r0, :]
+ *     w0 + src[v1, r1, :] w1) in float64 (the gathers of sino_hel2axl,
+ *     sino_hel2axl180 and sino_hel2hel, trajectory.py:70-240); src is
+ *     (n_views, n_rows, n_cols) float32; pairs (n_out x 4 int32: v0, r0, v1,
+ *     r1) and weights (n_out x 2 float64) are 16-byte aligned device tables
+ *     built from the geometry's interpZ on the host; reverse != 0 writes the
+ *     columns in reverse order; rows with an index out of range are left
+ *     unwritten and counted in *n_bad (device counter, may be NULL).
+ *   vg_axl2hel: sino_axl2hel (trajectory.py:45-67): helical sinogram
+ *     (n_views_h, n_rows_h, n_cols) from the axial (n_angs, n_rows, n_cols),
+ *     view i sampled at fractional axial view view_index[i] and rows
+ *     r + z_shift[i] with scipy map_coordinates(order=1) arithmetic: mode
+ *     'constant' (0 outside [0, n-1]), or 'grid-wrap' on clipped rows and
+ *     columns where wrap[i] != 0 (views past the last axial angle).
+ *   vg_rotsum_fp: forward_project_phantom (trajectory.py:17-42): sino (n_views,
+ *     nz, nx) = sum over y of the (nx, ny, nz) phantom sampled trilinearly
+ *     (cval 0) at M_v (x, y, z, 1), each coordinate rounded to 6 decimals;
+ *     mats holds n_views row-major 3 x 4 float32 matrices (rows x, y, z of the
+ *     view's affine transform). */
+int vg_rebin_rows(const float *src, int n_views, int n_rows, int n_cols, const int *pairs,
+                  const double *weights, int n_out, int reverse, float *dst,
+                  unsigned long long *n_bad, void *stream);
+int vg_axl2hel(const float *sinoA, int n_angs, int n_rows, int n_cols, const double *view_index,
+               const double *z_shift, const int *wrap, int n_views_h, int n_rows_h, float *sinoH,
+               void *stream);
+int vg_rotsum_fp(const float *vol, int nx, int ny, int nz, const float *mats, int n_views,
+                 float *sino, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

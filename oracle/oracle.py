@@ -617,3 +617,49 @@ def bh_sphere_fan_coefs(energies, counts, gammas, src_iso, atten_eff, attens):
     pp = -1.0 * np.log(np.sum(counts * np.exp(-1.0 * np.outer(pl, attens)), axis=1)
                        / np.sum(counts)) / atten_eff
     return np.polyfit(pp, pl, 2)
+
+
+# ---- helical rebinning front-end (trajectory.py) -----------------------------
+
+def rebin_rows(src, pairs, w, shape, reverse=False):
+    """The row gathers of sino_hel2axl / sino_hel2axl180 / sino_hel2hel
+    (trajectory.py:95-103): float32 rows times float64 weights, summed in
+    float64 and stored as float32; pairs (v0, r0, v1, r1) per output row."""
+    a = src[pairs[:, 0], pairs[:, 1], :] * w[:, 0:1]
+    b = src[pairs[:, 2], pairs[:, 3], :] * w[:, 1:2]
+    o = (a + b).astype(np.float32).reshape(shape)
+    return o[..., ::-1] if reverse else o
+
+
+def axl2hel(sinoA, view_index, z_shift, wrap, n_rows_h):
+    """sino_axl2hel's sampling (trajectory.py:56-67) with scipy's
+    map_coordinates, the reference's own call, for precomputed per-view
+    axial indices, z shifts and wrap flags."""
+    from scipy.ndimage import map_coordinates
+    nA, nR, nC = sinoA.shape
+    rows, cols = np.split(np.mgrid[0:n_rows_h, 0:nC], 2, axis=0)
+    views = np.zeros([1, n_rows_h, nC])
+    out = np.zeros([len(view_index), n_rows_h, nC], np.float32)
+    for i, (a, z, wr) in enumerate(zip(view_index, z_shift, wrap)):
+        views[:] = a
+        if not wr:
+            out[i] = map_coordinates(sinoA, (views, rows + z, cols), order=1, mode="constant", cval=0.0)
+        else:
+            out[i] = map_coordinates(sinoA, (views, (rows + z).clip(0, nR - 1), cols.clip(0, nC - 1)),
+                                     order=1, mode="grid-wrap")
+    return out
+
+
+def rotsum_fp(phantom, mats):
+    """forward_project_phantom's projection (trajectory.py:27-40) for given
+    per-view 3 x 4 affine matrices: the phantom sampled by map_coordinates
+    (order 1, cval 0) at each voxel's transformed coordinates (rounded to 6
+    decimals) and summed along y."""
+    from scipy.ndimage import map_coordinates
+    nX, nY, nZ = phantom.shape
+    g = np.mgrid[:nX, :nY, :nZ].astype(np.float32)
+    out = np.zeros((len(mats), nZ, nX), np.float32)
+    for i, m in enumerate(mats):
+        c = np.round(np.einsum("rk,kxyz->rxyz", m[:, :3], g) + m[:, 3, None, None, None], 6)
+        out[i] = map_coordinates(phantom, c, order=1, mode="constant", cval=0.0).sum(axis=1).T
+    return out

@@ -469,6 +469,47 @@ def main():
     li_l[0, :4] = [0.0, 8.0, 8.2, 8.0000005]   # on, at and past the table's end (mu 0.2: 40)
     out["bh_lut"] = dict(line_ints=li_l, coefs=coefs_tb, mu=0.2, cor=lut(li_l, coefs_tb, 0.2))
 
+    # --- helical rebinning front-end (trajectory.py, core_funcs.Geom) -------
+    import vir.trajectory as traj
+    rng = np.random.default_rng(27)
+    sinoA = rng.random((24, 10, 12)).astype(np.float32)
+    viewsH = np.linspace(0.0, 4 * np.pi, 50, endpoint=False)
+    viewsH[7] = 2 * np.pi * 23 / 24 + 0.05       # past the last axial angle: grid-wrap branch
+    viewsH[8] = 2 * np.pi * 5 / 24                # exactly on an axial angle
+    out["traj_axl2hel"] = dict(sinoA=sinoA, nRowsH=np.int32(6), viewsH=viewsH, nAngsH=np.int32(24),
+                               pitch=1.0, sinoH=traj.sino_axl2hel(sinoA, 6, viewsH, 24, 1.0))
+    zH = np.linspace(-1.0, 5.5, 50)
+    out["traj_axl2hel_z"] = dict(sinoA=sinoA, nRowsH=np.int32(6), viewsH=viewsH, nAngsH=np.int32(24),
+                                 pitch=1.0, Z=zH,
+                                 sinoH=traj.sino_axl2hel(sinoA, 6, viewsH, 24, 1.0, Z=zH))
+    gH = cf.Geom(nViews=96, coverage=4 * np.pi, zTran=8.0)
+    sinoH = rng.random((96, 6, 10)).astype(np.float32)
+    angsA = np.array([0.0, 0.3, 1.0, np.pi, 5.9])
+    zA = np.linspace(-3.0, 3.0, 7)
+    a1, a2 = traj.sino_hel2axl(sinoH, gH, angsA, zA)
+    f1, f2, b1, b2 = traj.sino_hel2axl180(sinoH, gH, angsA, zA)
+    gI = cf.Geom(nViews=40, coverage=4 * np.pi, angle0=0.1, zTran=6.0)
+    i1, i2 = traj.sino_hel2hel(sinoH, gH, gI, 4)
+    out["traj_hel2axl"] = dict(sinoH=sinoH, nViews=np.int32(96), coverage=4 * np.pi, zTran=8.0,
+                               angsA=angsA, zA=zA, a1=a1, a2=a2, f1=f1, f2=f2, b1=b1, b2=b2,
+                               int_nViews=np.int32(40), int_coverage=4 * np.pi, int_angle0=0.1,
+                               int_zTran=6.0, i1=i1, i2=i2, gH_Z=gH.Z, gH_Views=gH.Views)
+    iz = gH.interpZ(zA, 1.0, 6)
+    out["traj_interpZ"] = dict(zA=zA, angle=1.0, nRows=np.int32(6),
+                               **{f"r{k}": np.asarray(v) for k, v in enumerate(iz)})
+    gS = cf.Geom(nViews=96, coverage=4 * np.pi, zTran=8.0)
+    sub = traj.sino_hel_subset(sinoH, gS, 6, [-1.0, 2.0])
+    out["traj_subset"] = dict(z=np.array([-1.0, 2.0]), nRows=np.int32(6), sub=sub,
+                              Views=gS.Views, Z=gS.Z)
+    ph = rng.random((12, 10, 8)).astype(np.float32)
+    vws = np.array([0.0, 0.4, 1.3, np.pi / 2, 2.9, 4.4])
+    zz = np.array([0.0, 0.25, -1.5, 2.0, 0.7, -0.3])
+    import vir.affine_transforms as aff
+    mats = np.stack([(aff.rotateMat((0, 0, -v), center=np.array(ph.shape) / 2.0 - 0.5, seq='XYZ')
+                      @ aff.transMat((0, 0, -z)))[:3] for v, z in zip(vws, zz)])
+    out["traj_fp_phantom"] = dict(phantom=ph, views=vws, Z=zz, mats=mats,
+                                  sino=traj.forward_project_phantom(ph, vws, None, None, zz))
+
     path = os.path.join(HERE, "golden.npz")
     flat = {}
     for k, d in out.items():

@@ -337,3 +337,60 @@ def test_beamhard_float32_search_keys():
         assert np.array_equal(np.searchsorted(k, v, side), np.searchsorted(x, v.astype(np.float64), side))
         s = seg.numpy()
         assert np.array_equal(s[:-1, 2], (y[1:] - y[:-1]) / (x[1:] - x[:-1])) and s[-1, 2] == 0
+
+
+def _traj_geoms(h):
+    from vir_gb300 import trajectory as tr
+    G = tr.Geom(nViews=int(h["nViews"]), coverage=float(h["coverage"]), zTran=float(h["zTran"]))
+    GI = tr.Geom(nViews=int(h["int_nViews"]), coverage=float(h["int_coverage"]),
+                 angle0=float(h["int_angle0"]), zTran=float(h["int_zTran"]))
+    return G, GI
+
+
+def test_trajectory_host_logic(golden):
+    """vir_gb300.trajectory's host side against the reference: Geom's views,
+    z positions and interpZ, sino_hel_subset, the per-view affine matrices
+    and the axial indices of sino_axl2hel."""
+    from vir_gb300 import trajectory as tr
+    h = golden["traj_hel2axl"]
+    G, _ = _traj_geoms(h)
+    assert np.array_equal(G.Z, h["gH_Z"]) and np.array_equal(G.Views, h["gH_Views"])
+    iz = golden["traj_interpZ"]
+    r = G.interpZ(iz["zA"], float(iz["angle"]), int(iz["nRows"]))
+    assert all(np.array_equal(np.asarray(a), iz[f"r{k}"]) for k, a in enumerate(r))
+    s = golden["traj_subset"]
+    GS, _ = _traj_geoms(h)
+    sub = tr.sino_hel_subset(h["sinoH"], GS, int(s["nRows"]), s["z"])
+    assert np.array_equal(sub, s["sub"]) and np.array_equal(GS.Views, s["Views"])
+    assert np.array_equal(GS.Z, s["Z"])
+    f = golden["traj_fp_phantom"]
+    M = tr.view_matrices(f["phantom"].shape, f["views"], f["Z"])
+    assert np.allclose(M, f["mats"], rtol=1e-6, atol=1e-6)
+
+
+def test_trajectory_oracle(golden, orc):
+    from vir_gb300 import trajectory as tr
+    for case in ("traj_axl2hel", "traj_axl2hel_z"):
+        a = golden[case]
+        nA, nR, _ = a["sinoA"].shape
+        idx, zz, wrap, n = tr.axl2hel_index(nA, nR, int(a["nRowsH"]), a["viewsH"], int(a["nAngsH"]),
+                                            float(a["pitch"]), a.get("Z"))
+        assert n == a["viewsH"].size and wrap.sum() == 3
+        assert np.array_equal(orc.axl2hel(a["sinoA"], idx, zz, wrap, int(a["nRowsH"])), a["sinoH"])
+    h = golden["traj_hel2axl"]
+    G, GI = _traj_geoms(h)
+    src, A, Z = h["sinoH"], h["angsA"], h["zA"]
+    sh = (A.size, Z.size, src.shape[2])
+    pp, wp, pn, wn = tr._tables(G, [Z] * A.size, A, src.shape[1])
+    assert np.array_equal(orc.rebin_rows(src, pp, wp, sh), h["a1"], equal_nan=True)
+    assert np.array_equal(orc.rebin_rows(src, pn, wn, sh), h["a2"], equal_nan=True)
+    bp, bwp, bn, bwn = tr._tables(G, [Z] * A.size, A + np.pi, src.shape[1])
+    assert np.array_equal(orc.rebin_rows(src, bp, bwp, sh, True), h["b1"], equal_nan=True)
+    assert np.array_equal(orc.rebin_rows(src, bn, bwn, sh, True), h["b2"], equal_nan=True)
+    Zs = [tr.censpace(4, c=z) for z in GI.Z]
+    pp, wp, pn, wn = tr._tables(G, Zs, list(GI.Views), src.shape[1])
+    shi = (GI.nViews, 4, src.shape[2])
+    assert np.array_equal(orc.rebin_rows(src, pp, wp, shi), h["i1"], equal_nan=True)
+    assert np.array_equal(orc.rebin_rows(src, pn, wn, shi), h["i2"], equal_nan=True)
+    f = golden["traj_fp_phantom"]
+    assert rel(orc.rotsum_fp(f["phantom"], f["mats"]), f["sino"]) < 1e-6

@@ -56,6 +56,9 @@ _DROP_INS = {
     "projection.proj_mp": {n: "vir_gb300.projection.proj_mp:" + n
                            for n in ("mp_sd_f_proj", "mp_sd_b_proj", "mpc_sd_f_proj",
                                      "mpc_sd_b_proj")},
+    "trajectory": {n: "vir_gb300.trajectory:" + n
+                   for n in ("sino_axl2hel", "sino_hel2axl", "sino_hel2axl180", "sino_hel2hel",
+                             "sino_hel_subset", "forward_project_phantom")},
     "processing.beamhard": {n: "vir_gb300.beamhard:" + n
                             for n in ("beamhard_cor", "beamhard_cor_table", "beamhard_coefs",
                                       "beamhard_coefs2", "water_tub_phantom")},

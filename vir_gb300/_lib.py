@@ -124,6 +124,11 @@ _PROTOS = {
                    c_double, c_int, c_void_p],
     "vg_bh_interp": [c_void_p, c_int, c_void_p, c_int, c_size_t, c_void_p, c_void_p, c_int, c_int,
                      c_int, c_double, c_void_p, c_void_p],
+    "vg_rebin_rows": [c_void_p, c_int, c_int, c_int, c_void_p, c_void_p, c_int, c_int, c_void_p,
+                      c_void_p, c_void_p],
+    "vg_axl2hel": [c_void_p, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_int, c_int,
+                   c_void_p, c_void_p],
+    "vg_rotsum_fp": [c_void_p, c_int, c_int, c_int, c_void_p, c_int, c_void_p, c_void_p],
 }
 
 
