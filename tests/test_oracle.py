@@ -394,3 +394,22 @@ def test_trajectory_oracle(golden, orc):
     assert np.array_equal(orc.rebin_rows(src, pn, wn, shi), h["i2"], equal_nan=True)
     f = golden["traj_fp_phantom"]
     assert rel(orc.rotsum_fp(f["phantom"], f["mats"]), f["sino"]) < 1e-6
+
+
+def test_trajectory_interpZ_batch():
+    """The all-angles evaluation of Geom.interpZ that builds the rebinning
+    tables equals one interpZ call per angle, exactly (views on, between
+    and past the sampled angles; integer and fractional rotation counts)."""
+    from vir_gb300 import trajectory as tr
+    rng = np.random.default_rng(3)
+    for nV, cov, zt, a0, nR, nz in [(96, 4 * np.pi, 8.0, 0.0, 6, 7), (250, 2.7 * np.pi, 5.0, 0.3, 9, 11),
+                                    (64, 2 * np.pi, 0.0, 0.0, 4, 5), (200, 6 * np.pi, 20., 0.1, 12, 30)]:
+        G = tr.Geom(nViews=nV, coverage=cov, zTran=zt, angle0=a0)
+        Z = np.linspace(-zt / 2 if zt else -2, zt / 2 if zt else 2, nz)
+        angs = np.concatenate([np.linspace(0, 2 * np.pi, 30, endpoint=False), G.Views[:5],
+                               G.Views[:5] + np.pi, rng.random(10) * 7])
+        bat = tr._interpZ_batch(G, Z, angs, nR)
+        for i, a in enumerate(angs):
+            ref = G.interpZ(Z, a, nR)
+            for k in range(8):
+                assert np.array_equal(np.asarray(ref[k]), bat[k][i], equal_nan=True), (nV, i, k)

@@ -148,6 +148,57 @@ class Geom:
                 *closest(vn, dVn, lo_n, hi_n, dlo_n, dhi_n))
 
 
+def _interpZ_batch(geom, intZ, angles, nRows):
+    """Geom.interpZ for many angles at once, stacked (angles, slices, 2): the
+    same comparisons and arithmetic as one call per angle, broadcast over the
+    angles (searchsorted 'left' on a sorted row set is its count of entries
+    below the slice; an angle whose last rotation repeats the one before
+    excludes it, as interpZ drops it)."""
+    intZ = np.array(intZ, dtype=float)
+    ang = np.asarray(angles, dtype=float) % (2.0 * np.pi)
+    K = int(np.ceil(geom.nRotations)) + 1
+    A = np.arange(np.ceil(geom.nRotations) + 1)[None, :] * 2.0 * np.pi + ang[:, None]
+    V, nV = geom.Views, geom.nViews
+    vp = np.searchsorted(V, A, side='left')
+    vp = np.where(np.isclose(V[vp - 1], A), vp - 1, vp) % nV
+    vn = np.where(np.isclose(V[vp], A), vp, vp - 1) % nV
+    drop = (vn[:, -1] == vn[:, -2]) & (vp[:, -1] == vp[:, -2]) if K > 1 else np.zeros(len(ang), bool)
+    rows = censpace(nRows)
+    nz = intZ.size
+
+    def dview(v, wrap):
+        d = V[v] - A
+        if wrap:
+            d = d % (2 * np.pi)
+        d = np.where(np.isclose(d, 0.0), 0.0, d)
+        d = np.where(np.isclose(d, 2 * np.pi), 0.0, d)
+        return np.broadcast_to(d[:, :, None], d.shape + (nz,))
+
+    def side(v, dV):
+        zs = geom.Z[v][..., None] + rows                                     # (na, K, nRows)
+        up = (zs[:, :, None, :] < intZ[None, None, :, None]).sum(-1)           # (na, K, nz)
+        upc = up.clip(0, nRows - 1)
+        dn = np.where(np.isclose(np.take_along_axis(zs, upc, 2), intZ), up, up - 1)
+        hi, lo = upc, dn.clip(0, nRows - 1)
+        dlo = np.take_along_axis(zs, lo, 2) - intZ
+        dhi = np.take_along_axis(zs, hi, 2) - intZ
+        dlo = np.where(dlo <= 0, dlo, -np.inf)
+        dhi = np.where(dhi >= 0, dhi, np.inf)
+        out = []
+        for d, r in ((dlo, lo), (dhi, hi)):
+            dist = np.sqrt(d ** 2 + (dV / geom.dView) ** 2)
+            dist[drop, -1, :] = np.inf
+            k = dist.argmin(axis=1)[:, None, :]                              # (na, 1, nz)
+            out.append((np.take_along_axis(np.broadcast_to(v[:, :, None], dist.shape), k, 1)[:, 0],
+                        np.take_along_axis(dV, k, 1)[:, 0], np.take_along_axis(r, k, 1)[:, 0],
+                        np.take_along_axis(d, k, 1)[:, 0]))
+        (va, dva, ra, da), (vb, dvb, rb, db) = out
+        return (np.stack([va, vb], -1), np.stack([dva, dvb], -1), np.stack([ra, rb], -1),
+                np.stack([da, db], -1))
+
+    return side(vp, dview(vp, True)) + side(vn, dview(vn, False))
+
+
 def _pair_weights(idxV, idxR, dR):
     """Rows and weights of one interpolated slice set (trajectory.py:84-93)."""
     wR = dR[:, 1] - dR[:, 0]
@@ -160,7 +211,14 @@ def _pair_weights(idxV, idxR, dR):
 
 def _tables(geom, Zs, angs, nRows):
     """(pairs, weights) of the p and n interpolations for every (angle, z)
-    row, stacked angle-major."""
+    row, stacked angle-major.  This package's Geom evaluates all angles of
+    one slice set at once; other geometry objects are asked per angle."""
+    if isinstance(geom, Geom) and len(Zs) and all(np.array_equal(Zs[0], z) for z in Zs):
+        vp, _, rp, drp, vn, _, rn, drn = _interpZ_batch(geom, Zs[0], angs, nRows)
+        flat = lambda a: a.reshape(-1, 2)
+        a, b = _pair_weights(flat(vp), flat(rp), flat(drp))
+        c, d = _pair_weights(flat(vn), flat(rn), flat(drn))
+        return a, b, c, d
     pp, wp, pn, wn = [], [], [], []
     for Z, ang in zip(Zs, angs):
         vp, _, rp, drp, vn, _, rn, drn = geom.interpZ(Z, ang, nRows)
