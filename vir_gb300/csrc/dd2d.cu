@@ -136,7 +136,12 @@ __device__ __forceinline__ float det_edge(const vg_dd2d_geom &g, int j) {
 // Tile variants: WARPS (lines in flight per block) x MAXB (bins per lane,
 // strided by 32; a block owns 32 MAXB bins of one view).  vg_dd2d_geom's
 // `variant` selects one (1..FP_NVARIANTS), 0 picks by size (fp_variant_for).
-constexpr int FP_SEG = 16;  // pixels per lane in the line scan
+// Pixels per lane in the line scan: 8 keeps the 8-warp tiles at 80 registers,
+// three blocks per SM (16 needs 128 registers, two blocks, and ran 2 % slower).
+#ifndef VG_FP_SEG
+#define VG_FP_SEG 8
+#endif
+constexpr int FP_SEG = VG_FP_SEG;
 struct FpVariant { int warps, maxb; };
 constexpr FpVariant FP_VARIANTS[] = {{8, 6}, {8, 12}, {8, 24}, {4, 24}, {4, 48}, {2, 48}};
 constexpr int FP_NVARIANTS = sizeof(FP_VARIANTS) / sizeof(FP_VARIANTS[0]);
@@ -153,10 +158,10 @@ __host__ __device__ inline int fp_line_entries(int nd) { return pad_idx(nd + 1) 
 // where inv_w == 0.
 template <bool FAN, int FP_WARPS, int FP_MAXB, bool GUARD>
 #ifndef VG_FP_MINB8
-#define VG_FP_MINB8 2
+#define VG_FP_MINB8 3
 #endif
 // (the guarded variants of the 24-bin tiles give up occupancy rather than spill)
-__global__ void __launch_bounds__(FP_WARPS * 32, ((FP_MAXB > 24 || (GUARD && FP_MAXB == 24)) ? 1 : (FP_WARPS >= 8 ? VG_FP_MINB8 : 16 / FP_WARPS)))
+__global__ void __launch_bounds__(FP_WARPS * 32, ((FP_MAXB > 24 || (GUARD && FP_MAXB == 24)) ? 1 : (FP_WARPS >= 8 ? (FP_MAXB == 24 ? VG_FP_MINB8 : 2) : 16 / FP_WARPS)))
 dd2d_fp_kernel(vg_dd2d_geom g, const float *__restrict__ img, const float *__restrict__ imgT,
                const double *__restrict__ trig, float *__restrict__ out, int mode,
                const float *__restrict__ y, const float *__restrict__ inv_w) {
@@ -206,23 +211,24 @@ dd2d_fp_kernel(vg_dd2d_geom g, const float *__restrict__ img, const float *__res
 #pragma unroll
     for (int i = 0; i < FP_MAXB; ++i) acc[i] = 0.f;
 
-    for (int io = warp; io < no; io += FP_WARPS) {
+    // Stages line io into buffer Eb: (G, V) per pixel, the sentinel and the
+    // closing edge; returns the line's inverse-map coefficients (la, lb) and,
+    // for the guard, its first and last projected edges (Pf, Pl).
+    auto stage = [&](int io, float2 *Eb, float &la, float &lb, float &Pf, float &Pl) {
         const Line Lg = line_geo<FAN>(g, v, centre_coord(g.d_pix, io, no));
-        const float la = FAN ? g.DSO - Lg.co : 1.f;       // inverse map numerator U la - lb
-        const float lb = FAN ? g.DSD * Lg.cp : Lg.cp;
-        // the line's first and last projected edges in sweep order (guard only)
-        float Pf = 0.f, Pl = 0.f;
+        la = FAN ? g.DSO - Lg.co : 1.f;       // inverse map numerator U la - lb
+        lb = FAN ? g.DSD * Lg.cp : Lg.cp;
+        Pf = 0.f;
+        Pl = 0.f;
         if (guard) {
             Pf = proj<FAN>(g, v, Lg.cp, Lg.co, edge_coord(g.d_pix, rev ? nd : 0, nd));
             Pl = proj<FAN>(g, v, Lg.cp, Lg.co, edge_coord(g.d_pix, rev ? 0 : nd, nd));
         }
         const float *row = base + (size_t)io * nd;
-        __syncwarp();  // previous line's reads are done
-        // stage (P, S, V) of the line: lanes own FP_SEG consecutive pixels
-        // (edge coordinate b0 + i db along a lane's segment)
+        // lanes own FP_SEG consecutive pixels (edge coordinate b0 + i db along
+        // a lane's segment); along the segment the projection's numerator and
+        // denominator are affine in the edge number i: P_i = (n0 + i dn) / (d0 + i dd)
         const float db = rev ? -g.d_pix : g.d_pix;
-        // along the segment the projection's numerator and denominator are
-        // affine in the edge number i: P_i = (n0 + i dn) / (d0 + i dd)
         const float dn = (FAN ? g.DSD : 1.f) * v.pd * db;
         const float dd = -v.od * db;
         float carry = 0.f;
@@ -241,7 +247,7 @@ dd2d_fp_kernel(vg_dd2d_geom g, const float *__restrict__ img, const float *__res
                 Pv[i] = FAN ? num / fmaf((float)i, dd, d0) : num;
 #endif
             }
-            // pixels m0 .. m0 + FP_SEG - 1 (sweep order): four 16-byte loads when
+            // pixels m0 .. m0 + FP_SEG - 1 (sweep order): 16-byte loads when
             // the segment is whole and aligned, else element by element
             float tot = 0.f;
             if (vec_rows && m0 + FP_SEG <= nd) {
@@ -274,37 +280,49 @@ dd2d_fp_kernel(vg_dd2d_geom g, const float *__restrict__ img, const float *__res
             const int lim = nd - m0;  // pixel entries m0 + i with i < lim exist
 #pragma unroll
             for (int i = 0; i < FP_SEG; ++i) {
-                if (i < lim) E[pad_idx(m0 + i + 1)] = make_float2(fmaf(-q[i], Pv[i], run), q[i]);
+                if (i < lim) Eb[pad_idx(m0 + i + 1)] = make_float2(fmaf(-q[i], Pv[i], run), q[i]);
                 run = fmaf(q[i], Pv[i + 1] - Pv[i], run);
             }
         }
         // the sentinel before the first edge and the closing edge nd (line total)
         if (lane == 0) {
-            E[0] = make_float2(0.f, 0.f);
-            E[pad_idx(nd + 1)] = make_float2(carry, 0.f);
+            Eb[0] = make_float2(0.f, 0.f);
+            Eb[pad_idx(nd + 1)] = make_float2(carry, 0.f);
         }
+    };
+
+    // F of a staged line at detector edge (U, C(U))
+    auto F = [&](const float2 *Eb, float la, float lb, float Pf, float Pl, float2 uc) {
+        float sidx = fmaf(fmaf(uc.x, la, -lb), uc.y, half);
+        if (guard) sidx = uc.x <= Pf ? -1.f : (uc.x >= Pl ? (float)nd : sidx);
+        // slot of pixel floor(sidx): sentinel below the line, closing edge
+        // above (the conversion saturates, so the clamp also bounds +-inf)
+        const int k = min(max(__float2int_rd(sidx), -1), nd) + 1;
+        const float2 t = Eb[pad_idx(k)];
+        return fmaf(t.y, uc.x, t.x);
+    };
+
+    // Each warp stages its lines io = warp, warp + FP_WARPS, ... one at a
+    // time and walks the bin edges.  F at the left edge of bin lane + 32 i is
+    // streamed: bin i - 1 is finished as soon as edge i is known.  Its right
+    // edge is lane + 1's left edge, or for lane 31 lane 0's next one -- one
+    // rotation of (lane 0 ? F(edge i) : F(edge i - 1)).
+    const int src = (lane + 1) & 31;
+    for (int io = warp; io < no; io += FP_WARPS) {
+        float la, lb, Pf, Pl;
+        __syncwarp();  // previous line's reads are done
+        stage(io, E, la, lb, Pf, Pl);
         __syncwarp();
-        // F at the left edge of each of this lane's bins; right edges from lane + 1
-        // (lane 31's right edge is lane 0's next left edge)
-        float Fl[FP_MAXB + 1];
+        float f_prev = 0.f;
 #pragma unroll
         for (int i = 0; i <= FP_MAXB; ++i) {
             const float2 uc = UC[lane + 32 * i];  // edges past nb repeat the last one
-            float sidx = fmaf(fmaf(uc.x, la, -lb), uc.y, half);
-            if (guard) sidx = uc.x <= Pf ? -1.f : (uc.x >= Pl ? (float)nd : sidx);
-            // slot of pixel floor(sidx): sentinel below the line, closing edge
-            // above (the conversion saturates, so the clamp also bounds +-inf)
-            const int k = min(max(__float2int_rd(sidx), -1), nd) + 1;
-            const float2 t = E[pad_idx(k)];
-            Fl[i] = fmaf(t.y, uc.x, t.x);
-        }
-        // right edge of bin lane + 32 i: lane + 1's left edge, or for lane 31
-        // lane 0's next one -- one rotation of (lane 0 ? Fl[i + 1] : Fl[i])
-        const int src = (lane + 1) & 31;
-#pragma unroll
-        for (int i = 0; i < FP_MAXB; ++i) {
-            const float r = __shfl_sync(0xffffffffu, lane == 0 ? Fl[i + 1] : Fl[i], src);
-            acc[i] += r - Fl[i];
+            const float f_new = F(E, la, lb, Pf, Pl, uc);
+            if (i > 0) {
+                const float r = __shfl_sync(0xffffffffu, lane == 0 ? f_new : f_prev, src);
+                acc[i - 1] += r - f_prev;
+            }
+            f_prev = f_new;
         }
     }
 
