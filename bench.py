@@ -224,6 +224,11 @@ EXTRA = {
           "C4 detector): water polynomial with np.polyfit coefficients (float64 result) and with "
           "Python-float coefficients (float32 result), 1000-entry spectrum table (interp1d), "
           "4001-entry lookup table (np.interp); each result in numpy's dtype, bit for bit",
+    "rows": "projector rows without a workload of their own, at the C2 fan geometry (512^2, "
+            "720 views, 768 bins of 1.2 mm, DSO 500, DSD 1000, 0.9 mm pixels), the C1 parallel "
+            "geometry (256^2, 180 views, 367 bins) or the C5 cone geometry (256^3, 360 views, "
+            "512x384): separable footprint (fan, parallel rectangle), ray-driven AW and Joseph, "
+            "pixel-driven, Siddon ray lists (siddons + list FP/BP) and 10 TV-PDHG iterations",
     "helical": "helical rebinning front-end: 1440 helical views (2 rotations, 64 rows x 1024 "
                "columns, 16 rows per rotation of table travel) rebinned to 720 axial angles x "
                "128 slices (sino_hel2axl), the axial sinogram resampled back to the helical views "
@@ -431,6 +436,117 @@ def run_workload(args):
             "kind": "port", "cores": 1,
             "sample": "the oracle's numpy/scipy restatement of beamhard.py:16-47 and "
                       "beamhard_test.py:26-27 on 8 of 720 views, scaled to the full sinogram"}})
+        print(json.dumps(line), flush=True)
+        return 0
+    elif wl == "rows":
+        from vir_gb300 import phantoms as ph
+        from vir_gb300 import tv
+        from vir_gb300.projection import proj
+        from vir_gb300.sys_mat import fp_2d_par as f2, pd as pdm, rd, siddon, sp
+        orc = orc_mod()
+        out = {}
+
+        def case(name, fp, bp, units, cpu_fp, cpu_bp, cpu_scale, sample):
+            t_fp, t_bp = _event_ms(fp, reps, stream), _event_ms(bp, reps, stream)
+            t0 = time.perf_counter()
+            cpu_fp()
+            t1 = time.perf_counter()
+            cpu_bp()
+            t2 = time.perf_counter()
+            out[name] = {"kernel_ms": {"fp": t_fp, "bp": t_bp},
+                         "fwd_back_gups": 2 * units / ((t_fp + t_bp) / 1e3) / 1e9,
+                         "roofline_fp": _roof(units, t_fp, peak), "roofline_bp": _roof(units, t_bp, peak),
+                         "cpu_port_ms": {"fp": (t1 - t0) * 1e3 * cpu_scale,
+                                         "bp": (t2 - t1) * 1e3 * cpu_scale,
+                                         "cores": orc.num_threads(), "sample": sample}}
+
+        # C2 fan geometry
+        img, _ = ph.ellipse_phantom(512, 10, seed=2026, d_pix=0.9)
+        x2 = torch.from_numpy(img).to(dev)
+        a2 = np.linspace(0, 2 * np.pi, 720, endpoint=False)
+        geo = (500.0, 1000.0)
+        y2 = torch.rand((720, 768), device=dev)
+        yh = y2.cpu().numpy()
+        s24 = "24 of 720 views, scaled"
+        case("sf_fan", lambda: sp.sf_fp_fan_2d(x2, a2, 768, *geo, du=1.2, d_pix=0.9),
+             lambda: sp.sf_bp_fan_2d(y2, a2, (512, 512), *geo, du=1.2, d_pix=0.9), 720 * 512 * 512,
+             lambda: orc.sf_fp_fan_2d(img, a2[:24], 768, *geo, du=1.2, d_pix=0.9),
+             lambda: orc.sf_bp_fan_2d(yh[:24], a2[:24], (512, 512), *geo, du=1.2, d_pix=0.9), 30, s24)
+        for tag, jos in (("aw_fan", False), ("joseph_fan", True)):
+            case(tag, lambda: rd.aw_fp_fan_2d(x2, a2, 768, *geo, du=1.2, d_pix=0.9, joseph=jos),
+                 lambda: rd.aw_bp_fan_2d(y2, a2, (512, 512), *geo, du=1.2, d_pix=0.9, joseph=jos),
+                 720 * 512 * 512,
+                 lambda: orc.aw_fp_fan_2d(img, a2[:24], 768, *geo, du=1.2, d_pix=0.9, joseph=jos),
+                 lambda: orc.aw_bp_fan_2d(yh[:24], a2[:24], (512, 512), *geo, du=1.2, d_pix=0.9,
+                                          joseph=jos), 30, s24)
+        case("pd_fan", lambda: pdm.pd_fp_fan_2d(x2, a2, 768, *geo, du=1.2, d_pix=0.9),
+             lambda: pdm.pd_bp_fan_2d(y2, a2, (512, 512), *geo, du=1.2, d_pix=0.9), 720 * 512 * 512,
+             lambda: orc.pd_fp_fan_2d(img, a2[:24], 768, *geo, du=1.2, d_pix=0.9),
+             lambda: orc.pd_bp_fan_2d(yh[:24], a2[:24], (512, 512), *geo, du=1.2, d_pix=0.9), 30, s24)
+        # C1 parallel geometry
+        img1, _ = ph.ellipse_phantom(256, 10, seed=2025, d_pix=1.0)
+        x1 = torch.from_numpy(img1).to(dev)
+        a1 = np.linspace(0, np.pi, 180, endpoint=False)
+        y1 = torch.rand((180, 367), device=dev)
+        y1h = y1.cpu().numpy()
+        case("sf_par_rect", lambda: f2.separable_footprint_fp_2d(x1, a1, 367, 1.0, 1.0),
+             lambda: f2.separable_footprint_bp_2d(y1, a1, (256, 256), 1.0, 1.0), 180 * 256 * 256,
+             lambda: orc.separable_footprint_fp_2d(img1, a1, 367, 1.0, 1.0),
+             lambda: orc.separable_footprint_bp_2d(y1h, a1, (256, 256), 1.0, 1.0), 1,
+             "all 180 views")
+        # C1 Siddon ray lists: 66,060 rays through a 256 x 256 x 1 grid
+        dets = np.arange(367) - 183.0
+        src = np.zeros((180, 367, 3))
+        trg = np.zeros((180, 367, 3))
+        for i, v in enumerate(a1):
+            c, s_ = np.cos(v), np.sin(v)
+            R = np.array([[c, s_], [-s_, c]])
+            src[i, :, :2] = np.stack([np.full(367, -36700.0), dets], -1) @ R
+            trg[i, :, :2] = np.stack([np.full(367, 36700.0), dets], -1) @ R
+        t_sd = _event_ms(lambda: siddon.siddons_device(src, trg, (256, 256, 1), 1.0), 1, stream)
+        ind, ln, off, _, _ = siddon.siddons_device(src, trg, (256, 256, 1), 1.0)
+        xv = x1.reshape(-1)
+        yl = torch.rand(off.numel() - 1, device=dev)
+        ih, lh, oh = ind.cpu().numpy(), ln.cpu().numpy(), off.cpu().numpy()
+        case("siddon_lists", lambda: proj.list_fp_device(xv, ind, ln, off),
+             lambda: proj.list_bp_device(yl, ind, ln, off, xv.numel()), ind.numel(),
+             lambda: orc.list_fp(img1, ih, lh, oh),
+             lambda: orc.list_bp(yl.cpu().numpy(), ih, lh, oh, xv.numel()), 1, "the whole list")
+        out["siddon_lists"].update({"entries": int(ind.numel()), "rays": int(off.numel() - 1),
+                                    "siddons_ms": t_sd,
+                                    "units": "list entries (voxel-ray pairs)"})
+        # C5 cone geometry
+        n, na3, nu3, nv3 = 256, 360, 512, 384
+        e3 = ph.random_ellipsoids(20, fov_radius=n / 2, seed=2027)
+        x3 = ph.rasterize3d_device(e3, n, 1.0, device=dev)
+        a3 = np.linspace(0, 2 * np.pi, na3, endpoint=False)
+        kw3 = dict(du=1.6, dv=1.6, su=0.0, sv=0.0, d_pix=1.0)
+        y3 = torch.rand((na3, nu3, nv3), device=dev)
+        x3h, y3h = x3.cpu().numpy(), y3[:2].cpu().numpy()
+        s2 = "2 of 360 views, scaled"
+        for tag, jos in (("aw_cone", False), ("joseph_cone", True)):
+            case(tag, lambda: rd.aw_fp_cone_3d(x3, a3, nu3, nv3, 600.0, 1100.0, joseph=jos, **kw3),
+                 lambda: rd.aw_bp_cone_3d(y3, a3, (n, n, n), 600.0, 1100.0, joseph=jos, **kw3),
+                 na3 * n ** 3,
+                 lambda: orc.aw_fp_cone_3d(x3h, a3[:2], nu3, nv3, 600.0, 1100.0, joseph=jos, **kw3),
+                 lambda: orc.aw_bp_cone_3d(y3h, a3[:2], (n, n, n), 600.0, 1100.0, joseph=jos, **kw3),
+                 180, s2)
+        case("pd_cone", lambda: pdm.pd_fp_cone_3d(x3, a3, nu3, nv3, 600.0, 1100.0, **kw3),
+             lambda: pdm.pd_bp_cone_3d(y3, a3, (n, n, n), 600.0, 1100.0, **kw3), na3 * n ** 3,
+             lambda: orc.pd_fp_cone_3d(x3h, a3[:2], nu3, nv3, 600.0, 1100.0, **kw3),
+             lambda: orc.pd_bp_cone_3d(y3h, a3[:2], (n, n, n), 600.0, 1100.0, **kw3), 180, s2)
+        del x3, y3
+        torch.cuda.empty_cache()
+        # TV-PDHG on the C2 fan DD pair: 10 iterations (each one FP and one BP)
+        from vir_gb300.sys_mat import dd
+        yt = dd.dd_fp_fan_2d(x2, a2, 768, *geo, du=1.2, d_pix=0.9)
+        fpf = lambda z: dd.dd_fp_fan_2d(z, a2, 768, *geo, du=1.2, d_pix=0.9)
+        bpf = lambda z: dd.dd_bp_fan_2d(z, a2, (512, 512), *geo, du=1.2, d_pix=0.9)
+        t_tv = _event_ms(lambda: tv.pdhg(yt, fpf, bpf, (512, 512), lam=0.01, iters=10), 1, stream)
+        out["tv_pdhg"] = {"ms_10_iterations": t_tv, "iter_per_s": 10 / (t_tv / 1e3),
+                          "note": "each iteration: one DD fan FP, one BP and the three fused "
+                                  "elementwise kernels; set-up (A1, At1) inside the timed call"}
+        line.update({"cases": out})
         print(json.dumps(line), flush=True)
         return 0
     elif wl == "helical":
