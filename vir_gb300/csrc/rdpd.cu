@@ -271,33 +271,40 @@ pd_fp_kernel(vg_ray_geom g, const double *__restrict__ trig, const float *__rest
     const int ix = p / g.ny, iy = p - ix * g.ny;
     const float c = (float)__ldg(trig + 2 * ia), s = (float)__ldg(trig + 2 * ia + 1);
     const Foot f = footprint(g, c, s, ix, iy);
-    const int iu0 = max(0, (int)floorf((f.pmin - ubnd(g, 0)) / g.du) - 1);
-    const int iu1 = min(g.nu, (int)floorf((f.pmax - ubnd(g, 0)) / g.du) + 2);
+    // cell widths enter as reciprocals (one division per thread, not per cell);
+    // the cell ranges are the cells holding the interval's ends, widened by
+    // 1e-4 cell against the rounding of the index arithmetic
+    const float inv_du = 1.f / g.du, inv_dv = g.kind == 2 ? 1.f / g.dv : 1.f;
+    const float u0 = ubnd(g, 0);
+    const int iu0 = max(0, (int)floorf(fmaf(f.pmin - u0, inv_du, -1e-4f)));
+    const int iu1 = min(g.nu, (int)floorf(fmaf(f.pmax - u0, inv_du, 1e-4f)) + 1);
     if (g.kind < 2) {
         const float val = __ldg(img + p);
         if (val == 0.f) return;
+        const float k = val * f.scale * inv_du * g.d_pix;
         for (int iu = iu0; iu < iu1; ++iu) {
             const float l = fmaxf(f.pmin, ubnd(g, iu)), r = fminf(f.pmax, ubnd(g, iu + 1));
-            if (r > l) atomicAdd(sino + (size_t)ia * g.nu + iu, val * f.scale * (r - l) / g.du * g.d_pix);
+            if (r > l) atomicAdd(sino + (size_t)ia * g.nu + iu, k * (r - l));
         }
         return;
     }
+    const float kc = f.scale * inv_du * inv_dv * g.d_pix;
     const float *col = img + (size_t)p * g.nz;
     for (int iz = 0; iz < g.nz; ++iz) {
         const float val = __ldg(col + iz);
         if (val == 0.f) continue;
         const float zl = g.d_pix * ((float)iz - g.nz / 2.f), zr = g.d_pix * ((float)(iz + 1) - g.nz / 2.f);
         const float vmin = fminf(f.cm * zl, f.cm * zr), vmax = fmaxf(f.cm * zl, f.cm * zr);
-        const int iv0 = max(0, (int)floorf((vmin - vbnd(g, 0)) / g.dv) - 1);
-        const int iv1 = min(g.nv, (int)floorf((vmax - vbnd(g, 0)) / g.dv) + 2);
+        const int iv0 = max(0, (int)floorf(fmaf(vmin - vbnd(g, 0), inv_dv, -1e-4f)));
+        const int iv1 = min(g.nv, (int)floorf(fmaf(vmax - vbnd(g, 0), inv_dv, 1e-4f)) + 1);
+        const float kv = val * kc;
         for (int iv = iv0; iv < iv1; ++iv) {
             const float vl = fmaxf(vmin, vbnd(g, iv)), vr = fminf(vmax, vbnd(g, iv + 1));
             if (vr <= vl) continue;
+            const float kvv = kv * (vr - vl);
             for (int iu = iu0; iu < iu1; ++iu) {
                 const float ul = fmaxf(f.pmin, ubnd(g, iu)), ur = fminf(f.pmax, ubnd(g, iu + 1));
-                if (ur > ul)
-                    atomicAdd(sino + ((size_t)ia * g.nu + iu) * g.nv + iv,
-                              val * f.scale * ((ur - ul) / g.du * (vr - vl) / g.dv) * g.d_pix);
+                if (ur > ul) atomicAdd(sino + ((size_t)ia * g.nu + iu) * g.nv + iv, kvv * (ur - ul));
             }
         }
     }
@@ -313,31 +320,38 @@ pd_bp_kernel(vg_ray_geom g, const double *__restrict__ trig, const float *__rest
     const int iz = (int)(q % nz);
     const int p = (int)(q / nz), ix = p / g.ny, iy = p - ix * g.ny;
     const float zl = g.d_pix * ((float)iz - g.nz / 2.f), zr = g.d_pix * ((float)(iz + 1) - g.nz / 2.f);
+    // cell widths enter as reciprocals (one division per thread, not per cell);
+    // the cell ranges are the cells holding the interval's ends, widened by
+    // 1e-4 cell against the rounding of the index arithmetic
+    const float inv_du = 1.f / g.du, inv_dv = g.kind == 2 ? 1.f / g.dv : 1.f;
+    const float u0 = ubnd(g, 0), v0 = g.kind == 2 ? vbnd(g, 0) : 0.f;
     Kahan acc;
     for (int ia = 0; ia < g.na; ++ia) {
         const float c = (float)__ldg(trig + 2 * ia), s = (float)__ldg(trig + 2 * ia + 1);
         const Foot f = footprint(g, c, s, ix, iy);
-        const int iu0 = max(0, (int)floorf((f.pmin - ubnd(g, 0)) / g.du) - 1);
-        const int iu1 = min(g.nu, (int)floorf((f.pmax - ubnd(g, 0)) / g.du) + 2);
+        const int iu0 = max(0, (int)floorf(fmaf(f.pmin - u0, inv_du, -1e-4f)));
+        const int iu1 = min(g.nu, (int)floorf(fmaf(f.pmax - u0, inv_du, 1e-4f)) + 1);
         float part = 0.f;
         if (g.kind < 2) {
             const float *row = sino + (size_t)ia * g.nu;
+            const float k = f.scale * inv_du;
             for (int iu = iu0; iu < iu1; ++iu) {
                 const float l = fmaxf(f.pmin, ubnd(g, iu)), r = fminf(f.pmax, ubnd(g, iu + 1));
-                if (r > l) part += __ldg(row + iu) * (r - l) / g.du * f.scale;
+                if (r > l) part = fmaf(__ldg(row + iu), k * (r - l), part);
             }
         } else {
             const float vmin = fminf(f.cm * zl, f.cm * zr), vmax = fmaxf(f.cm * zl, f.cm * zr);
-            const int iv0 = max(0, (int)floorf((vmin - vbnd(g, 0)) / g.dv) - 1);
-            const int iv1 = min(g.nv, (int)floorf((vmax - vbnd(g, 0)) / g.dv) + 2);
+            const int iv0 = max(0, (int)floorf(fmaf(vmin - v0, inv_dv, -1e-4f)));
+            const int iv1 = min(g.nv, (int)floorf(fmaf(vmax - v0, inv_dv, 1e-4f)) + 1);
+            const float k = f.scale * inv_du * inv_dv;
+            const float *col = sino + (size_t)ia * g.nu * g.nv;
             for (int iv = iv0; iv < iv1; ++iv) {
                 const float vl = fmaxf(vmin, vbnd(g, iv)), vr = fminf(vmax, vbnd(g, iv + 1));
                 if (vr <= vl) continue;
+                const float kv = k * (vr - vl);
                 for (int iu = iu0; iu < iu1; ++iu) {
                     const float ul = fmaxf(f.pmin, ubnd(g, iu)), ur = fminf(f.pmax, ubnd(g, iu + 1));
-                    if (ur > ul)
-                        part += __ldg(sino + ((size_t)ia * g.nu + iu) * g.nv + iv) *
-                                ((ur - ul) / g.du * (vr - vl) / g.dv) * f.scale;
+                    if (ur > ul) part = fmaf(__ldg(col + (size_t)iu * g.nv + iv), kv * (ur - ul), part);
                 }
             }
         }
