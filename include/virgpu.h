@@ -404,6 +404,14 @@ int vg_compact_nonzero(const float *v, long long n, const long long *first, int 
 int vg_filter_rows(const float *in, int rows, int nu, const float *taps,
                    const float *row_weight, float *out, void *stream);
 
+/* The same filtering by FFT, as filter_sino computes it (filtration.py:238-309):
+ * each row (times row_weight when given) zero-padded to z (a power of two,
+ * 2 nu <= z <= 32768), rFFT, times spectrum (z/2 + 1 floats: 2H), inverse,
+ * first nu samples; float32 in shared memory, one block per row.  twiddles
+ * holds z complex values (float pairs) W^m = exp(-2 pi i m / z), m < z. */
+int vg_filter_rows_fft(const float *in, int rows, int nu, int z, const float *spectrum,
+                       const float *twiddles, const float *row_weight, float *out, void *stream);
+
 /* Beam-hardening pre-correction of logged sinograms (processing/beamhard.py),
  * elementwise over n values; `in` and `out` are float32 or float64
  * (in_f64 / out_f64), computed as numpy computes the reference's

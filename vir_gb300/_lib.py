@@ -120,6 +120,8 @@ _PROTOS = {
     "vg_count_nonzero": [c_void_p, ctypes.c_longlong, c_void_p, c_void_p],
     "vg_compact_nonzero": [c_void_p, ctypes.c_longlong, c_void_p, c_void_p, c_void_p, c_void_p],
     "vg_filter_rows": [c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p],
+    "vg_filter_rows_fft": [c_void_p, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p,
+                           c_void_p],
     "vg_bh_poly": [c_void_p, c_int, c_void_p, c_int, c_size_t, c_double, c_double, c_double,
                    c_double, c_int, c_void_p],
     "vg_bh_interp": [c_void_p, c_int, c_void_p, c_int, c_size_t, c_void_p, c_void_p, c_int, c_int,

@@ -3,10 +3,11 @@
 ``ramp_filter`` and ``window_filter`` design the half-spectrum filter on the
 host exactly as the reference does (``filtration.py:4-112``, ``:115-235``;
 float64 numpy: they are O(nu) setup).  ``filter_sino`` (``:238-309``)
-filters on the GPU: multiplying the zero-padded rFFT by 2H and cropping to
-nu is, for each output sample, a linear convolution of the row with the
-2*nu - 1 central taps of irfft(2H) -- the kernel ``vg_filter_rows`` applies
-it directly, in FP32 with compensated sums.  numpy in -> numpy out (float64,
+filters on the GPU by the same route as the reference: zero-padded rFFT,
+times 2H, inverse, cropped to nu (``vg_filter_rows_fft``: a shared-memory
+FFT per row, float32, O(z log z)).  Below 256 bins the equivalent linear
+convolution of the row with the 2*nu - 1 central taps of irfft(2H) is applied
+directly (``vg_filter_rows``, compensated sums).  numpy in -> numpy out (float64,
 as the reference returns), torch CUDA tensors stay on the device (float32).
 """
 from __future__ import annotations
@@ -94,15 +95,46 @@ def _device_taps(nu, du, filter_type, cutoff, real_space, dev):
     return t
 
 
+FFT_MIN_NU = 256  # from here on the FFT route is the faster one
+
+
+def _device_spectrum(nu, du, filter_type, cutoff, real_space, dev):
+    """(z, 2H as float32, twiddles W^m, m = 0..z-1, as float32 pairs) on dev."""
+    key = ("fft", int(nu), float(du), str(filter_type), float(cutoff), bool(real_space), str(dev))
+    with _taps_lock:
+        t = _taps.get(key)
+        if t is not None:
+            return t
+    z = int(2 ** np.ceil(np.log2(2 * nu)))
+    H, f = ramp_filter(nu, du=du, cutoff=cutoff, zero_pad=True, half_spectrum=True,
+                       real_space=real_space, return_freq=True)
+    H = window_filter(H, f, du=du, filter_type=filter_type, cutoff=cutoff)
+    m = np.arange(z)
+    tw = np.stack([np.cos(2 * np.pi * m / z), -np.sin(2 * np.pi * m / z)], -1)
+    t = (z, torch.from_numpy((2.0 * H).astype(np.float32)).to(dev),
+         torch.from_numpy(tw.astype(np.float32).reshape(-1)).to(dev))
+    with _taps_lock:
+        _taps[key] = t
+        if len(_taps) > 32:
+            _taps.popitem(last=False)
+    return t
+
+
 def filter_rows_device(x: torch.Tensor, du=1.0, filter_type="ramp", cutoff=0.5, real_space=True,
-                       row_weight=None) -> torch.Tensor:
+                       row_weight=None, method="auto") -> torch.Tensor:
     """Filter a float32 CUDA tensor along its last axis (optionally
-    multiplying every row by ``row_weight`` first)."""
+    multiplying every row by ``row_weight`` first).  method: "fft",
+    "direct", or "auto" (FFT from FFT_MIN_NU bins on)."""
     nu = x.shape[-1]
     rows = x.numel() // nu
-    taps = _device_taps(nu, du, filter_type, cutoff, real_space, x.device)
     out = torch.empty_like(x)
     wp = _core.ptr(row_weight) if row_weight is not None else None
+    if method == "fft" or (method == "auto" and nu >= FFT_MIN_NU):
+        z, spec, tw = _device_spectrum(nu, du, filter_type, cutoff, real_space, x.device)
+        call("vg_filter_rows_fft", _core.ptr(x), rows, nu, z, _core.ptr(spec), _core.ptr(tw), wp,
+             _core.ptr(out), _core.stream(x.device))
+        return out
+    taps = _device_taps(nu, du, filter_type, cutoff, real_space, x.device)
     call("vg_filter_rows", _core.ptr(x), rows, nu, _core.ptr(taps), wp, _core.ptr(out),
          _core.stream(x.device))
     return out
