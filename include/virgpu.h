@@ -258,7 +258,8 @@ typedef struct {
 } vg_dd_square_geom;
 
 /* Device workspace of the backprojection (four FP64 planes of the volume,
- * 8-byte aligned); 0 for an invalid geometry. */
+ * then the running integrals along u of the detector rows of one chunk of
+ * sources; 16-byte aligned); 0 for an invalid geometry. */
 size_t vg_dd_square_workspace_bytes(const vg_dd_square_geom *g);
 
 /* Forward projection, dd_fp_square (dd.py:903-930, dd_fp_translational

@@ -37,6 +37,10 @@
 
 #include "vg_common.cuh"
 
+#ifndef VG_SQ_TAB_MIN
+#define VG_SQ_TAB_MIN 2.f  // cells a voxel spans along u before its slab reads row integrals
+#endif
+
 namespace {
 
 using namespace vg;
@@ -46,6 +50,7 @@ struct SqGeo {
     float DSO, DSD, d_pix, du, dv, inv_du, inv_dv;
     float p_b0, z_b0;          // first voxel boundaries: parallel/orthogonal, z
     float u_b0, v_b0;          // first detector boundaries
+    float u_end;               // last u boundary, u_b0 + nu du
     float sp0, dsp, sz0, dsz;  // source centres sp0 + k dsp, sz0 + k dsz
     float ssp, ssz;
     float scale;               // d_pix^2 / (du dv)
@@ -63,6 +68,7 @@ SqGeo make_geo(const vg_dd_square_geom *g) {
     q.z_b0 = 0.0f - g->d_pix * ((float)g->nz * 0.5f);
     q.u_b0 = (g->su + g->ssrc_p) - g->du * ((float)g->nu * 0.5f);
     q.v_b0 = (g->sv + g->ssrc_z) - g->dv * ((float)g->nv * 0.5f);
+    q.u_end = fmaf((float)g->nu, g->du, q.u_b0);
     // pf.censpace(n, d, s) = arange(n) d + (s - d (n - 1) / 2)
     q.dsp = g->dsrc_p; q.dsz = g->dsrc_z;
     q.sp0 = g->ssrc_p - g->dsrc_p * ((float)(g->nsrc_p - 1) * 0.5f);
@@ -190,10 +196,107 @@ sq_fp_kernel(SqGeo g, const float *__restrict__ vol, float4 *__restrict__ sino,
 constexpr int BPP = 32;  // parallel voxels per block (lanes)
 constexpr int BPZ = 8;   // z slices per block (warps)
 
+// Running integrals along u of every detector row (isp, isz, iv) of a chunk
+// of sources, for the slabs whose voxels span several cells: with U_j the
+// cell boundaries and T_j = du sum_{i<j} c_i (compensated float32 prefix, all
+// four sides),
+// entry j holds x_j = T_j - c_j U_j and y_j = c_j, so the integral of the row
+// from U_0 to u in cell j is G(u) = x_j + y_j u (entry nu: (T_nu, 0)); a
+// voxel's u-overlap sum over the row is then G(pr) - G(pl) with both ends
+// clamped to the detector.  Table: per row nu + 1 entries of two float4 (x, y).
+// compensated float sums (Knuth's TwoSum): (s, c) holds s + c exactly to
+// float32 rounding of the compensation
+struct CSum {
+    float s, c;
+};
+__device__ __forceinline__ CSum csum_add(CSum a, float v) {
+    const float t = __fadd_rn(a.s, v);
+    const float bp = __fsub_rn(t, a.s);
+    const float e = __fadd_rn(__fsub_rn(a.s, __fsub_rn(t, bp)), __fsub_rn(v, bp));
+    return CSum{t, __fadd_rn(a.c, e)};
+}
+__device__ __forceinline__ CSum csum_add(CSum a, CSum b) {
+    CSum r = csum_add(a, b.s);
+    r.c = __fadd_rn(r.c, b.c);
+    return r;
+}
+
+__global__ void __launch_bounds__(256)
+sq_bp_prep(SqGeo g, const float4 *__restrict__ sino, int isp0, float4 *__restrict__ tab) {
+    __shared__ CSum wsum[8][4];
+    const int r = blockIdx.x;  // row within the chunk: (isp - isp0, isz, iv)
+    const float4 *c = sino + ((size_t)isp0 * g.nsz * g.nv + r) * g.nu;
+    float4 *t = tab + 2 * (size_t)r * (g.nu + 1);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int per = (g.nu + 255) / 256, j0 = threadIdx.x * per;
+    CSum loc[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+    for (int i = 0; i < per; ++i)
+        if (j0 + i < g.nu) {
+            const float4 v = __ldg(c + j0 + i);
+            loc[0] = csum_add(loc[0], v.x); loc[1] = csum_add(loc[1], v.y);
+            loc[2] = csum_add(loc[2], v.z); loc[3] = csum_add(loc[3], v.w);
+        }
+    CSum inc[4] = {loc[0], loc[1], loc[2], loc[3]};
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const CSum a{__shfl_up_sync(0xffffffffu, inc[q].s, o), __shfl_up_sync(0xffffffffu, inc[q].c, o)};
+            if (lane >= o) inc[q] = csum_add(inc[q], a);
+        }
+    }
+    if (lane == 31)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) wsum[warp][q] = inc[q];
+    __syncthreads();
+    // exclusive prefix of this thread: earlier warps, earlier lanes of this warp
+    CSum run[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        run[q] = CSum{0.f, 0.f};
+        for (int w = 0; w < warp; ++w) run[q] = csum_add(run[q], wsum[w][q]);
+        const CSum before{__shfl_up_sync(0xffffffffu, inc[q].s, 1), __shfl_up_sync(0xffffffffu, inc[q].c, 1)};
+        if (lane > 0) run[q] = csum_add(run[q], before);
+    }
+    const float du = g.du;
+    for (int i = 0; i < per; ++i) {
+        const int j = j0 + i;
+        if (j < g.nu) {
+            const float4 v = __ldg(c + j);
+            const float U = fmaf((float)j, g.du, g.u_b0);
+            // x_j = T_j - c_j U_j, T_j = du (s + c)
+            t[2 * j] = make_float4(fmaf(run[0].s, du, fmaf(-v.x, U, run[0].c * du)),
+                                   fmaf(run[1].s, du, fmaf(-v.y, U, run[1].c * du)),
+                                   fmaf(run[2].s, du, fmaf(-v.z, U, run[2].c * du)),
+                                   fmaf(run[3].s, du, fmaf(-v.w, U, run[3].c * du)));
+            t[2 * j + 1] = v;
+            run[0] = csum_add(run[0], v.x); run[1] = csum_add(run[1], v.y);
+            run[2] = csum_add(run[2], v.z); run[3] = csum_add(run[3], v.w);
+        }
+    }
+    if (threadIdx.x == 255) {
+        t[2 * g.nu] = make_float4(fmaf(run[0].s, du, run[0].c * du), fmaf(run[1].s, du, run[1].c * du),
+                                  fmaf(run[2].s, du, run[2].c * du), fmaf(run[3].s, du, run[3].c * du));
+        t[2 * g.nu + 1] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+}
+
+// G(u) of one table row (see sq_bp_prep), u clamped to the detector
+__device__ __forceinline__ float4 sq_G(const float4 *__restrict__ tr, const SqGeo &g, float u) {
+    const float uc = fminf(fmaxf(u, g.u_b0), g.u_end);
+    const int j = min(max((int)floorf((uc - g.u_b0) * g.inv_du), 0), g.nu);
+    const float4 x = __ldg(tr + 2 * j), y = __ldg(tr + 2 * j + 1);
+    return make_float4(fmaf(y.x, uc, x.x), fmaf(y.y, uc, x.y), fmaf(y.z, uc, x.z), fmaf(y.w, uc, x.w));
+}
+
+// TAB: the slabs of this launch (io0 + blockIdx.y) read the row integrals;
+// the host gives them the slabs whose voxels span VG_SQ_TAB_MIN or more cells
+// along u (the magnification grows with io), the others a direct launch.
+template <bool TAB>
 __global__ void __launch_bounds__(BPP * BPZ, 4)
 sq_bp_kernel(SqGeo g, const float4 *__restrict__ sino, int isp0, int isp1, int first,
-             double *__restrict__ planes) {
-    const int io = blockIdx.y;
+             double *__restrict__ planes, const float4 *__restrict__ tab, int io0) {
+    const int io = io0 + blockIdx.y;
     const int tiles_p = (g.n + BPP - 1) / BPP;
     const int ip = (blockIdx.x % tiles_p) * BPP + threadIdx.x;
     const int iz = (blockIdx.x / tiles_p) * BPZ + threadIdx.y;
@@ -202,6 +305,7 @@ sq_bp_kernel(SqGeo g, const float4 *__restrict__ sino, int isp0, int isp1, int f
     Kahan a0, a1, a2, a3;
     if (mag_ok(M)) {
         const float md = M * g.d_pix;
+        constexpr bool pref = TAB;
         for (int isp = isp0; isp < isp1; ++isp) {
             const float sp = fmaf((float)isp, g.dsp, g.sp0);
             const float P0 = fmaf(M, g.p_b0, -fmaf(M, sp, -g.ssp));
@@ -222,8 +326,14 @@ sq_bp_kernel(SqGeo g, const float4 *__restrict__ sino, int isp0, int isp1, int f
                     if (wv <= 0.f) continue;
                     const float4 *row = base + (size_t)iv * g.nu;
                     float t0 = 0.f, t1 = 0.f, t2 = 0.f, t3 = 0.f;
+                    if (pref) {
+                        const float4 *tr = tab + 2 * (((size_t)(isp - isp0) * g.nsz + isz) * g.nv + iv) *
+                                                     (size_t)(g.nu + 1);
+                        const float4 a = sq_G(tr, g, pl), b = sq_G(tr, g, pr);
+                        t0 = b.x - a.x; t1 = b.y - a.y; t2 = b.z - a.z; t3 = b.w - a.w;
+                    }
                     float ul = fmaf((float)iu0, g.du, g.u_b0);
-                    for (int iu = iu0; iu < g.nu && ul < pr; ++iu) {
+                    for (int iu = iu0; !pref && iu < g.nu && ul < pr; ++iu) {
                         const float ur = fmaf((float)(iu + 1), g.du, g.u_b0);
                         const float wu = fminf(ur, pr) - fmaxf(ul, pl);
                         ul = ur;
@@ -335,6 +445,25 @@ size_t plane_bytes(const vg_dd_square_geom *g) {
     return (size_t)4 * g->n * g->n * g->nz * sizeof(double);
 }
 
+// Sources per back-projection launch with row integrals: their table (two
+// float4 per cell boundary) stays within 256 MiB.
+int tab_chunk(const vg_dd_square_geom *g) {
+    const size_t per_src = (size_t)g->nsrc_z * g->nv * (g->nu + 1) * 2 * sizeof(float4);
+    size_t c = ((size_t)256 << 20) / (per_src ? per_src : 1);
+    if (c < 1) c = 1;
+    if (c > (size_t)g->nsrc_p) c = g->nsrc_p;
+    return (int)c;
+}
+
+size_t tab_bytes(const vg_dd_square_geom *g) {
+    return (size_t)tab_chunk(g) * g->nsrc_z * g->nv * (g->nu + 1) * 2 * sizeof(float4);
+}
+
+// workspace: the four FP64 planes, then (256-byte aligned) the row-integral table
+size_t ws_bytes(const vg_dd_square_geom *g) {
+    return ((plane_bytes(g) + 255) & ~(size_t)255) + tab_bytes(g);
+}
+
 int launch_fp(const vg_dd_square_geom *g, const float *vol, float *out, const float *y,
               const float *w, cudaStream_t st) {
     const SqGeo q = make_geo(g);
@@ -379,13 +508,45 @@ int launch_bp(const vg_dd_square_geom *g, const float *sino, double *planes, flo
     dim3 grid(ceil_div(g->n, BPP) * ceil_div(g->nz, BPZ), g->n);
     VG_REQUIRE((long long)ceil_div(g->n, BPP) * ceil_div(g->nz, BPZ) < 2147483647LL,
                "dd_square: volume too large");
-    const int chunk = bp_chunk(g);
+    // slabs io >= io_tab (magnification, hence the cells a voxel spans,
+    // grows with io up to the source plane) read row integrals
+    int io_tab = g->n;
+    for (int io = 0; io < g->n; ++io) {
+        const float M = q.DSD / (q.DSO - fmaf((float)io, q.d_pix, q.p_b0));
+        if (M > 0.f && M < INFINITY && M * q.d_pix >= VG_SQ_TAB_MIN * q.du) {
+            io_tab = io;
+            break;
+        }
+    }
+    const bool use_tab = io_tab < g->n;
+    float4 *tab = reinterpret_cast<float4 *>(reinterpret_cast<char *>(planes) +
+                                             ((plane_bytes(g) + 255) & ~(size_t)255));
+    int chunk = bp_chunk(g);
+    if (use_tab && tab_chunk(g) < chunk) chunk = tab_chunk(g);
     for (int s0 = 0; s0 < g->nsrc_p; s0 += chunk) {
         const int s1 = s0 + chunk < g->nsrc_p ? s0 + chunk : g->nsrc_p;
-        sq_bp_kernel<<<grid, dim3(BPP, BPZ), 0, st>>>(q, reinterpret_cast<const float4 *>(sino),
-                                                      s0, s1, s0 == 0, planes);
-        int s = launch_status("dd_square_bp");
-        if (s) return s;
+        if (use_tab) {
+            const long long rows = (long long)(s1 - s0) * g->nsrc_z * g->nv;
+            VG_REQUIRE(rows < 2147483647LL, "dd_square: too many detector rows per chunk");
+            sq_bp_prep<<<(unsigned)rows, 256, 0, st>>>(q, reinterpret_cast<const float4 *>(sino), s0,
+                                                       tab);
+            int s = launch_status("dd_square_bp_prep");
+            if (s) return s;
+        }
+        if (io_tab > 0) {
+            dim3 gd(grid.x, io_tab);
+            sq_bp_kernel<false><<<gd, dim3(BPP, BPZ), 0, st>>>(
+                q, reinterpret_cast<const float4 *>(sino), s0, s1, s0 == 0, planes, nullptr, 0);
+            int s = launch_status("dd_square_bp");
+            if (s) return s;
+        }
+        if (use_tab) {
+            dim3 gt(grid.x, g->n - io_tab);
+            sq_bp_kernel<true><<<gt, dim3(BPP, BPZ), 0, st>>>(
+                q, reinterpret_cast<const float4 *>(sino), s0, s1, s0 == 0, planes, tab, io_tab);
+            int s = launch_status("dd_square_bp");
+            if (s) return s;
+        }
     }
     dim3 cgrid(ceil_div(g->nz, CZ) * ceil_div(g->n, CY), ceil_div(g->n, CX));
     if (w)
@@ -399,7 +560,7 @@ int launch_bp(const vg_dd_square_geom *g, const float *sino, double *planes, flo
 
 extern "C" size_t vg_dd_square_workspace_bytes(const vg_dd_square_geom *g) {
     if (check(g)) return 0;
-    return plane_bytes(g);
+    return ws_bytes(g);
 }
 
 extern "C" int vg_dd_square_fp(const vg_dd_square_geom *g, const float *vol, float *sino,
@@ -417,9 +578,9 @@ extern "C" int vg_dd_square_bp(const vg_dd_square_geom *g, const float *sino, fl
     if (s) return s;
     VG_REQUIRE(sino && vol && workspace, "dd_square_bp: null pointer");
     VG_REQUIRE(((uintptr_t)sino & 15) == 0, "dd_square_bp: sinogram not 16-byte aligned");
-    VG_REQUIRE(workspace_bytes >= plane_bytes(g), "dd_square_bp: workspace of %zu bytes, %zu needed",
-               workspace_bytes, plane_bytes(g));
-    VG_REQUIRE(((uintptr_t)workspace & 7) == 0, "dd_square_bp: workspace not 8-byte aligned");
+    VG_REQUIRE(workspace_bytes >= ws_bytes(g), "dd_square_bp: workspace of %zu bytes, %zu needed",
+               workspace_bytes, ws_bytes(g));
+    VG_REQUIRE(((uintptr_t)workspace & 15) == 0, "dd_square_bp: workspace not 16-byte aligned");
     return launch_bp(g, sino, static_cast<double *>(workspace), vol, nullptr, 0.f,
                      as_stream(stream));
 }
@@ -431,10 +592,10 @@ extern "C" int vg_dd_square_sirt_iter(const vg_dd_square_geom *g, const float *y
     int s = check(g);
     if (s) return s;
     VG_REQUIRE(y && w_sino && w_vol && x && r && workspace, "dd_square_sirt_iter: null pointer");
-    VG_REQUIRE(workspace_bytes >= plane_bytes(g),
+    VG_REQUIRE(workspace_bytes >= ws_bytes(g),
                "dd_square_sirt_iter: workspace of %zu bytes, %zu needed", workspace_bytes,
-               plane_bytes(g));
-    VG_REQUIRE(((uintptr_t)workspace & 7) == 0, "dd_square_sirt_iter: workspace not 8-byte aligned");
+               ws_bytes(g));
+    VG_REQUIRE(((uintptr_t)workspace & 15) == 0, "dd_square_sirt_iter: workspace not 16-byte aligned");
     VG_REQUIRE((((uintptr_t)y | (uintptr_t)w_sino | (uintptr_t)r) & 15) == 0,
                "dd_square_sirt_iter: sinogram buffers must be 16-byte aligned");
     cudaStream_t st = as_stream(stream);
