@@ -63,7 +63,10 @@ __global__ void fdk_transpose_back(vg_dd3d_geom g, const float *__restrict__ in,
 // Thread = FZ consecutive slices of one (x, y) column; the u coordinate,
 // 1 / U and the u interpolation are shared by the column's slices.  The
 // view table is converted to float once per block into shared memory.
-constexpr int FZ = 4;
+#ifndef VG_FDK_FZ
+#define VG_FDK_FZ 4
+#endif
+constexpr int FZ = VG_FDK_FZ;
 
 __global__ void __launch_bounds__(256)
 fdk_bp_kernel(vg_dd3d_geom g, const float *__restrict__ q, const double *__restrict__ trig,
@@ -83,7 +86,11 @@ fdk_bp_kernel(vg_dd3d_geom g, const float *__restrict__ q, const double *__restr
     for (int t = 0; t < FZ; ++t) z[t] = g.d_pix * ((float)(zb + t) + 0.5f - 0.5f * g.nz);
     const float iu_off = 0.5f * g.nu - 0.5f - g.su, iv_off = 0.5f * g.nv - 0.5f - g.sv;
     const float idu = 1.0f / g.du, idv = 1.0f / g.dv;
+    // per-view terms summed in groups of 16 views, the group sums compensated
     Kahan acc[FZ];
+    float grp[FZ];
+#pragma unroll
+    for (int t = 0; t < FZ; ++t) grp[t] = 0.f;
     for (int ia = 0; ia < g.na; ++ia) {
         const float2 t2 = cs[ia];
         const float c = t2.x, s = t2.y;
@@ -117,14 +124,19 @@ fdk_bp_kernel(vg_dd3d_geom g, const float *__restrict__ q, const double *__restr
                 };
                 q00 = at(0, jv); q01 = at(0, jv + 1); q10 = at(1, jv); q11 = at(1, jv + 1);
             }
-            const float val = (1.f - au) * ((1.f - av) * q00 + av * q01) +
-                              au * ((1.f - av) * q10 + av * q11);
-            acc[t].add(val * w);
+            const float a = fmaf(av, q01 - q00, q00), b = fmaf(av, q11 - q10, q10);
+            grp[t] = fmaf(fmaf(au, b - a, a), w, grp[t]);
+        }
+        if ((ia & 15) == 15) {
+#pragma unroll
+            for (int t = 0; t < FZ; ++t) { acc[t].add(grp[t]); grp[t] = 0.f; }
         }
     }
 #pragma unroll
-    for (int t = 0; t < FZ; ++t)
+    for (int t = 0; t < FZ; ++t) {
+        acc[t].add(grp[t]);
         if (zb + t < g.nz) vol[((size_t)ix * g.ny + iy) * g.nz + zb + t] = acc[t].s * scale;
+    }
 }
 
 int check(const vg_dd3d_geom *g) {
