@@ -479,6 +479,11 @@ def run_workload(args):
                  lambda: orc.aw_fp_fan_2d(img, a2[:24], 768, *geo, du=1.2, d_pix=0.9, joseph=jos),
                  lambda: orc.aw_bp_fan_2d(yh[:24], a2[:24], (512, 512), *geo, du=1.2, d_pix=0.9,
                                           joseph=jos), 30, s24)
+        from vir_gb300 import reconstruction as rcn
+        t_fbp = _event_ms(lambda: rcn.fbp_2d(y2, a2, (512, 512), geom="fan", DSO=500.0, DSD=1000.0,
+                                             du=1.2, d_pix=0.9), reps, stream)
+        out["fbp_fan"] = {"ms": t_fbp, "note": "C2 geometry: cosine weight, ramp filter (FFT "
+                                               "route), 1/U^2-weighted back projection"}
         case("pd_fan", lambda: pdm.pd_fp_fan_2d(x2, a2, 768, *geo, du=1.2, d_pix=0.9),
              lambda: pdm.pd_bp_fan_2d(y2, a2, (512, 512), *geo, du=1.2, d_pix=0.9), 720 * 512 * 512,
              lambda: orc.pd_fp_fan_2d(img, a2[:24], 768, *geo, du=1.2, d_pix=0.9),

@@ -31,16 +31,18 @@ __global__ void fbp2d_bp_kernel(vg_dd2d_geom g, const float *__restrict__ q,
     float y = g.d_pix * ((float)iy + 0.5f - 0.5f * g.ny);
     float inv_du = 1.0f / g.du;
     float off = 0.5f * g.nu - 0.5f - g.su;  // s -> fractional bin index
+    // per-view terms summed in groups of 16 views, the group sums compensated
     Kahan acc;
+    float grp = 0.f;
     for (int ia = 0; ia < g.na; ++ia) {
         float c = (float)__ldg(trig + 2 * ia), s = (float)__ldg(trig + 2 * ia + 1);
         float p = -s * x + c * y;
         float w = 1.0f;
         if (FAN) {
-            float d = g.DSO - (c * x + s * y);
-            p = g.DSD * p / d;
-            float U = d / g.DSO;
-            w = 1.0f / (U * U);
+            const float r = 1.0f / (g.DSO - (c * x + s * y));  // one division per view
+            p = g.DSD * p * r;
+            const float Ui = g.DSO * r;                          // 1 / U
+            w = Ui * Ui;
         }
         float t = p * inv_du + off;
         float ft = floorf(t);
@@ -49,8 +51,13 @@ __global__ void fbp2d_bp_kernel(vg_dd2d_geom g, const float *__restrict__ q,
         const float *row = q + (size_t)ia * g.nu;
         float v0 = (j >= 0 && j < g.nu) ? __ldg(row + j) : 0.f;
         float v1 = (j + 1 >= 0 && j + 1 < g.nu) ? __ldg(row + j + 1) : 0.f;
-        acc.add(w * ((1.0f - a) * v0 + a * v1));
+        grp = fmaf(w, fmaf(a, v1 - v0, v0), grp);
+        if ((ia & 15) == 15) {
+            acc.add(grp);
+            grp = 0.f;
+        }
     }
+    acc.add(grp);
     img[(size_t)ix * g.ny + iy] = acc.s * scale;
 }
 

@@ -325,7 +325,9 @@ pd_bp_kernel(vg_ray_geom g, const double *__restrict__ trig, const float *__rest
     // 1e-4 cell against the rounding of the index arithmetic
     const float inv_du = 1.f / g.du, inv_dv = g.kind == 2 ? 1.f / g.dv : 1.f;
     const float u0 = ubnd(g, 0), v0 = g.kind == 2 ? vbnd(g, 0) : 0.f;
+    // per-view terms summed in groups of 16 views, the group sums compensated
     Kahan acc;
+    float grp = 0.f;
     for (int ia = 0; ia < g.na; ++ia) {
         const float c = (float)__ldg(trig + 2 * ia), s = (float)__ldg(trig + 2 * ia + 1);
         const Foot f = footprint(g, c, s, ix, iy);
@@ -355,8 +357,13 @@ pd_bp_kernel(vg_ray_geom g, const double *__restrict__ trig, const float *__rest
                 }
             }
         }
-        acc.add(part);
+        grp += part;
+        if ((ia & 15) == 15) {
+            acc.add(grp);
+            grp = 0.f;
+        }
     }
+    acc.add(grp);
     img[q] = acc.s * scale;
 }
 
