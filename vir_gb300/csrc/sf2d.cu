@@ -39,7 +39,12 @@ __global__ void sf_fan_fp_kernel(vg_sf2d_geom g, const float *__restrict__ img,
     // t = a x + b y + c0 (double set-up per bin, float walk)
     const double A = uc * s - g.DSD * c, B = -(uc * c + g.DSD * s), C = uc * g.DSO;
     const float a = (float)(A / K), b = (float)(B / K), c0 = (float)(C / K);
+    // the pixel range of a line only has to contain the strip |t| < 1: it is
+    // found with the reciprocal pitch (floor / ceil keep it conservative)
+    const float idp = 1.0f / g.d_pix;
+    // line terms summed in groups of 16 lines, the group sums compensated
     Kahan acc;
+    float grp = 0.f;
     if (fabsf(b) >= fabsf(a)) {
         // x lines (column ix): y range of |t| < 1, read img[ix][iy] (contiguous in iy)
         const float ib = 1.0f / b;
@@ -48,15 +53,14 @@ __global__ void sf_fan_fp_kernel(vg_sf2d_geom g, const float *__restrict__ img,
             const float t0 = fmaf(a, x, c0);
             const float y1 = (-1.f - t0) * ib, y2 = (1.f - t0) * ib;
             const float ylo = fminf(y1, y2), yhi = fmaxf(y1, y2);
-            const int j0 = max(0, (int)floorf(ylo / g.d_pix + 0.5f * g.ny - 0.5f));
-            const int j1 = min(g.ny - 1, (int)ceilf(yhi / g.d_pix + 0.5f * g.ny - 0.5f));
-            float part = 0.f;
+            const int j0 = max(0, (int)floorf(fmaf(ylo, idp, 0.5f * g.ny - 0.5f)));
+            const int j1 = min(g.ny - 1, (int)ceilf(fmaf(yhi, idp, 0.5f * g.ny - 0.5f)));
             for (int iy = j0; iy <= j1; ++iy) {
                 const float t = fmaf(b, centre(g.d_pix, iy, g.ny), t0);
                 const float w = fmaxf(0.f, 1.f - fabsf(t));
-                part = fmaf(__ldg(img + (size_t)ix * g.ny + iy), w, part);
+                grp = fmaf(__ldg(img + (size_t)ix * g.ny + iy), w, grp);
             }
-            acc.add(part);
+            if ((ix & 15) == 15) { acc.add(grp); grp = 0.f; }
         }
     } else {
         const float ia_ = 1.0f / a;
@@ -65,17 +69,17 @@ __global__ void sf_fan_fp_kernel(vg_sf2d_geom g, const float *__restrict__ img,
             const float t0 = fmaf(b, y, c0);
             const float x1 = (-1.f - t0) * ia_, x2 = (1.f - t0) * ia_;
             const float xlo = fminf(x1, x2), xhi = fmaxf(x1, x2);
-            const int i0 = max(0, (int)floorf(xlo / g.d_pix + 0.5f * g.nx - 0.5f));
-            const int i1 = min(g.nx - 1, (int)ceilf(xhi / g.d_pix + 0.5f * g.nx - 0.5f));
-            float part = 0.f;
+            const int i0 = max(0, (int)floorf(fmaf(xlo, idp, 0.5f * g.nx - 0.5f)));
+            const int i1 = min(g.nx - 1, (int)ceilf(fmaf(xhi, idp, 0.5f * g.nx - 0.5f)));
             for (int ix = i0; ix <= i1; ++ix) {
                 const float t = fmaf(a, centre(g.d_pix, ix, g.nx), t0);
                 const float w = fmaxf(0.f, 1.f - fabsf(t));
-                part = fmaf(__ldg(imgT + (size_t)iy * g.nx + ix), w, part);
+                grp = fmaf(__ldg(imgT + (size_t)iy * g.nx + ix), w, grp);
             }
-            acc.add(part);
+            if ((iy & 15) == 15) { acc.add(grp); grp = 0.f; }
         }
     }
+    acc.add(grp);
     sino[(size_t)ia * g.nu + iu] = acc.s * g.d_pix;
 }
 
@@ -86,25 +90,29 @@ __global__ void sf_fan_bp_kernel(vg_sf2d_geom g, const float *__restrict__ sino,
     if (iy >= g.ny) return;
     const float x = centre(g.d_pix, ix, g.nx), y = centre(g.d_pix, iy, g.ny);
     const float inv_du = 1.0f / g.du;
+    const float iDd = 1.0f / (g.DSD * g.d_pix);
+    // view terms summed in groups of 16 views, the group sums compensated
     Kahan acc;
+    float grp = 0.f;
     for (int ia = 0; ia < g.na; ++ia) {
         const float c = (float)__ldg(trig + 2 * ia), s = (float)__ldg(trig + 2 * ia + 1);
         const float xp = fmaf(c, x, s * y), yp = fmaf(-s, x, c * y);
         const float den = g.DSO - yp;
-        const float u0 = g.DSD * xp / den, W = g.DSD * g.d_pix / den;
-        const float iW = 1.0f / W;
+        const float r = 1.0f / den;  // one division per view
+        const float u0 = g.DSD * xp * r, W = g.DSD * g.d_pix * r;
+        const float iW = den * iDd;
         // bins with |u_c - u0| < W: u_c = du (iu - nu/2 + 0.5)
         const int k0 = max(0, (int)ceilf((u0 - W) * inv_du + 0.5f * g.nu - 0.5f));
         const int k1 = min(g.nu - 1, (int)floorf((u0 + W) * inv_du + 0.5f * g.nu - 0.5f));
         const float *row = sino + (size_t)ia * g.nu;
-        float part = 0.f;
         for (int iu = k0; iu <= k1; ++iu) {
             const float uc = g.du * ((float)iu - 0.5f * g.nu + 0.5f);
             const float w = fmaxf(0.f, 1.f - fabsf((uc - u0) * iW));
-            part = fmaf(__ldg(row + iu), w, part);
+            grp = fmaf(__ldg(row + iu), w, grp);
         }
-        acc.add(part);
+        if ((ia & 15) == 15) { acc.add(grp); grp = 0.f; }
     }
+    acc.add(grp);
     img[(size_t)ix * g.ny + iy] = acc.s * g.d_pix;
 }
 
