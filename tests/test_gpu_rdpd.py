@@ -84,6 +84,29 @@ def test_rd_2d_vs_oracle(vg, orc, joseph):
             assert rel(bp, bo) < tol, name
 
 
+@pytest.mark.parametrize("geo", ["par", "fan", "fan_near", "fan_wide"])
+def test_joseph_bp_gather_vs_oracle(vg, orc, geo):
+    """The gathered 2D Joseph back projection: ragged 16-pixel tiles (200 x 130),
+    more than 256 candidate rays per tile and view (du 0.2 against 0.7 mm
+    pixels), a source 12 mm from the image corner (per-pixel ray ranges fall
+    back to the tile's) and a wide fan (edge rays at 41 degrees)."""
+    from vir_gb300.sys_mat import rd
+    rng = np.random.default_rng(21)
+    na, nu = 90, 700
+    angs = np.linspace(0, np.pi if geo == "par" else 2 * np.pi, na, endpoint=False)
+    y = rng.random((na, nu)).astype(np.float32)
+    y[:, ::7] = 0.0  # zero rays are skipped
+    kw = dict(du=0.2, su=0.4, d_pix=0.7, joseph=True)
+    fan = {"fan": (220.0, 400.0), "fan_near": (95.0, 300.0), "fan_wide": (220.0, 80.0)}
+    args = (angs, (200, 130)) + fan.get(geo, ())
+    name = "par" if geo == "par" else "fan"
+    bp = getattr(rd, "aw_bp_%s_2d" % name)(y, *args, **kw)
+    bo = getattr(orc, "aw_bp_%s_2d" % name)(y, *args, **kw)
+    # interior exact to float32 rounding; the border as in test_rd_2d_vs_oracle
+    assert rel(bp[1:-1, 1:-1], bo[1:-1, 1:-1]) < 2e-5
+    assert rel(bp, bo) < 1e-2
+
+
 @pytest.mark.parametrize("joseph", [False, True])
 def test_rd_cone_vs_oracle(vg, orc, joseph):
     """nu != nv: the rows come from nv (rd.py:688 uses nu)."""

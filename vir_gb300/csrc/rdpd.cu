@@ -58,6 +58,23 @@ __device__ __forceinline__ void slab(float r0, float dr, float lo, float hi, flo
     }
 }
 
+// Adds corner c of cell cur (its sum slot[c]) into the image when it is
+// inside the image and nonzero.
+template <int DIM>
+__device__ __forceinline__ void flush(int c, const int *cur, float *__restrict__ bimg, const int *n,
+                                      size_t sx, size_t sy, const float *slot) {
+    if (slot[c] == 0.f) return;
+    bool ok = true;
+    size_t off = 0;
+#pragma unroll
+    for (int a = 0; a < DIM; ++a) {
+        const int i = cur[a] + ((c >> a) & 1);
+        ok = ok && i >= 0 && i < n[a];
+        off += (size_t)i * (a == 0 ? sx : (a == 1 ? sy : 1));
+    }
+    if (ok) atomicAdd(bimg + off, slot[c]);
+}
+
 // One ray: returns the line integral (BP = false) or adds s times the
 // ray's weights into bimg (BP = true).  DIM 2 or 3; img is x-major with
 // z fastest.
@@ -82,6 +99,18 @@ __device__ float trace(const Ray &R, const float *__restrict__ img, float *__res
         // samples at t = te + k / 2 <= tx (the reference's t += step; its float32
         // running sum drifts from te + k / 2 over a ray, this does not)
         const int cap = (int)fminf((tx - te) / step, 4.f * (n[0] + n[1] + (DIM == 3 ? n[2] : 0))) + 2;
+        // 2D back projection: the splats of consecutive samples into the
+        // corners of the current cell cur are summed in registers (slot c:
+        // corner cur + bits of c) and added into the image when the cell moves
+        // on, about 1.4 atomics per sample instead of 4.  Neighbouring rays of a
+        // warp splat into the same pixels, and those atomics were the 2D
+        // kernel's limit.  In 3D the lanes' splats spread along z and their
+        // atomics coalesce; there the per-sample splats are kept (the lanes'
+        // flushes, at different samples, issue far more atomic instructions).
+        int cur[3] = {0, 0, 0};
+        float slot[1 << DIM];
+#pragma unroll
+        for (int c = 0; c < (1 << DIM); ++c) slot[c] = 0.f;
         for (int it = 0; it < cap; ++it) {
             const float t = fmaf((float)it, step, te);
             if (!(t <= tx)) break;
@@ -116,21 +145,68 @@ __device__ float trace(const Ray &R, const float *__restrict__ img, float *__res
                     i0[a] = (int)floorf(f[a]);
                     w0[a] = f[a] - i0[a];
                 }
+                if (DIM == 3) {  // 3D: each splat added at once (see the comment at cur)
+#pragma unroll
+                    for (int c = 0; c < (1 << DIM); ++c) {
+                        float w = s * step;
+                        bool ok = true;
+                        size_t off = 0;
+#pragma unroll
+                        for (int a = 0; a < DIM; ++a) {
+                            const int bit = (c >> a) & 1, i = i0[a] + bit;
+                            ok = ok && i >= 0 && i < n[a];
+                            w *= bit ? w0[a] : 1.f - w0[a];
+                            off += (size_t)i * (a == 0 ? sx : (a == 1 ? sy : 1));
+                        }
+                        if (ok) atomicAdd(bimg + off, w);
+                    }
+                    continue;
+                }
+                if (it == 0) {
+#pragma unroll
+                    for (int a = 0; a < DIM; ++a) cur[a] = i0[a];
+                }
+                // move the corner sums to the sample's cell, one axis at a time:
+                // corners the cell leaves are added into the image, the ones it
+                // keeps stay, the new ones start at zero
+#pragma unroll
+                for (int a = 0; a < DIM; ++a) {
+                    const int dl = i0[a] - cur[a];
+                    if (dl == 0) continue;
+                    const int bit = 1 << a;
+#pragma unroll
+                    for (int c = 0; c < (1 << DIM); ++c) {
+                        if (c & bit) continue;
+                        // c: the low corner along a, c | bit: the high one
+                        if (dl == 1) {
+                            flush<DIM>(c, cur, bimg, n, sx, sy, slot);
+                            slot[c] = slot[c | bit];
+                            slot[c | bit] = 0.f;
+                        } else if (dl == -1) {
+                            flush<DIM>(c | bit, cur, bimg, n, sx, sy, slot);
+                            slot[c | bit] = slot[c];
+                            slot[c] = 0.f;
+                        } else {
+                            flush<DIM>(c, cur, bimg, n, sx, sy, slot);
+                            flush<DIM>(c | bit, cur, bimg, n, sx, sy, slot);
+                            slot[c] = slot[c | bit] = 0.f;
+                        }
+                    }
+                    cur[a] = i0[a];
+                }
+                const float sw = s * step;
 #pragma unroll
                 for (int c = 0; c < (1 << DIM); ++c) {
-                    float w = s * step;
-                    bool ok = true;
-                    size_t off = 0;
+                    float w = sw;
 #pragma unroll
-                    for (int a = 0; a < DIM; ++a) {
-                        const int bit = (c >> a) & 1, i = i0[a] + bit;
-                        ok = ok && i >= 0 && i < n[a];
-                        w *= bit ? w0[a] : 1.f - w0[a];
-                        off += (size_t)i * (a == 0 ? sx : (a == 1 ? sy : 1));
-                    }
-                    if (ok) atomicAdd(bimg + off, w);
+                    for (int a = 0; a < DIM; ++a) w *= ((c >> a) & 1) ? w0[a] : 1.f - w0[a];
+                    slot[c] += w;
                 }
             }
+        }
+        if (BP && DIM == 2) {
+#pragma unroll
+            for (int c = 0; c < (1 << DIM); ++c) flush<DIM>(c, cur, bimg, n, sx, sy, slot);
         }
         return acc;
     }
