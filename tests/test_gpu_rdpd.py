@@ -85,11 +85,11 @@ def test_rd_2d_vs_oracle(vg, orc, joseph):
 
 
 @pytest.mark.parametrize("geo", ["par", "fan", "fan_near", "fan_wide"])
-def test_joseph_bp_gather_vs_oracle(vg, orc, geo):
-    """The gathered 2D Joseph back projection: ragged 16-pixel tiles (200 x 130),
-    more than 256 candidate rays per tile and view (du 0.2 against 0.7 mm
-    pixels), a source 12 mm from the image corner (per-pixel ray ranges fall
-    back to the tile's) and a wide fan (edge rays at 41 degrees)."""
+def test_joseph_bp_2d_vs_oracle(vg, orc, geo):
+    """The 2D Joseph back projection (per-cell sums in registers before the
+    atomics) on a non-square 200 x 130 image with rays 0.2 mm apart against
+    0.7 mm pixels (several rays per pixel), zero rays, a source 12 mm from the
+    image corner and a wide fan (edge rays at 41 degrees)."""
     from vir_gb300.sys_mat import rd
     rng = np.random.default_rng(21)
     na, nu = 90, 700
