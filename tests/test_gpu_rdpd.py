@@ -160,3 +160,26 @@ def test_pd_vs_oracle(vg, orc):
     ys = np.random.default_rng(12).random(fp.shape).astype(np.float32)
     bp = pd.pd_bp_cone_3d(ys, a3, vol.shape, 40.0, 80.0, **kw)
     assert rel(bp, orc.pd_bp_cone_3d(ys, a3, vol.shape, 40.0, 80.0, **kw)) < 2e-5
+
+
+def test_pd_cone_columns_vs_oracle(vg, orc):
+    """Cone pixel-driven FP and BP, one warp per column: x, y not multiples of
+    the 2 x 4 column patch, 300 slices (three z chunks of 128, the last
+    ragged), zero voxels, a detector taller than the volume's shadow, and a
+    coarse detector (pitch 0.3 mm under 0.8 mm voxels: footprints over more
+    than 4 cells take the general walk)."""
+    from vir_gb300.sys_mat import pd
+    rng = np.random.default_rng(23)
+    shape = (13, 10, 300)
+    vol = rng.random(shape).astype(np.float32)
+    vol[:, :, ::5] = 0.0
+    a3 = np.linspace(0, 2 * np.pi, 9, endpoint=False)
+    # the float32 footprint ends (~13 mm off axis) carry ~1.5e-5 mm of rounding:
+    # up to 5e-5 of a 0.3 mm cell's overlap, the same in the per-pixel kernels
+    for du, nu, nv, tol in ((1.1, 28, 420, 2e-5), (0.3, 90, 1300, 1e-4)):
+        kw = dict(du=du, dv=0.9 * du / 1.1, su=0.3, sv=-0.4, d_pix=0.8)
+        fp = pd.pd_fp_cone_3d(vol, a3, nu, nv, 200.0, 320.0, **kw)
+        assert rel(fp, orc.pd_fp_cone_3d(vol, a3, nu, nv, 200.0, 320.0, **kw)) < tol, du
+        ys = rng.random((9, nu, nv)).astype(np.float32)
+        bp = pd.pd_bp_cone_3d(ys, a3, shape, 200.0, 320.0, **kw)
+        assert rel(bp, orc.pd_bp_cone_3d(ys, a3, shape, 200.0, 320.0, **kw)) < 2e-5, du

@@ -16,10 +16,11 @@
 // cone's detector rows use nv (rd.py:688 uses nu).  Every walk is bounded
 // by an iteration count derived from the volume size.
 //
-// Pixel-driven: the back projection is a gather, one thread per pixel or
-// voxel over all views; the forward projection scatters each pixel's
-// footprint into the 1-4 overlapped bins with float atomics, as the
-// reference's loop does (pd.py:56-127).  The fan scale 1 / (|cos(a + g)| +
+// Pixel-driven: the back projection is a gather, one thread per pixel (2D)
+// or one warp per voxel column (cone) over all views; the forward projection
+// scatters each pixel's footprint into the 1-4 overlapped bins with float
+// atomics, as the reference's loop does (pd.py:56-127), one thread per pixel
+// (2D) or one warp per voxel column and view (cone).  The fan scale 1 / (|cos(a + g)| +
 // |sin(a + g)|) with g = atan(u_c / DSD) is evaluated through
 // cos(a + g) = (c - s t) / sqrt(1 + t^2), sin(a + g) = (s + c t) /
 // sqrt(1 + t^2), t = u_c / DSD, and the cone's 1 / cos(g) as sqrt(1 + t^2).
@@ -32,6 +33,10 @@ namespace {
 using namespace vg;
 
 constexpr float RD_EPS = 1e-6f;  // rd.py:42
+
+#ifndef VG_PD_CONE_COLUMNS
+#define VG_PD_CONE_COLUMNS 1
+#endif
 
 struct Ray {
     float o[3], h[3];
@@ -443,6 +448,177 @@ pd_bp_kernel(vg_ray_geom g, const double *__restrict__ trig, const float *__rest
     img[q] = acc.s * scale;
 }
 
+#ifndef VG_PD_ZPT
+#define VG_PD_ZPT 4
+#endif
+constexpr int PD_ZPT = VG_PD_ZPT, PD_FAST = 4;
+
+// Cone FP with one warp per (x, y) column and view: lanes hold the voxels
+// z = l + 32 m of a z chunk (as pd_bp_cone_kernel), so the warp's atomics
+// fall on neighbouring v cells of one u row.  The u overlaps are worked out
+// once per column and view; each term is pd_fp_kernel's
+// ((value kc) (vr - vl)) (ur - ul), cells of zero overlap and zero voxels add
+// nothing.
+__global__ void __launch_bounds__(256)
+pd_fp_cone_kernel(vg_ray_geom g, const double *__restrict__ trig, const float *__restrict__ img,
+                  float *__restrict__ sino, int colx) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int bx = blockIdx.x % colx, by = blockIdx.x / colx;
+    const int ix = bx * 2 + (warp >> 2), iy = by * 4 + (warp & 3);
+    const int zb = blockIdx.y * 32 * PD_ZPT, ia = blockIdx.z;
+    if (ix >= g.nx || iy >= g.ny) return;  // warp-uniform; no barriers below
+    const float c = (float)__ldg(trig + 2 * ia), s = (float)__ldg(trig + 2 * ia + 1);
+    const Foot f = footprint(g, c, s, ix, iy);
+    const float inv_du = 1.f / g.du, inv_dv = 1.f / g.dv;
+    const float u0 = ubnd(g, 0), v0 = vbnd(g, 0);
+    const int iu0 = max(0, (int)floorf(fmaf(f.pmin - u0, inv_du, -1e-4f)));
+    const int iu1 = min(g.nu, (int)floorf(fmaf(f.pmax - u0, inv_du, 1e-4f)) + 1);
+    const int nuc = iu1 - iu0;
+    const float kc = f.scale * inv_du * inv_dv * g.d_pix;
+    float *view = sino + (size_t)ia * g.nu * g.nv;
+    const float *col = img + ((size_t)ix * g.ny + iy) * g.nz;
+    float wu[PD_FAST];
+#pragma unroll
+    for (int a = 0; a < PD_FAST; ++a) {
+        const float ul = fmaxf(f.pmin, ubnd(g, iu0 + a)), ur = fminf(f.pmax, ubnd(g, iu0 + a + 1));
+        wu[a] = (a < nuc && ur > ul) ? ur - ul : 0.f;
+    }
+#pragma unroll
+    for (int m = 0; m < PD_ZPT; ++m) {
+        const int iz = zb + lane + 32 * m;
+        const float val = iz < g.nz ? __ldg(col + iz) : 0.f;
+        if (val == 0.f) continue;
+        const float zl = g.d_pix * ((float)iz - g.nz / 2.f), zr = g.d_pix * ((float)(iz + 1) - g.nz / 2.f);
+        const float vmn = fminf(f.cm * zl, f.cm * zr), vmx = fmaxf(f.cm * zl, f.cm * zr);
+        const int iv0 = max(0, (int)floorf(fmaf(vmn - v0, inv_dv, -1e-4f)));
+        const int iv1 = min(g.nv, (int)floorf(fmaf(vmx - v0, inv_dv, 1e-4f)) + 1);
+        const float kv = val * kc;
+        if (nuc <= PD_FAST && iv1 - iv0 <= PD_FAST) {
+            float wv[PD_FAST];
+#pragma unroll
+            for (int j = 0; j < PD_FAST; ++j) {
+                const float vl = fmaxf(vmn, vbnd(g, iv0 + j)), vr = fminf(vmx, vbnd(g, iv0 + j + 1));
+                wv[j] = (iv0 + j < iv1 && vr > vl) ? kv * (vr - vl) : 0.f;
+            }
+#pragma unroll
+            for (int a = 0; a < PD_FAST; ++a) {
+                if (a >= nuc) break;  // warp-uniform
+                float *row = view + (size_t)(iu0 + a) * g.nv + iv0;
+#pragma unroll
+                for (int j = 0; j < PD_FAST; ++j)
+                    if (wv[j] != 0.f && wu[a] > 0.f) atomicAdd(row + j, wv[j] * wu[a]);
+            }
+        } else {
+            for (int iv = iv0; iv < iv1; ++iv) {
+                const float vl = fmaxf(vmn, vbnd(g, iv)), vr = fminf(vmx, vbnd(g, iv + 1));
+                if (vr <= vl) continue;
+                const float kvv = kv * (vr - vl);
+                for (int iu = iu0; iu < iu1; ++iu) {
+                    const float ul = fmaxf(f.pmin, ubnd(g, iu)), ur = fminf(f.pmax, ubnd(g, iu + 1));
+                    if (ur > ul) atomicAdd(view + (size_t)iu * g.nv + iv, kvv * (ur - ul));
+                }
+            }
+        }
+    }
+}
+
+// Cone BP with one warp per (x, y) column: the column's u footprint (cells,
+// overlaps) is worked out once per view for all its voxels, lane l holding the
+// voxels z = l + 32 m, m < PD_ZPT (a z chunk of 32 PD_ZPT voxels per block
+// row); the 8 warps of a block are a 2 x 4 patch of neighbouring columns,
+// whose footprints share sinogram cells in L1.  When the footprint covers at
+// most 4 u and 4 v cells, the u overlaps (ur - ul) and each voxel's
+// k (vr - vl) are computed once per view and held in registers; otherwise
+// the cells are walked as in pd_bp_kernel.  Each term has pd_bp_kernel's
+// weight (k (vr - vl)) (ur - ul), and cells of zero overlap add nothing; per
+// view the terms are summed u cells outside, v cells inside.
+
+__global__ void __launch_bounds__(256)
+pd_bp_cone_kernel(vg_ray_geom g, const double *__restrict__ trig, const float *__restrict__ sino,
+                  float *__restrict__ img, float scale) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int ix = blockIdx.x * 2 + (warp >> 2), iy = blockIdx.y * 4 + (warp & 3);
+    const int zb = blockIdx.z * 32 * PD_ZPT;
+    if (ix >= g.nx || iy >= g.ny) return;  // warp-uniform; no barriers below
+    const float inv_du = 1.f / g.du, inv_dv = 1.f / g.dv;
+    const float u0 = ubnd(g, 0), v0 = vbnd(g, 0);
+    float zl[PD_ZPT], zr[PD_ZPT], grp[PD_ZPT];
+    bool in[PD_ZPT];
+    Kahan acc[PD_ZPT];
+#pragma unroll
+    for (int m = 0; m < PD_ZPT; ++m) {
+        const int iz = zb + lane + 32 * m;
+        in[m] = iz < g.nz;
+        zl[m] = g.d_pix * ((float)iz - g.nz / 2.f);
+        zr[m] = g.d_pix * ((float)(iz + 1) - g.nz / 2.f);
+        grp[m] = 0.f;
+    }
+    for (int ia = 0; ia < g.na; ++ia) {
+        const float c = (float)__ldg(trig + 2 * ia), s = (float)__ldg(trig + 2 * ia + 1);
+        const Foot f = footprint(g, c, s, ix, iy);
+        const int iu0 = max(0, (int)floorf(fmaf(f.pmin - u0, inv_du, -1e-4f)));
+        const int iu1 = min(g.nu, (int)floorf(fmaf(f.pmax - u0, inv_du, 1e-4f)) + 1);
+        const int nuc = iu1 - iu0;
+        const float k = f.scale * inv_du * inv_dv;
+        const float *view = sino + (size_t)ia * g.nu * g.nv;
+        float wu[PD_FAST];
+#pragma unroll
+        for (int a = 0; a < PD_FAST; ++a) {
+            const float ul = fmaxf(f.pmin, ubnd(g, iu0 + a)), ur = fminf(f.pmax, ubnd(g, iu0 + a + 1));
+            wu[a] = (a < nuc && ur > ul) ? ur - ul : 0.f;
+        }
+#pragma unroll
+        for (int m = 0; m < PD_ZPT; ++m) {
+            const float vmn = fminf(f.cm * zl[m], f.cm * zr[m]), vmx = fmaxf(f.cm * zl[m], f.cm * zr[m]);
+            const int iv0 = in[m] ? max(0, (int)floorf(fmaf(vmn - v0, inv_dv, -1e-4f))) : 0;
+            const int iv1 = in[m] ? min(g.nv, (int)floorf(fmaf(vmx - v0, inv_dv, 1e-4f)) + 1) : 0;
+            const int nvc = iv1 - iv0;
+            float part = 0.f;
+            if (nuc <= PD_FAST && nvc <= PD_FAST) {
+                float wv[PD_FAST];
+#pragma unroll
+                for (int j = 0; j < PD_FAST; ++j) {
+                    const float vl = fmaxf(vmn, vbnd(g, iv0 + j)), vr = fminf(vmx, vbnd(g, iv0 + j + 1));
+                    wv[j] = (j < nvc && vr > vl) ? k * (vr - vl) : 0.f;
+                }
+#pragma unroll
+                for (int a = 0; a < PD_FAST; ++a) {
+                    if (a >= nuc) break;  // warp-uniform
+                    const float *col = view + (size_t)(iu0 + a) * g.nv + iv0;
+#pragma unroll
+                    for (int j = 0; j < PD_FAST; ++j)
+                        if (wv[j] > 0.f && wu[a] > 0.f) part = fmaf(__ldg(col + j), wv[j] * wu[a], part);
+                }
+            } else {
+                for (int iu = iu0; iu < iu1; ++iu) {
+                    const float ul = fmaxf(f.pmin, ubnd(g, iu)), ur = fminf(f.pmax, ubnd(g, iu + 1));
+                    if (!(ur > ul)) continue;
+                    const float *col = view + (size_t)iu * g.nv;
+                    for (int iv = iv0; iv < iv1; ++iv) {
+                        const float vl = fmaxf(vmn, vbnd(g, iv)), vr = fminf(vmx, vbnd(g, iv + 1));
+                        if (vr <= vl) continue;
+                        part = fmaf(__ldg(col + iv), (k * (vr - vl)) * (ur - ul), part);
+                    }
+                }
+            }
+            grp[m] += part;
+        }
+        if ((ia & 15) == 15) {
+#pragma unroll
+            for (int m = 0; m < PD_ZPT; ++m) {
+                acc[m].add(grp[m]);
+                grp[m] = 0.f;
+            }
+        }
+    }
+    float *out = img + ((size_t)ix * g.ny + iy) * g.nz;
+#pragma unroll
+    for (int m = 0; m < PD_ZPT; ++m) {
+        acc[m].add(grp[m]);
+        if (in[m]) out[zb + lane + 32 * m] = acc[m].s * scale;
+    }
+}
+
 int check(const vg_ray_geom *g) {
     VG_REQUIRE(g, "ray/pixel-driven: null geometry");
     VG_REQUIRE(g->kind >= 0 && g->kind <= 2, "ray/pixel-driven: kind must be 0 (par), 1 (fan), 2 (cone)");
@@ -514,6 +690,13 @@ extern "C" int vg_pd_fp(const vg_ray_geom *g, const float *img, const double *tr
     cudaStream_t st = as_stream(stream);
     cudaError_t e = cudaMemsetAsync(sino, 0, sino_count(g) * sizeof(float), st);
     if (e != cudaSuccess) return cuda_status(e, "pd_fp: clear");
+    if (g->kind == 2 && VG_PD_CONE_COLUMNS) {
+        const int colx = ceil_div(g->nx, 2);
+        dim3 grid(colx * ceil_div(g->ny, 4), ceil_div(g->nz, 32 * PD_ZPT), g->na);
+        VG_REQUIRE(grid.y < 65536, "pd_fp: volume too large");
+        pd_fp_cone_kernel<<<grid, 256, 0, st>>>(*g, trig, img, sino, colx);
+        return launch_status("pd_fp");
+    }
     dim3 grid(ceil_div((long long)g->nx * g->ny, 256), g->na);
     pd_fp_kernel<<<grid, 256, 0, st>>>(*g, trig, img, sino);
     return launch_status("pd_fp");
@@ -527,6 +710,12 @@ extern "C" int vg_pd_bp(const vg_ray_geom *g, const float *sino, const double *t
     // img / na / d_pix * du (pd.py:232); cone * dv (pd.py:479)
     float sc = g->du / ((float)g->na * g->d_pix);
     if (g->kind == 2) sc *= g->dv;
+    if (g->kind == 2 && VG_PD_CONE_COLUMNS) {
+        dim3 grid(ceil_div(g->nx, 2), ceil_div(g->ny, 4), ceil_div(g->nz, 32 * PD_ZPT));
+        VG_REQUIRE(grid.y < 65536 && grid.z < 65536, "pd_bp: volume too large");
+        pd_bp_cone_kernel<<<grid, 256, 0, as_stream(stream)>>>(*g, trig, sino, img, sc);
+        return launch_status("pd_bp");
+    }
     const long long n = (long long)img_count(g);
     VG_REQUIRE(ceil_div(n, 256) < 2147483647LL, "pd_bp: volume too large");
     pd_bp_kernel<<<ceil_div(n, 256), 256, 0, as_stream(stream)>>>(*g, trig, sino, img, sc);
