@@ -240,16 +240,30 @@ __device__ float trace(const Ray &R, const float *__restrict__ img, float *__res
 #pragma unroll
         for (int a = 0; a < DIM; ++a) out = out || ir[a] < 0 || ir[a] >= n[a];
         if (out) break;
-        int a;
-        if (DIM == 2) a = tn[0] <= tn[1] ? 0 : 1;
-        else a = (tn[0] <= tn[1] && tn[0] <= tn[2]) ? 0 : (tn[1] <= tn[2] ? 1 : 2);
-        const float tnext = fminf(tn[a], tx);
+        // the axis whose boundary comes first (ties to the lower axis), as
+        // per-axis flags so that the walk state stays in registers
+        bool pick[3];
+        if (DIM == 2) {
+            pick[0] = tn[0] <= tn[1];
+            pick[1] = !pick[0];
+            pick[2] = false;
+        } else {
+            pick[0] = tn[0] <= tn[1] && tn[0] <= tn[2];
+            pick[1] = !pick[0] && tn[1] <= tn[2];
+            pick[2] = !pick[0] && !pick[1];
+        }
+        const float tnext = fminf(pick[0] ? tn[0] : (pick[1] ? tn[1] : tn[2]), tx);
         const size_t v = ir[0] * sx + ir[1] * sy + (DIM == 3 ? (size_t)ir[2] : 0);
         if (BP) atomicAdd(bimg + v, s * (tnext - t));
         else acc += __ldg(img + v) * (tnext - t);
         t = tnext;
-        tn[a] += ts[a];
-        ir[a] += dir[a];
+#pragma unroll
+        for (int a = 0; a < DIM; ++a) {
+            if (pick[a]) {
+                tn[a] += ts[a];
+                ir[a] += dir[a];
+            }
+        }
     }
     return acc;
 }
