@@ -34,6 +34,10 @@ using namespace vg;
 
 constexpr float RD_EPS = 1e-6f;  // rd.py:42
 
+#ifndef VG_JOSEPH_AFFINE
+#define VG_JOSEPH_AFFINE 1
+#endif
+
 #ifndef VG_PD_CONE_COLUMNS
 #define VG_PD_CONE_COLUMNS 1
 #endif
@@ -116,12 +120,36 @@ __device__ float trace(const Ray &R, const float *__restrict__ img, float *__res
         float slot[1 << DIM];
 #pragma unroll
         for (int c = 0; c < (1 << DIM); ++c) slot[c] = 0.f;
+#if VG_JOSEPH_AFFINE
+        // sample k's pixel coordinates, (o + t h - c0) / d at t = te + k step,
+        // as F0 + k dF (one FMA per axis, no division per sample; within an ulp
+        // of |f| of the quotient); the samples are the loop's own: k < cap with
+        // te + k step <= tx, a prefix of k found once
+        float F0[3], dF[3];
+#pragma unroll
+        for (int a = 0; a < DIM; ++a) {
+            F0[a] = (R.o[a] + te * R.h[a] - c0[a]) / d;
+            dF[a] = step * R.h[a] / d;
+        }
+        int kend;
+        {
+            int k = min((int)floorf((tx - te) / step), cap - 1);
+            for (int q = 0; q < 3 && k >= 0 && !(fmaf((float)k, step, te) <= tx); ++q) --k;
+            for (int q = 0; q < 3 && k + 1 < cap && fmaf((float)(k + 1), step, te) <= tx; ++q) ++k;
+            kend = k + 1;
+        }
+        for (int it = 0; it < kend; ++it) {
+            float f[3];
+#pragma unroll
+            for (int a = 0; a < DIM; ++a) f[a] = fmaf((float)it, dF[a], F0[a]);
+#else
         for (int it = 0; it < cap; ++it) {
             const float t = fmaf((float)it, step, te);
             if (!(t <= tx)) break;
             float f[3];
 #pragma unroll
             for (int a = 0; a < DIM; ++a) f[a] = (R.o[a] + t * R.h[a] - c0[a]) / d;
+#endif
             if (!BP && DIM == 2) {  // rd.py:269-289: clamped bilinear
                 const float fx = fminf(fmaxf(f[0], 0.f), n[0] - 2.f);
                 const float fy = fminf(fmaxf(f[1], 0.f), n[1] - 2.f);
