@@ -447,6 +447,11 @@ def run_workload(args):
         out = {}
 
         def case(name, fp, bp, units, cpu_fp, cpu_bp, cpu_scale, sample):
+            if args.kernels_only:  # profiling aid: launch the pair, no timing, no CPU port
+                for _ in range(args.kernels_only):
+                    fp(); bp()
+                out[name] = {}
+                return
             t_fp, t_bp = _event_ms(fp, reps, stream), _event_ms(bp, reps, stream)
             t0 = time.perf_counter()
             cpu_fp()

@@ -493,7 +493,10 @@ pd_bp_kernel(vg_ray_geom g, const double *__restrict__ trig, const float *__rest
 #ifndef VG_PD_ZPT
 #define VG_PD_ZPT 4
 #endif
-constexpr int PD_ZPT = VG_PD_ZPT, PD_FAST = 4;
+#ifndef VG_PD_FV
+#define VG_PD_FV 3
+#endif
+constexpr int PD_ZPT = VG_PD_ZPT, PD_FAST = 4, PD_FV = VG_PD_FV;  // fast path: u, v cells
 
 // Cone FP with one warp per (x, y) column and view: lanes hold the voxels
 // z = l + 32 m of a z chunk (as pd_bp_cone_kernel), so the warp's atomics
@@ -535,10 +538,10 @@ pd_fp_cone_kernel(vg_ray_geom g, const double *__restrict__ trig, const float *_
         const int iv0 = max(0, (int)floorf(fmaf(vmn - v0, inv_dv, -1e-4f)));
         const int iv1 = min(g.nv, (int)floorf(fmaf(vmx - v0, inv_dv, 1e-4f)) + 1);
         const float kv = val * kc;
-        if (nuc <= PD_FAST && iv1 - iv0 <= PD_FAST) {
-            float wv[PD_FAST];
+        if (nuc <= PD_FAST && iv1 - iv0 <= PD_FV) {
+            float wv[PD_FV];
 #pragma unroll
-            for (int j = 0; j < PD_FAST; ++j) {
+            for (int j = 0; j < PD_FV; ++j) {
                 const float vl = fmaxf(vmn, vbnd(g, iv0 + j)), vr = fminf(vmx, vbnd(g, iv0 + j + 1));
                 wv[j] = (iv0 + j < iv1 && vr > vl) ? kv * (vr - vl) : 0.f;
             }
@@ -547,7 +550,7 @@ pd_fp_cone_kernel(vg_ray_geom g, const double *__restrict__ trig, const float *_
                 if (a >= nuc) break;  // warp-uniform
                 float *row = view + (size_t)(iu0 + a) * g.nv + iv0;
 #pragma unroll
-                for (int j = 0; j < PD_FAST; ++j)
+                for (int j = 0; j < PD_FV; ++j)
                     if (wv[j] != 0.f && wu[a] > 0.f) atomicAdd(row + j, wv[j] * wu[a]);
             }
         } else {
@@ -569,7 +572,7 @@ pd_fp_cone_kernel(vg_ray_geom g, const double *__restrict__ trig, const float *_
 // voxels z = l + 32 m, m < PD_ZPT (a z chunk of 32 PD_ZPT voxels per block
 // row); the 8 warps of a block are a 2 x 4 patch of neighbouring columns,
 // whose footprints share sinogram cells in L1.  When the footprint covers at
-// most 4 u and 4 v cells, the u overlaps (ur - ul) and each voxel's
+// most 4 u and 3 v cells, the u overlaps (ur - ul) and each voxel's
 // k (vr - vl) are computed once per view and held in registers; otherwise
 // the cells are walked as in pd_bp_kernel.  Each term has pd_bp_kernel's
 // weight (k (vr - vl)) (ur - ul), and cells of zero overlap add nothing; per
@@ -616,10 +619,10 @@ pd_bp_cone_kernel(vg_ray_geom g, const double *__restrict__ trig, const float *_
             const int iv1 = in[m] ? min(g.nv, (int)floorf(fmaf(vmx - v0, inv_dv, 1e-4f)) + 1) : 0;
             const int nvc = iv1 - iv0;
             float part = 0.f;
-            if (nuc <= PD_FAST && nvc <= PD_FAST) {
-                float wv[PD_FAST];
+            if (nuc <= PD_FAST && nvc <= PD_FV) {
+                float wv[PD_FV];
 #pragma unroll
-                for (int j = 0; j < PD_FAST; ++j) {
+                for (int j = 0; j < PD_FV; ++j) {
                     const float vl = fmaxf(vmn, vbnd(g, iv0 + j)), vr = fminf(vmx, vbnd(g, iv0 + j + 1));
                     wv[j] = (j < nvc && vr > vl) ? k * (vr - vl) : 0.f;
                 }
@@ -628,7 +631,7 @@ pd_bp_cone_kernel(vg_ray_geom g, const double *__restrict__ trig, const float *_
                     if (a >= nuc) break;  // warp-uniform
                     const float *col = view + (size_t)(iu0 + a) * g.nv + iv0;
 #pragma unroll
-                    for (int j = 0; j < PD_FAST; ++j)
+                    for (int j = 0; j < PD_FV; ++j)
                         if (wv[j] > 0.f && wu[a] > 0.f) part = fmaf(__ldg(col + j), wv[j] * wu[a], part);
                 }
             } else {
