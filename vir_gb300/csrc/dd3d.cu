@@ -188,7 +188,10 @@ __device__ __forceinline__ void fp_cells(const float4 *uw, const int *uk, const 
     }
 }
 
-__global__ void __launch_bounds__(256, 3)
+#ifndef VG_CONE_FP_MINB
+#define VG_CONE_FP_MINB 3
+#endif
+__global__ void __launch_bounds__(256, VG_CONE_FP_MINB)
 dd3d_fp_kernel(vg_dd3d_geom g, const float *__restrict__ vol, const float4 *__restrict__ vf,
                const float2 *__restrict__ tab, float *__restrict__ sino) {
     __shared__ FpTables S;
@@ -378,7 +381,10 @@ __device__ float bp_voxel_view(const vg_dd3d_geom &g, const View3 &v, const floa
     return part * sz.x;
 }
 
-__global__ void __launch_bounds__(256, 3)
+#ifndef VG_CONE_BP_MINB
+#define VG_CONE_BP_MINB 5
+#endif
+__global__ void __launch_bounds__(256, VG_CONE_BP_MINB)
 dd3d_bp_kernel(vg_dd3d_geom g, const float *__restrict__ sino, const float4 *__restrict__ vf,
                const float2 *__restrict__ tab, float *__restrict__ vol) {
     __shared__ BpTables T;
