@@ -183,3 +183,21 @@ def test_pd_cone_columns_vs_oracle(vg, orc):
         ys = rng.random((9, nu, nv)).astype(np.float32)
         bp = pd.pd_bp_cone_3d(ys, a3, shape, 200.0, 320.0, **kw)
         assert rel(bp, orc.pd_bp_cone_3d(ys, a3, shape, 200.0, 320.0, **kw)) < 2e-5, du
+
+
+@pytest.mark.parametrize("geo", ["par", "fan"])
+def test_pd_fp_2d_runs_vs_oracle(vg, orc, geo):
+    """2D pixel-driven FP, one thread per run of 32 pixels along y: 45 x 70
+    image (runs cut short at the column end), zero pixels inside runs, views
+    all round (footprints moving both ways along u; at 90 and 270 degrees the
+    fan's direction changes across the image)."""
+    from vir_gb300.sys_mat import pd
+    rng = np.random.default_rng(31)
+    img = rng.random((45, 70)).astype(np.float32)
+    img[:, 3::9] = 0.0
+    img[7] = 0.0
+    angs = np.linspace(0, 2 * np.pi, 36, endpoint=False)
+    kw = dict(du=0.7, su=0.25, d_pix=0.9)
+    args = (angs, 160) + (() if geo == "par" else (90.0, 170.0))
+    fp = getattr(pd, "pd_fp_%s_2d" % geo)(img, *args, **kw)
+    assert rel(fp, getattr(orc, "pd_fp_%s_2d" % geo)(img, *args, **kw)) < 2e-5

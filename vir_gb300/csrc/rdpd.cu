@@ -19,8 +19,8 @@
 // Pixel-driven: the back projection is a gather, one thread per pixel (2D)
 // or one warp per voxel column (cone) over all views; the forward projection
 // scatters each pixel's footprint into the 1-4 overlapped bins with float
-// atomics, as the reference's loop does (pd.py:56-127), one thread per pixel
-// (2D) or one warp per voxel column and view (cone).  The fan scale 1 / (|cos(a + g)| +
+// atomics, as the reference's loop does (pd.py:56-127), one thread per run of
+// pixels along y (2D) or one warp per voxel column and view (cone).  The fan scale 1 / (|cos(a + g)| +
 // |sin(a + g)|) with g = atan(u_c / DSD) is evaluated through
 // cos(a + g) = (c - s t) / sqrt(1 + t^2), sin(a + g) = (s + c t) /
 // sqrt(1 + t^2), t = u_c / DSD, and the cone's 1 / cos(g) as sqrt(1 + t^2).
@@ -433,6 +433,59 @@ pd_fp_kernel(vg_ray_geom g, const double *__restrict__ trig, const float *__rest
     }
 }
 
+// 2D FP with a run of PD_RUN pixels along y per thread: the footprints of
+// consecutive pixels move monotonically along u (towards larger u when
+// c > 0 (parallel) or c DSO > x (fan), the sign of dp/dy), so the thread
+// visits each pixel's bins in that direction and sums consecutive
+// contributions to one bin in a register, adding the sum into the sinogram
+// when the bin changes.  Each contribution is pd_fp_kernel's.
+#ifndef VG_PD_RUN
+#define VG_PD_RUN 32
+#endif
+constexpr int PD_RUN = VG_PD_RUN;
+
+__global__ void __launch_bounds__(256)
+pd_fp_run_kernel(vg_ray_geom g, const double *__restrict__ trig, const float *__restrict__ img,
+                 float *__restrict__ sino) {
+    const int runs = (g.ny + PD_RUN - 1) / PD_RUN;
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    const int ia = blockIdx.y;
+    if (q >= g.nx * runs) return;
+    const int ix = q / runs, iy0 = (q - ix * runs) * PD_RUN;
+    const float c = (float)__ldg(trig + 2 * ia), s = (float)__ldg(trig + 2 * ia + 1);
+    const float inv_du = 1.f / g.du;
+    const float u0 = ubnd(g, 0);
+    const float x = g.d_pix * ((float)ix + 0.5f - g.nx / 2.f);
+    const bool up = g.kind == 0 ? c >= 0.f : c * g.DSO >= x;
+    float *row = sino + (size_t)ia * g.nu;
+    int pb = -1;
+    float pv = 0.f;
+    for (int i = 0; i < PD_RUN; ++i) {
+        const int iy = iy0 + i;
+        if (iy >= g.ny) break;
+        const float val = __ldg(img + (size_t)ix * g.ny + iy);
+        if (val == 0.f) continue;
+        const Foot f = footprint(g, c, s, ix, iy);
+        const int iu0 = max(0, (int)floorf(fmaf(f.pmin - u0, inv_du, -1e-4f)));
+        const int iu1 = min(g.nu, (int)floorf(fmaf(f.pmax - u0, inv_du, 1e-4f)) + 1);
+        const float k = val * f.scale * inv_du * g.d_pix;
+        for (int m = 0; m < iu1 - iu0; ++m) {
+            const int iu = up ? iu0 + m : iu1 - 1 - m;
+            const float l = fmaxf(f.pmin, ubnd(g, iu)), r = fminf(f.pmax, ubnd(g, iu + 1));
+            if (!(r > l)) continue;
+            const float w = k * (r - l);
+            if (iu == pb) {
+                pv += w;
+            } else {
+                if (pb >= 0) atomicAdd(row + pb, pv);
+                pb = iu;
+                pv = w;
+            }
+        }
+    }
+    if (pb >= 0) atomicAdd(row + pb, pv);
+}
+
 // BP: thread = pixel / voxel (lanes along z for the cone), gather over views.
 __global__ void __launch_bounds__(256)
 pd_bp_kernel(vg_ray_geom g, const double *__restrict__ trig, const float *__restrict__ sino,
@@ -740,6 +793,11 @@ extern "C" int vg_pd_fp(const vg_ray_geom *g, const float *img, const double *tr
         dim3 grid(colx * ceil_div(g->ny, 4), ceil_div(g->nz, 32 * PD_ZPT), g->na);
         VG_REQUIRE(grid.y < 65536, "pd_fp: volume too large");
         pd_fp_cone_kernel<<<grid, 256, 0, st>>>(*g, trig, img, sino, colx);
+        return launch_status("pd_fp");
+    }
+    if (g->kind < 2 && PD_RUN > 1) {
+        dim3 grid(ceil_div((long long)g->nx * ceil_div(g->ny, PD_RUN), 256), g->na);
+        pd_fp_run_kernel<<<grid, 256, 0, st>>>(*g, trig, img, sino);
         return launch_status("pd_fp");
     }
     dim3 grid(ceil_div((long long)g->nx * g->ny, 256), g->na);
