@@ -201,3 +201,17 @@ def test_pd_fp_2d_runs_vs_oracle(vg, orc, geo):
     args = (angs, 160) + (() if geo == "par" else (90.0, 170.0))
     fp = getattr(pd, "pd_fp_%s_2d" % geo)(img, *args, **kw)
     assert rel(fp, getattr(orc, "pd_fp_%s_2d" % geo)(img, *args, **kw)) < 2e-5
+
+
+def test_joseph_cone_bp_z_faces_vs_oracle(vg, orc):
+    """Cone Joseph BP with detector rows beyond both z faces, so samples
+    splat onto the first and last slices (half of their corners outside the
+    volume)."""
+    from vir_gb300.sys_mat import rd
+    rng = np.random.default_rng(33)
+    shape = (10, 9, 16)
+    angs = np.linspace(0, 2 * np.pi, 14, endpoint=False)
+    kw = dict(du=1.1, dv=0.7, su=0.2, sv=-0.1, d_pix=1.0, joseph=True)
+    y = rng.random((14, 30, 48)).astype(np.float32)
+    bp = rd.aw_bp_cone_3d(y, angs, shape, 50.0, 90.0, **kw)
+    assert rel(bp, orc.aw_bp_cone_3d(y, angs, shape, 50.0, 90.0, **kw)) < 1e-4
