@@ -86,6 +86,13 @@ int vg_siddon2d_trace(int nx, int ny, const double *trig, int na, int n_dets,
                       double d_det, double d_pix, int *count,
                       unsigned long long *hash, double *len, void *stream);
 
+/* Check of the FP64 quotient the Siddon kernels use for plane crossings:
+ * q[i] = a[i] / b[i] from the reciprocal RN(1 / b[i]) and one FMA correction
+ * (Markstein), which must equal the correctly rounded quotient bit for bit.
+ * Device arrays of n doubles; finite operands, b[i] != 0.  No counterpart in
+ * vir (a self-check of this library). */
+int vg_div_rn_check(const double *a, const double *b, size_t n, double *q, void *stream);
+
 /* ---- Siddon ray lists (3D) ------------------------------------------------ */
 
 /* Per-ray set-up of sys_mat/siddon.py:siddons (computed on the host in the

@@ -51,6 +51,43 @@ def test_siddon_c1_voxel_sequences(vg, orc):
     assert int(cnt_o.sum()) == orc.siddons_count_2d((256, 256), angs, 367)
 
 
+def test_siddon_division_correctly_rounded(vg):
+    """The Siddon kernels' FP64 quotients (reciprocal plus one FMA correction)
+    equal the correctly rounded quotients bit for bit: on the plane-crossing
+    operands of the C1 geometry (every view and ray, every 4th plane of each
+    axis, as the kernels form them) and on 2 M random operands spanning 1e-10
+    to 1e10 over 1e-17 to 1e3."""
+    import torch
+    from vir_gb300 import _core
+    from vir_gb300._lib import call
+    dev = torch.device("cuda")
+    angs = np.linspace(0, np.pi, 180, endpoint=False)
+    trig = _core.trig_cache.get(angs, None, dev).cpu().numpy().reshape(-1, 2)
+    n, n_dets, d_det, d_pix = 256, 367, 1.0, 1.0
+    k = np.arange(n_dets, dtype=np.float64)
+    det = d_det * ((k - n_dets * 0.5) + 0.5)
+    edges = d_pix * (np.arange(0, n + 1, 4, dtype=np.float64) - n * 0.5)
+    A, B = [], []
+    for dx, dy in trig:
+        x0, y0 = det * -dy, det * dx
+        if dx != 0.0:
+            A.append((edges[None, :] - x0[:, None]).ravel()); B.append(np.full(A[-1].size, dx))
+        if dy != 0.0:
+            A.append((edges[None, :] - y0[:, None]).ravel()); B.append(np.full(A[-1].size, dy))
+    rng = np.random.default_rng(41)
+    m = 2_000_000
+    A.append(rng.choice([-1.0, 1.0], m) * 10.0 ** rng.uniform(-10, 10, m))
+    B.append(rng.choice([-1.0, 1.0], m) * 10.0 ** rng.uniform(-17, 3, m))
+    a, b = np.concatenate(A), np.concatenate(B)
+    ta, tb = torch.from_numpy(a).to(dev), torch.from_numpy(b).to(dev)
+    q = torch.empty_like(ta)
+    call("vg_div_rn_check", _core.ptr(ta), _core.ptr(tb), a.size, _core.ptr(q), _core.stream(dev))
+    torch.cuda.synchronize()
+    ref = a / b
+    bad = np.flatnonzero(q.cpu().numpy().view(np.uint64) != ref.view(np.uint64))
+    assert bad.size == 0, (bad.size, a[bad[:3]], b[bad[:3]])
+
+
 @pytest.mark.parametrize("shape,n_dets,d_det,d_pix,na,span", [
     ((256, 256), 367, 1.0, 1.0, 180, np.pi),     # config C1
     ((40, 33), 61, 0.7, 1.3, 37, 2 * np.pi),     # ragged, non power-of-two pitch

@@ -80,6 +80,7 @@ _PROTOS = {
                        c_void_p, c_void_p],
     "vg_siddon2d_trace": [c_int, c_int, c_void_p, c_int, c_int, c_double, c_double, c_void_p,
                           c_void_p, c_void_p, c_void_p],
+    "vg_div_rn_check": [c_void_p, c_void_p, c_size_t, c_void_p, c_void_p],
     "vg_siddon2d_bp_scatter": [c_void_p, c_int, c_int, c_void_p, c_int, c_int, c_double,
                                c_double, c_void_p, c_void_p, c_size_t, c_void_p],
     "vg_siddons_count": [ctypes.POINTER(SiddonRays), c_void_p, c_void_p, c_void_p],

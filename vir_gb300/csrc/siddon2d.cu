@@ -35,8 +35,35 @@ __device__ __forceinline__ double div_pix(const SidGeom &g, double v) {
     return g.dpix_pow2 ? d_mul(v, g.inv_dpix) : d_div(v, g.d_pix);
 }
 
+// a / b rounded to nearest, given y = RN(1 / b): q0 = RN(a y) is within an
+// ulp of a / b, r = a - b q0 is exact (one FMA), and RN(q0 + r y) is the
+// correctly rounded quotient (Markstein's theorem; Muller et al., Handbook of
+// Floating-Point Arithmetic, division with a fused multiply-add).  Three FP64
+// operations per quotient once y is known; finite, normal operands only.
+#ifndef VG_SID_RCP
+#define VG_SID_RCP 1
+#endif
+__device__ __forceinline__ double div_by(double a, double b, double y) {
+#if VG_SID_RCP
+    const double q0 = __dmul_rn(a, y);
+    const double r = __fma_rn(-b, q0, a);
+    return __fma_rn(r, y, q0);
+#else
+    return d_div(a, b);
+#endif
+}
+
+__device__ __forceinline__ double rcp_of(double b) {
+#if VG_SID_RCP
+    return b != 0.0 ? __drcp_rn(b) : 0.0;
+#else
+    return 0.0;
+#endif
+}
+
 struct Ray {
     double x0, y0, t0, t1;
+    double rdx, rdy;  // RN(1 / dx), RN(1 / dy)
     bool valid;
 };
 
@@ -45,9 +72,11 @@ __device__ __forceinline__ Ray ray_setup(const SidGeom &g, int k, double dx, dou
     double det = d_mul(g.d_det, d_add((double)k - (double)g.n_dets * 0.5, 0.5));
     r.x0 = d_mul(det, -dy);
     r.y0 = d_mul(det, dx);
+    r.rdx = rcp_of(dx);
+    r.rdy = rcp_of(dy);
     double tx0 = -INFINITY, txn = INFINITY, ty0 = -INFINITY, tyn = INFINITY;
-    if (dx != 0.0) { tx0 = d_div(d_sub(g.xb0, r.x0), dx); txn = d_div(d_sub(g.xbn, r.x0), dx); }
-    if (dy != 0.0) { ty0 = d_div(d_sub(g.yb0, r.y0), dy); tyn = d_div(d_sub(g.ybn, r.y0), dy); }
+    if (dx != 0.0) { tx0 = div_by(d_sub(g.xb0, r.x0), dx, r.rdx); txn = div_by(d_sub(g.xbn, r.x0), dx, r.rdx); }
+    if (dy != 0.0) { ty0 = div_by(d_sub(g.yb0, r.y0), dy, r.rdy); tyn = div_by(d_sub(g.ybn, r.y0), dy, r.rdy); }
     r.t0 = fmax(fmin(tx0, txn), fmin(ty0, tyn));
     r.t1 = fmin(fmax(tx0, txn), fmax(ty0, tyn));
     r.valid = !(r.t1 <= r.t0 || isinf(r.t0) || isinf(r.t1));
@@ -56,21 +85,22 @@ __device__ __forceinline__ Ray ray_setup(const SidGeom &g, int k, double dx, dou
 
 // Crossing parameter of the j-th plane in traversal order (t non-decreasing
 // in j): index i = j when the direction component is positive, n - j else.
-__device__ __forceinline__ double cross_t(double d_pix, int n, int j, bool pos, double o, double d) {
+__device__ __forceinline__ double cross_t(double d_pix, int n, int j, bool pos, double o, double d,
+                                          double rd) {
     int i = pos ? j : n - j;
-    return d_div(d_sub(edge(d_pix, i, n), o), d);
+    return div_by(d_sub(edge(d_pix, i, n), o), d, rd);
 }
 
 // First traversal index whose crossing is >= t0 (n + 1 when none).
-__device__ int first_crossing(double d_pix, int n, bool pos, double o, double d, double t0,
-                              double b0) {
+__device__ int first_crossing(double d_pix, int n, bool pos, double o, double d, double rd,
+                              double t0, double b0) {
     double p = d_add(o, d_mul(t0, d));
     double fi = floor((p - b0) / d_pix);
     int j = (int)fmin(fmax(pos ? fi : (double)n - fi, 0.0), (double)(n + 1));
     // settle on the exact boundary (a handful of steps at most)
-    for (int it = 0; it < 4 && j > 0 && cross_t(d_pix, n, j - 1, pos, o, d) >= t0; ++it) --j;
-    while (j > 0 && cross_t(d_pix, n, j - 1, pos, o, d) >= t0) --j;
-    while (j <= n && cross_t(d_pix, n, j, pos, o, d) < t0) ++j;
+    for (int it = 0; it < 4 && j > 0 && cross_t(d_pix, n, j - 1, pos, o, d, rd) >= t0; ++it) --j;
+    while (j > 0 && cross_t(d_pix, n, j - 1, pos, o, d, rd) >= t0) --j;
+    while (j <= n && cross_t(d_pix, n, j, pos, o, d, rd) < t0) ++j;
     return j;
 }
 
@@ -120,13 +150,13 @@ siddon2d_fp_kernel(SidGeom g, const float *__restrict__ img, const double *__res
         int jx = g.nx + 1, jy = g.ny + 1;
         double tx = INF, ty = INF;
         if (dx != 0.0) {
-            jx = first_crossing(g.d_pix, g.nx, px, r.x0, dx, r.t0, g.xb0);
-            if (jx <= g.nx) tx = cross_t(g.d_pix, g.nx, jx, px, r.x0, dx);
+            jx = first_crossing(g.d_pix, g.nx, px, r.x0, dx, r.rdx, r.t0, g.xb0);
+            if (jx <= g.nx) tx = cross_t(g.d_pix, g.nx, jx, px, r.x0, dx, r.rdx);
             if (tx > r.t1) tx = INF;
         }
         if (dy != 0.0) {
-            jy = first_crossing(g.d_pix, g.ny, py, r.y0, dy, r.t0, g.yb0);
-            if (jy <= g.ny) ty = cross_t(g.d_pix, g.ny, jy, py, r.y0, dy);
+            jy = first_crossing(g.d_pix, g.ny, py, r.y0, dy, r.rdy, r.t0, g.yb0);
+            if (jy <= g.ny) ty = cross_t(g.d_pix, g.ny, jy, py, r.y0, dy, r.rdy);
             if (ty > r.t1) ty = INF;
         }
         double tprev = INF;
@@ -137,12 +167,12 @@ siddon2d_fp_kernel(SidGeom g, const float *__restrict__ img, const double *__res
                 tn = tx;
                 if (tn == INF) break;
                 ++jx;
-                tx = jx <= g.nx ? cross_t(g.d_pix, g.nx, jx, px, r.x0, dx) : INF;
+                tx = jx <= g.nx ? cross_t(g.d_pix, g.nx, jx, px, r.x0, dx, r.rdx) : INF;
                 if (tx > r.t1) tx = INF;
             } else {
                 tn = ty;
                 ++jy;
-                ty = jy <= g.ny ? cross_t(g.d_pix, g.ny, jy, py, r.y0, dy) : INF;
+                ty = jy <= g.ny ? cross_t(g.d_pix, g.ny, jy, py, r.y0, dy, r.rdy) : INF;
                 if (ty > r.t1) ty = INF;
             }
             if (tprev != INF && tn > tprev) {
@@ -204,13 +234,13 @@ siddon2d_slot_gather(const float *__restrict__ buf, int npix, int S, int nvc, in
 // this pixel's neighbourhood, so this enumerates exactly the forward
 // segments: the pair is an exact transpose, degenerate rays included.
 __device__ __forceinline__ int window_crossings(double d_pix, int n, int i_lo, double o, double d,
-                                                double t0, double t1, double *out) {
+                                                double rd, double t0, double t1, double *out) {
     int c = 0;
     if (d == 0.0) return 0;
     for (int q = 0; q < 4; ++q) {
         int i = i_lo + q;
         if (i < 0 || i > n) continue;
-        double t = d_div(d_sub(edge(d_pix, i, n), o), d);
+        double t = div_by(d_sub(edge(d_pix, i, n), o), d, rd);
         if (t0 <= t && t <= t1) out[c++] = t;
     }
     // ascending order (the sequence is monotone in i; reverse when d < 0)
@@ -243,8 +273,8 @@ siddon2d_bp_kernel(SidGeom g, const float *__restrict__ sino, const double *__re
             Ray r = ray_setup(g, k, dx, dy);
             if (!r.valid) continue;
             double tx[4], ty[4], t[8];
-            int nx_ = window_crossings(g.d_pix, g.nx, ix - 1, r.x0, dx, r.t0, r.t1, tx);
-            int ny_ = window_crossings(g.d_pix, g.ny, iy - 1, r.y0, dy, r.t0, r.t1, ty);
+            int nx_ = window_crossings(g.d_pix, g.nx, ix - 1, r.x0, dx, r.rdx, r.t0, r.t1, tx);
+            int ny_ = window_crossings(g.d_pix, g.ny, iy - 1, r.y0, dy, r.rdy, r.t0, r.t1, ty);
             // merge the two ascending lists
             int a = 0, b = 0, n = 0;
             while (a < nx_ || b < ny_) {
@@ -295,6 +325,25 @@ extern "C" int vg_siddon2d_fp(const float *img, int nx, int ny, const double *tr
     siddon2d_fp_kernel<0><<<grid, 128, 0, as_stream(stream)>>>(g, img, trig, na, sino, Trace{},
                                                               Slots{nullptr, nullptr, 1, 0});
     return launch_status("siddon2d_fp");
+}
+
+namespace {
+__global__ void div_rn_check_kernel(const double *__restrict__ a, const double *__restrict__ b,
+                                    size_t n, double *__restrict__ q) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x) {
+        const double bb = b[i];
+        q[i] = div_by(a[i], bb, rcp_of(bb));
+    }
+}
+}  // namespace
+
+extern "C" int vg_div_rn_check(const double *a, const double *b, size_t n, double *q, void *stream) {
+    VG_REQUIRE(a && b && q, "div_rn_check: null pointer");
+    if (n == 0) return VG_OK;
+    const int blocks = (int)((n + 255) / 256 < 152 * 32 ? (n + 255) / 256 : 152 * 32);
+    div_rn_check_kernel<<<blocks, 256, 0, as_stream(stream)>>>(a, b, n, q);
+    return launch_status("div_rn_check");
 }
 
 extern "C" int vg_siddon2d_trace(int nx, int ny, const double *trig, int na, int n_dets,
