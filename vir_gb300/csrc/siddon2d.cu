@@ -128,14 +128,25 @@ struct Slots {
 };
 
 // MODE 0: line integrals; 1: trace (count, hash, length); 2: slot scatter.
-template <int MODE>
+// P threads (consecutive lanes) share a ray: thread `part` walks the segments
+// that start in [tau_part, tau_part+1), the ray's [t0, t1] cut in P equal
+// pieces (tau_0 = t0, tau_P = +inf).  Each starts from its first crossings at
+// or after tau_part, as the single walk starts from those at or after t0, so
+// the parts together visit the single walk's segments, each once.  MODE 0
+// adds the parts' sums in part order; the trace needs one walk (P = 1).
+#ifndef VG_SID_PARTS
+#define VG_SID_PARTS 8
+#endif
+template <int MODE, int P>
 __global__ void
 siddon2d_fp_kernel(SidGeom g, const float *__restrict__ img, const double *__restrict__ trig,
                    int na, float *__restrict__ sino, Trace tr, Slots sl) {
+    static_assert(P == 1 || (MODE != 1 && 32 % P == 0), "parts split rays in MODE 0 and 2");
     constexpr bool TRACE = MODE == 1;
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int gid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int k = gid / P, part = gid % P;
     int ia = blockIdx.y + sl.ia0;
-    if (k >= g.n_dets || ia >= na) return;
+    if (k >= g.n_dets || ia >= na) return;  // whole groups of P lanes
     const float yv = MODE == 2 ? __ldg(sl.y + (size_t)ia * g.n_dets + k) : 0.f;
     float *slot = MODE == 2 ? sl.buf + (size_t)blockIdx.y * g.nx * g.ny * sl.S + k % sl.S : nullptr;
     double dx = trig[2 * ia], dy = trig[2 * ia + 1];
@@ -146,16 +157,20 @@ siddon2d_fp_kernel(SidGeom g, const float *__restrict__ img, const double *__res
     double tlen = 0.0;
     if (r.valid) {
         const double INF = INFINITY;
+        // this part's range [tbeg, tend) of segment starts
+        const double span = d_sub(r.t1, r.t0);
+        const double tbeg = part == 0 ? r.t0 : d_add(r.t0, d_mul(span, (double)part / P));
+        const double tend = part == P - 1 ? INF : d_add(r.t0, d_mul(span, (double)(part + 1) / P));
         bool px = dx > 0.0, py = dy > 0.0;
         int jx = g.nx + 1, jy = g.ny + 1;
         double tx = INF, ty = INF;
         if (dx != 0.0) {
-            jx = first_crossing(g.d_pix, g.nx, px, r.x0, dx, r.rdx, r.t0, g.xb0);
+            jx = first_crossing(g.d_pix, g.nx, px, r.x0, dx, r.rdx, tbeg, g.xb0);
             if (jx <= g.nx) tx = cross_t(g.d_pix, g.nx, jx, px, r.x0, dx, r.rdx);
             if (tx > r.t1) tx = INF;
         }
         if (dy != 0.0) {
-            jy = first_crossing(g.d_pix, g.ny, py, r.y0, dy, r.rdy, r.t0, g.yb0);
+            jy = first_crossing(g.d_pix, g.ny, py, r.y0, dy, r.rdy, tbeg, g.yb0);
             if (jy <= g.ny) ty = cross_t(g.d_pix, g.ny, jy, py, r.y0, dy, r.rdy);
             if (ty > r.t1) ty = INF;
         }
@@ -194,7 +209,26 @@ siddon2d_fp_kernel(SidGeom g, const float *__restrict__ img, const double *__res
                 }
             }
             tprev = tn;
+            if (P > 1 && tprev >= tend) break;  // the next segment starts in the next part
         }
+    }
+    if (MODE == 0 && P > 1) {
+        // the parts' sums, added in part order by the group's first lane
+        const unsigned mask = ((1u << P) - 1u) << ((threadIdx.x & 31) & ~(P - 1));
+        float ps[P], pc[P];
+#pragma unroll
+        for (int q = 0; q < P; ++q) {
+            ps[q] = __shfl_sync(mask, acc.s, q, P);
+            pc[q] = __shfl_sync(mask, acc.c, q, P);
+        }
+        if (part != 0) return;
+        Kahan tot;
+#pragma unroll
+        for (int q = 0; q < P; ++q) {
+            tot.add(ps[q]);
+            tot.add(-pc[q]);
+        }
+        acc = tot;
     }
     size_t o = (size_t)ia * g.n_dets + k;
     if (TRACE) {
@@ -321,8 +355,8 @@ extern "C" int vg_siddon2d_fp(const float *img, int nx, int ny, const double *tr
     if (st) return st;
     VG_REQUIRE(na > 0 && na < 65536, "siddon2d_fp: na out of range");
     VG_REQUIRE(img && trig && sino, "siddon2d_fp: null pointer");
-    dim3 grid(ceil_div(n_dets, 128), na);
-    siddon2d_fp_kernel<0><<<grid, 128, 0, as_stream(stream)>>>(g, img, trig, na, sino, Trace{},
+    dim3 grid(ceil_div((long long)n_dets * VG_SID_PARTS, 128), na);
+    siddon2d_fp_kernel<0, VG_SID_PARTS><<<grid, 128, 0, as_stream(stream)>>>(g, img, trig, na, sino, Trace{},
                                                               Slots{nullptr, nullptr, 1, 0});
     return launch_status("siddon2d_fp");
 }
@@ -355,7 +389,7 @@ extern "C" int vg_siddon2d_trace(int nx, int ny, const double *trig, int na, int
     VG_REQUIRE(na > 0 && na < 65536, "siddon2d_trace: na out of range");
     VG_REQUIRE(trig && count && hash && len, "siddon2d_trace: null pointer");
     dim3 grid(ceil_div(n_dets, 128), na);
-    siddon2d_fp_kernel<1><<<grid, 128, 0, as_stream(stream)>>>(g, nullptr, trig, na, nullptr,
+    siddon2d_fp_kernel<1, 1><<<grid, 128, 0, as_stream(stream)>>>(g, nullptr, trig, na, nullptr,
                                                               Trace{count, hash, len},
                                                               Slots{nullptr, nullptr, 1, 0});
     return launch_status("siddon2d_trace");
@@ -413,8 +447,8 @@ extern "C" int vg_siddon2d_bp_scatter(const float *sino, int na, int n_dets, con
         const int nv = na - ia0 < nvc ? na - ia0 : nvc;
         cudaError_t e = cudaMemsetAsync(buf, 0, (size_t)nv * per_view, s);
         if (e != cudaSuccess) return cuda_status(e, "siddon2d_bp_scatter: clear");
-        dim3 grid(ceil_div(n_dets, 128), nv);
-        siddon2d_fp_kernel<2><<<grid, 128, 0, s>>>(g, nullptr, trig, na, nullptr, Trace{},
+        dim3 grid(ceil_div((long long)n_dets * VG_SID_PARTS, 128), nv);
+        siddon2d_fp_kernel<2, VG_SID_PARTS><<<grid, 128, 0, s>>>(g, nullptr, trig, na, nullptr, Trace{},
                                                      Slots{sino, buf, S, ia0});
         st = launch_status("siddon2d_bp_scatter");
         if (st) return st;
