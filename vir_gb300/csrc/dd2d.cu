@@ -37,6 +37,10 @@
 
 // Edge projections divide with __fdividef (reciprocal + multiply, 2 ulp)
 // unless built with -DVG_FAST_DIV=0 (IEEE division).
+#ifndef VG_SIRT_FUSED_TABLES
+#define VG_SIRT_FUSED_TABLES 1
+#endif
+
 #ifndef VG_FAST_DIV
 #define VG_FAST_DIV 1
 #endif
@@ -154,8 +158,83 @@ constexpr int FP_NVARIANTS = sizeof(FP_VARIANTS) / sizeof(FP_VARIANTS[0]);
 __host__ __device__ __forceinline__ int pad_idx(int m) { return m + (m >> 4); }
 __host__ __device__ inline int fp_line_entries(int nd) { return pad_idx(nd + 1) + 1; }
 
+struct BpWork {
+    float2 *ts;  // [na][nu + 1]: (T_j - j du sino_j, du sino_j)
+    float *scl;  // [na][scl_stride]: signed line scale for the view's driving axis
+};
+
+// scale rows hold max(nx, ny) lines, padded to an even count so that a
+// pixel patch reads its two lines as one 8-byte load
+__host__ __device__ inline int scl_stride(const vg_dd2d_geom &g) {
+    const int nm = g.nx > g.ny ? g.nx : g.ny;
+    return nm + (nm & 1);
+}
+
+size_t bp_ws_ts_bytes(const vg_dd2d_geom *g) {
+    return ((size_t)g->na * (g->nu + 1) * sizeof(float2) + 255) & ~(size_t)255;
+}
+size_t bp_ws_bytes(const vg_dd2d_geom *g) {
+    return bp_ws_ts_bytes(g) + (((size_t)g->na * scl_stride(*g) * sizeof(float) + 255) & ~(size_t)255);
+}
+BpWork bp_ws(const vg_dd2d_geom *g, void *ws) {
+    BpWork w;
+    w.ts = reinterpret_cast<float2 *>(ws);
+    w.scl = reinterpret_cast<float *>(reinterpret_cast<char *>(ws) + bp_ws_ts_bytes(g));
+    return w;
+}
+
+// Prefix table of view ia's sinogram row (row[j], global or shared memory)
+// and the view's line scales, by one block of 256 threads.
+template <bool FAN>
+__device__ __forceinline__ void bp_prep_view(const vg_dd2d_geom &g, const float *row, int ia,
+                                             const double *__restrict__ trig, BpWork w,
+                                             double *wsum) {
+    float2 *ts = w.ts + (size_t)ia * (g.nu + 1);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    // contiguous segment per thread
+    const int per = (g.nu + 255) / 256;
+    const int j0 = threadIdx.x * per;
+    double loc = 0.0;
+    for (int i = 0; i < per; ++i)
+        if (j0 + i < g.nu) loc += (double)row[j0 + i];
+    double inc = loc;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const double t = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += t;
+    }
+    if (lane == 31) wsum[warp] = inc;
+    __syncthreads();
+    double off = 0.0;
+    for (int q = 0; q < warp; ++q) off += wsum[q];
+    double run = off + inc - loc;
+    const double du = (double)g.du;
+    for (int i = 0; i < per; ++i) {
+        const int j = j0 + i;
+        if (j < g.nu) {
+            const float sv = row[j];
+            ts[j] = make_float2((float)((run - (double)j * (double)sv) * du), g.du * sv);
+            run += (double)sv;
+        }
+    }
+    if (threadIdx.x == 255) ts[g.nu] = make_float2((float)(run * du), 0.f);
+    // line scales of this view, negated for lines whose edges project in
+    // decreasing order (the pixel's interval is then [P(b+1), P(b)])
+    const ViewGeo v = view_geo(trig, ia);
+    const int no = v.xdrv ? g.ny : g.nx;
+    const int nd = v.xdrv ? g.nx : g.ny;
+    for (int io = threadIdx.x; io < no; io += 256) {
+        const Line L = line_geo<FAN>(g, v, centre_coord(g.d_pix, io, no));
+        const float P0 = proj<FAN>(g, v, L.cp, L.co, edge_coord(g.d_pix, 0, nd));
+        const float P1 = proj<FAN>(g, v, L.cp, L.co, edge_coord(g.d_pix, nd, nd));
+        w.scl[(size_t)ia * scl_stride(g) + io] = P1 >= P0 ? L.scl : -L.scl;
+    }
+}
+
 // mode 0: out = FP;  mode 1 (SIRT residual): out = (y - FP) * inv_w, or FP
-// where inv_w == 0.
+// where inv_w == 0;  mode 2: mode 1, and the block (256 threads, all bins of
+// the view) then writes the view's back-projection table and line scales
+// into pw, as dd2d_bp_prep would from the residual row.
 template <bool FAN, int FP_WARPS, int FP_MAXB, bool GUARD>
 #ifndef VG_FP_MINB8
 #define VG_FP_MINB8 3
@@ -164,7 +243,7 @@ template <bool FAN, int FP_WARPS, int FP_MAXB, bool GUARD>
 __global__ void __launch_bounds__(FP_WARPS * 32, ((FP_MAXB > 24 || (GUARD && FP_MAXB == 24)) ? 1 : (FP_WARPS >= 8 ? (FP_MAXB == 24 ? VG_FP_MINB8 : 2) : 16 / FP_WARPS)))
 dd2d_fp_kernel(vg_dd2d_geom g, const float *__restrict__ img, const float *__restrict__ imgT,
                const double *__restrict__ trig, float *__restrict__ out, int mode,
-               const float *__restrict__ y, const float *__restrict__ inv_w) {
+               const float *__restrict__ y, const float *__restrict__ inv_w, BpWork pw) {
     constexpr int FP_BINS = 32 * FP_MAXB;  // bins per block
     extern __shared__ float2 smem2[];
     __shared__ float2 UC[FP_BINS + 32];  // per bin edge (U, C(U)); entries past nb repeat nb
@@ -333,17 +412,24 @@ dd2d_fp_kernel(vg_dd2d_geom g, const float *__restrict__ img, const float *__res
     for (int i = 0; i < FP_MAXB; ++i) red[warp * FP_BINS + lane + 32 * i] = acc[i];
     __syncthreads();
     const float f = g.d_pix / g.du;
+    float *resid = reinterpret_cast<float *>(UC);  // mode 2: the residual row (UC is no longer read)
     for (int e = threadIdx.x; e < nb; e += FP_WARPS * 32) {
         float sum = 0.f;
 #pragma unroll
         for (int w = 0; w < FP_WARPS; ++w) sum += red[w * FP_BINS + e];
         float fp = sum * f;
         const size_t o = (size_t)ia * g.nu + jbase + e;
-        if (mode == 1) {
+        if (mode >= 1) {
             const float wi = inv_w[o];
             fp = (wi != 0.f) ? (y[o] - fp) * wi : fp;
         }
         out[o] = fp;
+        if (FP_WARPS == 8 && mode == 2) resid[e] = fp;
+    }
+    if (FP_WARPS == 8 && mode == 2) {
+        __shared__ double wsum[8];
+        __syncthreads();
+        bp_prep_view<FAN>(g, resid, ia, trig, pw, wsum);
     }
 }
 
@@ -379,30 +465,6 @@ constexpr int BP_TY = VG_BP_TY;  // pixels along y (threadIdx.x, contiguous in i
 constexpr int BP_TX = VG_BP_TX;  // pixels along x (threadIdx.y)
 constexpr int BP_VC = (BP_TY * BP_TX < 128) ? BP_TY * BP_TX : 128;  // views staged per chunk
 
-struct BpWork {
-    float2 *ts;  // [na][nu + 1]: (T_j - j du sino_j, du sino_j)
-    float *scl;  // [na][scl_stride]: signed line scale for the view's driving axis
-};
-
-// scale rows hold max(nx, ny) lines, padded to an even count so that a
-// pixel patch reads its two lines as one 8-byte load
-__host__ __device__ inline int scl_stride(const vg_dd2d_geom &g) {
-    const int nm = g.nx > g.ny ? g.nx : g.ny;
-    return nm + (nm & 1);
-}
-
-size_t bp_ws_ts_bytes(const vg_dd2d_geom *g) {
-    return ((size_t)g->na * (g->nu + 1) * sizeof(float2) + 255) & ~(size_t)255;
-}
-size_t bp_ws_bytes(const vg_dd2d_geom *g) {
-    return bp_ws_ts_bytes(g) + (((size_t)g->na * scl_stride(*g) * sizeof(float) + 255) & ~(size_t)255);
-}
-BpWork bp_ws(const vg_dd2d_geom *g, void *ws) {
-    BpWork w;
-    w.ts = reinterpret_cast<float2 *>(ws);
-    w.scl = reinterpret_cast<float *>(reinterpret_cast<char *>(ws) + bp_ws_ts_bytes(g));
-    return w;
-}
 
 // One block per view: prefix table of the sinogram row and line scales.
 template <bool FAN>
@@ -410,48 +472,7 @@ __global__ void __launch_bounds__(256)
 dd2d_bp_prep(vg_dd2d_geom g, const float *__restrict__ sino, const double *__restrict__ trig,
              BpWork w) {
     __shared__ double wsum[8];
-    const int ia = blockIdx.x;
-    const float *row = sino + (size_t)ia * g.nu;
-    float2 *ts = w.ts + (size_t)ia * (g.nu + 1);
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    // contiguous segment per thread
-    const int per = (g.nu + 255) / 256;
-    const int j0 = threadIdx.x * per;
-    double loc = 0.0;
-    for (int i = 0; i < per; ++i)
-        if (j0 + i < g.nu) loc += (double)__ldg(row + j0 + i);
-    double inc = loc;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const double t = __shfl_up_sync(0xffffffffu, inc, o);
-        if (lane >= o) inc += t;
-    }
-    if (lane == 31) wsum[warp] = inc;
-    __syncthreads();
-    double off = 0.0;
-    for (int q = 0; q < warp; ++q) off += wsum[q];
-    double run = off + inc - loc;
-    const double du = (double)g.du;
-    for (int i = 0; i < per; ++i) {
-        const int j = j0 + i;
-        if (j < g.nu) {
-            const float sv = __ldg(row + j);
-            ts[j] = make_float2((float)((run - (double)j * (double)sv) * du), g.du * sv);
-            run += (double)sv;
-        }
-    }
-    if (threadIdx.x == 255) ts[g.nu] = make_float2((float)(run * du), 0.f);
-    // line scales of this view, negated for lines whose edges project in
-    // decreasing order (the pixel's interval is then [P(b+1), P(b)])
-    const ViewGeo v = view_geo(trig, ia);
-    const int no = v.xdrv ? g.ny : g.nx;
-    const int nd = v.xdrv ? g.nx : g.ny;
-    for (int io = threadIdx.x; io < no; io += 256) {
-        const Line L = line_geo<FAN>(g, v, centre_coord(g.d_pix, io, no));
-        const float P0 = proj<FAN>(g, v, L.cp, L.co, edge_coord(g.d_pix, 0, nd));
-        const float P1 = proj<FAN>(g, v, L.cp, L.co, edge_coord(g.d_pix, nd, nd));
-        w.scl[(size_t)ia * scl_stride(g) + io] = P1 >= P0 ? L.scl : -L.scl;
-    }
+    bp_prep_view<FAN>(g, sino + (size_t)blockIdx.x * g.nu, blockIdx.x, trig, w, wsum);
 }
 
 __device__ __forceinline__ float rcp_approx(float x) {
@@ -595,7 +616,8 @@ int check_geom(const vg_dd2d_geom *g) {
 
 template <bool FAN, int W, int B>
 int launch_fp_t(const vg_dd2d_geom *g, const float *img, const float *imgT, const double *trig,
-                float *out, int mode, const float *y, const float *inv_w, cudaStream_t st) {
+                float *out, int mode, const float *y, const float *inv_w, cudaStream_t st,
+                BpWork pw) {
     const int nd = g->nx > g->ny ? g->nx : g->ny;
     size_t smem = (size_t)W * fp_line_entries(nd) * sizeof(float2);
     const size_t red = (size_t)W * 32 * B * sizeof(float);
@@ -615,7 +637,7 @@ int launch_fp_t(const vg_dd2d_geom *g, const float *img, const float *imgT, cons
         attr[guard] = smem;
     }
     dim3 grid(ceil_div(g->nu, 32 * B), g->na);
-    kern<<<grid, W * 32, smem, st>>>(*g, img, imgT, trig, out, mode, y, inv_w);
+    kern<<<grid, W * 32, smem, st>>>(*g, img, imgT, trig, out, mode, y, inv_w, pw);
     return launch_status("dd2d_fp");
 }
 
@@ -632,36 +654,47 @@ int fp_variant_for(const vg_dd2d_geom *g) {
 template <bool FAN>
 int launch_fp_fan(int v, const vg_dd2d_geom *g, const float *img, const float *imgT,
                   const double *trig, float *out, int mode, const float *y, const float *inv_w,
-                  cudaStream_t st) {
+                  cudaStream_t st, BpWork pw) {
     switch (v) {
-        case 1: return launch_fp_t<FAN, 8, 6>(g, img, imgT, trig, out, mode, y, inv_w, st);
-        case 2: return launch_fp_t<FAN, 8, 12>(g, img, imgT, trig, out, mode, y, inv_w, st);
-        case 3: return launch_fp_t<FAN, 8, 24>(g, img, imgT, trig, out, mode, y, inv_w, st);
-        case 4: return launch_fp_t<FAN, 4, 24>(g, img, imgT, trig, out, mode, y, inv_w, st);
-        case 5: return launch_fp_t<FAN, 4, 48>(g, img, imgT, trig, out, mode, y, inv_w, st);
-        case 6: return launch_fp_t<FAN, 2, 48>(g, img, imgT, trig, out, mode, y, inv_w, st);
+        case 1: return launch_fp_t<FAN, 8, 6>(g, img, imgT, trig, out, mode, y, inv_w, st, pw);
+        case 2: return launch_fp_t<FAN, 8, 12>(g, img, imgT, trig, out, mode, y, inv_w, st, pw);
+        case 3: return launch_fp_t<FAN, 8, 24>(g, img, imgT, trig, out, mode, y, inv_w, st, pw);
+        case 4: return launch_fp_t<FAN, 4, 24>(g, img, imgT, trig, out, mode, y, inv_w, st, pw);
+        case 5: return launch_fp_t<FAN, 4, 48>(g, img, imgT, trig, out, mode, y, inv_w, st, pw);
+        case 6: return launch_fp_t<FAN, 2, 48>(g, img, imgT, trig, out, mode, y, inv_w, st, pw);
         default: VG_REQUIRE(false, "dd2d_fp: variant %d out of range 0..%d", v, FP_NVARIANTS);
     }
 }
 
 int launch_fp(const vg_dd2d_geom *g, const float *img, const float *imgT, const double *trig,
-              float *out, int mode, const float *y, const float *inv_w, cudaStream_t st) {
+              float *out, int mode, const float *y, const float *inv_w, cudaStream_t st,
+              BpWork pw = BpWork{nullptr, nullptr}) {
     const int v = g->variant ? g->variant : fp_variant_for(g);
-    return g->fan ? launch_fp_fan<true>(v, g, img, imgT, trig, out, mode, y, inv_w, st)
-                  : launch_fp_fan<false>(v, g, img, imgT, trig, out, mode, y, inv_w, st);
+    return g->fan ? launch_fp_fan<true>(v, g, img, imgT, trig, out, mode, y, inv_w, st, pw)
+                  : launch_fp_fan<false>(v, g, img, imgT, trig, out, mode, y, inv_w, st, pw);
+}
+
+// The SIRT forward projection can also write the back projection's tables
+// (mode 2) when one block of 8 warps holds all bins of a view.
+bool fp_builds_bp_tables(const vg_dd2d_geom *g) {
+    const int v = g->variant ? g->variant : fp_variant_for(g);
+    if (v < 1 || v > FP_NVARIANTS) return false;
+    return FP_VARIANTS[v - 1].warps == 8 && 32 * FP_VARIANTS[v - 1].maxb >= g->nu;
 }
 
 int launch_bp(const vg_dd2d_geom *g, const float *sino, const double *trig, float *img, int mode,
               const float *inv_w, float gamma, float *xT, void *ws, size_t ws_bytes,
-              cudaStream_t st) {
+              cudaStream_t st, bool prep = true) {
     VG_REQUIRE(ws != nullptr && ws_bytes >= bp_ws_bytes(g),
                "dd2d_bp: workspace of %zu bytes needed (vg_dd2d_workspace_bytes)", bp_ws_bytes(g));
     VG_REQUIRE(((uintptr_t)ws & 255) == 0, "dd2d_bp: workspace must be 256-byte aligned");
     const BpWork w = bp_ws(g, ws);
-    if (g->fan) dd2d_bp_prep<true><<<g->na, 256, 0, st>>>(*g, sino, trig, w);
-    else        dd2d_bp_prep<false><<<g->na, 256, 0, st>>>(*g, sino, trig, w);
-    int s = launch_status("dd2d_bp_prep");
-    if (s) return s;
+    if (prep) {
+        if (g->fan) dd2d_bp_prep<true><<<g->na, 256, 0, st>>>(*g, sino, trig, w);
+        else        dd2d_bp_prep<false><<<g->na, 256, 0, st>>>(*g, sino, trig, w);
+        int s = launch_status("dd2d_bp_prep");
+        if (s) return s;
+    }
     dim3 grid(ceil_div(g->ny, 2 * BP_TY), ceil_div(g->nx, 2 * BP_TX));
     VG_REQUIRE(grid.y < 65536, "dd2d_bp: nx too large");
     dim3 block(BP_TY, BP_TX);
@@ -710,9 +743,16 @@ extern "C" int vg_dd2d_sirt_iter(const vg_dd2d_geom *g, const float *y, const fl
     if (st) return st;
     VG_REQUIRE(y && inv_w_sino && inv_w_img && trig && x && xT && r, "dd2d_sirt_iter: null pointer");
     cudaStream_t s = as_stream(stream);
-    st = launch_fp(g, x, xT, trig, r, 1, y, inv_w_sino, s);
+    VG_REQUIRE(workspace != nullptr && workspace_bytes >= bp_ws_bytes(g),
+               "dd2d_sirt_iter: workspace of %zu bytes needed (vg_dd2d_workspace_bytes)",
+               bp_ws_bytes(g));
+    VG_REQUIRE(((uintptr_t)workspace & 255) == 0, "dd2d_sirt_iter: workspace must be 256-byte aligned");
+    // the residual's back-projection tables come from the forward projection's
+    // epilogue when its block holds whole views (no separate table launch)
+    const bool fused = VG_SIRT_FUSED_TABLES && fp_builds_bp_tables(g);
+    st = launch_fp(g, x, xT, trig, r, fused ? 2 : 1, y, inv_w_sino, s, bp_ws(g, workspace));
     if (st) return st;
-    return launch_bp(g, r, trig, x, 1, inv_w_img, gamma, xT, workspace, workspace_bytes, s);
+    return launch_bp(g, r, trig, x, 1, inv_w_img, gamma, xT, workspace, workspace_bytes, s, !fused);
 }
 
 // ---------------------------------------------------------------------------
