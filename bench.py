@@ -743,6 +743,8 @@ def main():
 
     # ---- per-kernel timing of the two fused kernels (same stream, events) --
     g = sirt.g
+    from vir_gb300 import _lib
+    launches_per_update = _lib.load().vg_dd2d_sirt_launches(ctypes.byref(g))
     reps = 20
     e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
     fp_ms, bp_ms = [], []
@@ -823,7 +825,7 @@ def main():
                      "algorithmic_bytes_per_launch": alg_bytes, "peak_source": peak_src},
         "e2e": {"value": e2e_val, "unit": "iter/s", "h2d_bytes_per_step": int(y.nbytes),
                 "d2h_bytes_per_step": int(img.nbytes)},
-        "gpu_launches": K * U * 3,                        # FP, BP prefix table, BP per update
+        "gpu_launches": K * U * launches_per_update,      # library kernels per update (2 or 3)
         "clocks": clk.summary(),
     }
     if rank == 0 and not args.no_cpu_baseline:

@@ -211,6 +211,12 @@ int vg_dd2d_sirt_iter(const vg_dd2d_geom *g, const float *y,
                       float *r, void *workspace, size_t workspace_bytes,
                       void *stream);
 
+/* Kernel launches vg_dd2d_sirt_iter makes per update for this geometry: 2
+ * when the forward projection's epilogue writes the back projection's
+ * tables (one block of 8 warps holds all bins of a view), else 3; 0 for a
+ * geometry vg_dd2d_sirt_iter rejects. */
+int vg_dd2d_sirt_launches(const vg_dd2d_geom *g);
+
 /* Pixel-driven FBP backprojection of a ramp-filtered sinogram q (na, nu)
  * (filtered by vg_filter_rows, i.e. filtration.filter_sino's 2H):
  *   img(x, y) = pi / (2 na) * sum_views q(s(x, y)) / U(x, y)^2,

@@ -162,6 +162,8 @@ def load(build_if_missing: bool = True):
         L.vg_dd2d_fp_variants.restype = c_int
         L.vg_dd2d_fp_default_variant.argtypes = [ctypes.POINTER(DD2DGeom)]
         L.vg_dd2d_fp_default_variant.restype = c_int
+        L.vg_dd2d_sirt_launches.argtypes = [ctypes.POINTER(DD2DGeom)]
+        L.vg_dd2d_sirt_launches.restype = c_int
         L.vg_dd2d_workspace_bytes.argtypes = [ctypes.POINTER(DD2DGeom)]
         L.vg_dd2d_workspace_bytes.restype = c_size_t
         L.vg_dd3d_workspace_bytes.argtypes = [ctypes.POINTER(DD3DGeom)]
@@ -192,7 +194,7 @@ def call(name, *args):
 def exported_symbols():
     return list(_PROTOS) + ["vg_version", "vg_last_error", "vg_status_string",
                             "vg_dd2d_workspace_bytes", "vg_dd2d_noalloc_scratch_bytes",
-                            "vg_dd2d_fp_variants", "vg_dd2d_fp_default_variant",
+                            "vg_dd2d_fp_variants", "vg_dd2d_fp_default_variant", "vg_dd2d_sirt_launches",
                             "vg_list_bp_workspace_bytes", "vg_dd3d_workspace_bytes",
                             "vg_dd_square_workspace_bytes", "vg_compact_blocks",
                             "vg_siddon2d_bp_workspace_bytes"]

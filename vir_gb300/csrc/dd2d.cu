@@ -755,6 +755,11 @@ extern "C" int vg_dd2d_sirt_iter(const vg_dd2d_geom *g, const float *y, const fl
     return launch_bp(g, r, trig, x, 1, inv_w_img, gamma, xT, workspace, workspace_bytes, s, !fused);
 }
 
+extern "C" int vg_dd2d_sirt_launches(const vg_dd2d_geom *g) {
+    if (check_geom(g) != VG_OK) return 0;
+    return (VG_SIRT_FUSED_TABLES && fp_builds_bp_tables(g)) ? 2 : 3;
+}
+
 // ---------------------------------------------------------------------------
 // Allocation-free backprojection.
 //
