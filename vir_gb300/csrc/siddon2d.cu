@@ -134,6 +134,9 @@ struct Slots {
 // or after tau_part, as the single walk starts from those at or after t0, so
 // the parts together visit the single walk's segments, each once.  MODE 0
 // adds the parts' sums in part order; the trace needs one walk (P = 1).
+#ifndef VG_SID_TRAV
+#define VG_SID_TRAV 1
+#endif
 #ifndef VG_SID_PARTS
 #define VG_SID_PARTS 8
 #endif
@@ -175,38 +178,76 @@ siddon2d_fp_kernel(SidGeom g, const float *__restrict__ img, const double *__res
             if (ty > r.t1) ty = INF;
         }
         double tprev = INF;
+        // A segment's voxel is vir's floor of its midpoint.  The midpoint lies at
+        // least h |d| / 2 (h = tn - tprev) from the cell's boundaries along each
+        // axis (less the crossings' own rounding), and its computed coordinates
+        // are within a few FP64 ulps of L = the ray's largest coordinate or
+        // parameter magnitude, so when h |dx| and h |dy| both exceed 1e-9 L the
+        // floors are the cell the walk is in: the walk's cell (cx, cy), set from
+        // the floors of the first such segment and stepped at every crossing,
+        // is used; shorter segments (and rays nearly along an axis) take the
+        // floors.
+        const double L = 1.0 + fabs(r.t0) + fabs(r.t1) + fabs(r.x0) + fabs(r.y0) + fabs(g.xb0) +
+                         fabs(g.yb0);
+        const double thr = VG_SID_TRAV ? 1e-9 * L * fmax(fabs(r.rdx), fabs(r.rdy)) : INF;
+        int cx = 0, cy = 0;
+        bool walk_cell = false;
+        const int sx = px ? 1 : -1, sy = py ? 1 : -1;
         // bounded: every step consumes one of nx + ny + 2 crossings
         for (int step = 0; step < g.nx + g.ny + 4; ++step) {
             double tn;
+            bool xcross;
             if (tx <= ty) {
                 tn = tx;
                 if (tn == INF) break;
+                xcross = true;
                 ++jx;
                 tx = jx <= g.nx ? cross_t(g.d_pix, g.nx, jx, px, r.x0, dx, r.rdx) : INF;
                 if (tx > r.t1) tx = INF;
             } else {
                 tn = ty;
+                xcross = false;
                 ++jy;
                 ty = jy <= g.ny ? cross_t(g.d_pix, g.ny, jy, py, r.y0, dy, r.rdy) : INF;
                 if (ty > r.t1) ty = INF;
             }
             if (tprev != INF && tn > tprev) {
-                double m = d_mul(0.5, d_add(tprev, tn));
-                double fx = floor(div_pix(g, d_sub(d_add(r.x0, d_mul(m, dx)), g.xb0)));
-                double fy = floor(div_pix(g, d_sub(d_add(r.y0, d_mul(m, dy)), g.yb0)));
-                if (fx >= 0.0 && fx < g.nx && fy >= 0.0 && fy < g.ny) {
-                    size_t pix = (size_t)fx * g.ny + (int)fy;
+                const double h = d_sub(tn, tprev);
+                int ix, iy;
+                if (walk_cell && h > thr) {
+                    ix = cx;
+                    iy = cy;
+                } else {
+                    double m = d_mul(0.5, d_add(tprev, tn));
+                    double fx = floor(div_pix(g, d_sub(d_add(r.x0, d_mul(m, dx)), g.xb0)));
+                    double fy = floor(div_pix(g, d_sub(d_add(r.y0, d_mul(m, dy)), g.yb0)));
+                    // outside the grid by more than the int range: no voxel
+                    ix = fx >= 0.0 && fx < g.nx ? (int)fx : -1;
+                    iy = fy >= 0.0 && fy < g.ny ? (int)fy : -1;
+                    if (!walk_cell && h > thr) {
+                        walk_cell = true;
+                        cx = (int)fmax(fmin(fx, 1e9), -1e9);
+                        cy = (int)fmax(fmin(fy, 1e9), -1e9);
+                    }
+                }
+                if (ix >= 0 && ix < g.nx && iy >= 0 && iy < g.ny) {
+                    size_t pix = (size_t)ix * g.ny + iy;
                     if (TRACE) {
                         ++tcount;
                         thash = trace_mix(thash, pix);
-                        tlen = d_add(tlen, d_sub(tn, tprev));
+                        tlen = d_add(tlen, h);
                     } else if (MODE == 2) {
-                        slot[pix * sl.S] += __fmul_rn(yv, (float)d_sub(tn, tprev));
+                        slot[pix * sl.S] += __fmul_rn(yv, (float)h);
                     } else {
-                        float w = (float)d_sub(tn, tprev);
+                        float w = (float)h;
                         acc.add(__fmul_rn(__ldg(img + pix), w));
                     }
                 }
+            }
+            // the crossing moves the walk into the next cell along its axis
+            if (walk_cell) {
+                if (xcross) cx += sx;
+                else cy += sy;
             }
             tprev = tn;
             if (P > 1 && tprev >= tend) break;  // the next segment starts in the next part
