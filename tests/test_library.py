@@ -48,6 +48,25 @@ def test_argument_errors_without_gpu():
     assert b"positive" in L.vg_last_error()
 
 
+def test_sirt_launch_count_without_gpu():
+    """vg_dd2d_sirt_launches (host-only): 2 launches per SIRT update when one
+    8-warp block holds all bins of a view (the forward projection then writes
+    the back projection's tables), 3 otherwise, 0 for a rejected geometry."""
+    from vir_gb300 import _lib
+    L = _lib.load()
+    # the fan SIRT benchmark geometry: 512^2, 720 views, 768 bins (8 warps x 24 bins)
+    g = _lib.DD2DGeom(512, 512, 720, 768, 1.2, 0.0, 0.9, 500.0, 1000.0, 1, 0)
+    assert L.vg_dd2d_sirt_launches(ctypes.byref(g)) == 2
+    # 1024^2 with 1536 bins: 4-warp tiles, the table kernel runs separately
+    g = _lib.DD2DGeom(1024, 1024, 90, 1536, 1.0, 0.0, 1.0, 0.0, 0.0, 0, 0)
+    assert L.vg_dd2d_sirt_launches(ctypes.byref(g)) == 3
+    # an explicit 8-warp variant (6 bins per lane) whose block covers half of the bins
+    g = _lib.DD2DGeom(256, 256, 90, 384, 1.0, 0.0, 1.0, 0.0, 0.0, 0, 1)
+    assert L.vg_dd2d_sirt_launches(ctypes.byref(g)) == 3
+    g = _lib.DD2DGeom(0, 256, 90, 384, 1.0, 0.0, 1.0, 0.0, 0.0, 0, 0)
+    assert L.vg_dd2d_sirt_launches(ctypes.byref(g)) == 0
+
+
 def test_drop_in_table_resolves_and_installs():
     """Every vir function named in the drop-in table exists here, and
     install_into replaces it in an imported vir package (a stand-in tree of
