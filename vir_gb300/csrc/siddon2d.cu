@@ -85,22 +85,36 @@ __device__ __forceinline__ Ray ray_setup(const SidGeom &g, int k, double dx, dou
 
 // Crossing parameter of the j-th plane in traversal order (t non-decreasing
 // in j): index i = j when the direction component is positive, n - j else.
+// The plane position is edge(d_pix, i, n), read from `et` (a table of the
+// same values) when given.
 __device__ __forceinline__ double cross_t(double d_pix, int n, int j, bool pos, double o, double d,
-                                          double rd) {
+                                          double rd, const double *et = nullptr) {
     int i = pos ? j : n - j;
-    return div_by(d_sub(edge(d_pix, i, n), o), d, rd);
+    const double e = et ? et[i] : edge(d_pix, i, n);
+    return div_by(d_sub(e, o), d, rd);
 }
 
 // First traversal index whose crossing is >= t0 (n + 1 when none).
 __device__ int first_crossing(double d_pix, int n, bool pos, double o, double d, double rd,
-                              double t0, double b0) {
+                              double t0, double b0, const double *et = nullptr) {
     double p = d_add(o, d_mul(t0, d));
     double fi = floor((p - b0) / d_pix);
     int j = (int)fmin(fmax(pos ? fi : (double)n - fi, 0.0), (double)(n + 1));
     // settle on the exact boundary (a handful of steps at most)
-    for (int it = 0; it < 4 && j > 0 && cross_t(d_pix, n, j - 1, pos, o, d, rd) >= t0; ++it) --j;
-    while (j > 0 && cross_t(d_pix, n, j - 1, pos, o, d, rd) >= t0) --j;
-    while (j <= n && cross_t(d_pix, n, j, pos, o, d, rd) < t0) ++j;
+    for (int it = 0; it < 4 && j > 0 && cross_t(d_pix, n, j - 1, pos, o, d, rd, et) >= t0; ++it) --j;
+    while (j > 0 && cross_t(d_pix, n, j - 1, pos, o, d, rd, et) >= t0) --j;
+    while (j <= n && cross_t(d_pix, n, j, pos, o, d, rd, et) < t0) ++j;
+    return j;
+}
+
+// Last traversal index whose crossing is <= t1 (-1 when none).
+__device__ int last_crossing(double d_pix, int n, bool pos, double o, double d, double rd,
+                             double t1, double b0, const double *et) {
+    double p = d_add(o, d_mul(t1, d));
+    double fi = floor((p - b0) / d_pix);
+    int j = (int)fmin(fmax(pos ? fi : (double)n - fi, -1.0), (double)n);
+    while (j >= 0 && cross_t(d_pix, n, j, pos, o, d, rd, et) > t1) --j;
+    while (j < n && cross_t(d_pix, n, j + 1, pos, o, d, rd, et) <= t1) ++j;
     return j;
 }
 
@@ -134,6 +148,12 @@ struct Slots {
 // or after tau_part, as the single walk starts from those at or after t0, so
 // the parts together visit the single walk's segments, each once.  MODE 0
 // adds the parts' sums in part order; the trace needs one walk (P = 1).
+#ifndef VG_SID_TAB
+#define VG_SID_TAB 1
+#endif
+#ifndef VG_SID_TAB_MAX
+#define VG_SID_TAB_MAX 2048  // plane positions held in shared memory (16 KB)
+#endif
 #ifndef VG_SID_TRAV
 #define VG_SID_TRAV 1
 #endif
@@ -146,6 +166,16 @@ siddon2d_fp_kernel(SidGeom g, const float *__restrict__ img, const double *__res
                    int na, float *__restrict__ sino, Trace tr, Slots sl) {
     static_assert(P == 1 || (MODE != 1 && 32 % P == 0), "parts split rays in MODE 0 and 2");
     constexpr bool TRACE = MODE == 1;
+    // the plane positions of both axes, once per block (the same FP64 values
+    // edge() computes), when they fit
+    __shared__ double etab[VG_SID_TAB_MAX];
+    const bool tab = VG_SID_TAB && g.nx + g.ny + 2 <= VG_SID_TAB_MAX;
+    if (tab) {
+        for (int i = threadIdx.x; i <= g.nx; i += blockDim.x) etab[i] = edge(g.d_pix, i, g.nx);
+        for (int i = threadIdx.x; i <= g.ny; i += blockDim.x) etab[g.nx + 1 + i] = edge(g.d_pix, i, g.ny);
+    }
+    __syncthreads();
+    const double *etx = tab ? etab : nullptr, *ety = tab ? etab + g.nx + 1 : nullptr;
     const int gid = blockIdx.x * blockDim.x + threadIdx.x;
     const int k = gid / P, part = gid % P;
     int ia = blockIdx.y + sl.ia0;
@@ -165,19 +195,22 @@ siddon2d_fp_kernel(SidGeom g, const float *__restrict__ img, const double *__res
         const double tbeg = part == 0 ? r.t0 : d_add(r.t0, d_mul(span, (double)part / P));
         const double tend = part == P - 1 ? INF : d_add(r.t0, d_mul(span, (double)(part + 1) / P));
         bool px = dx > 0.0, py = dy > 0.0;
-        int jx = g.nx + 1, jy = g.ny + 1;
-        double tx = INF, ty = INF;
+        // crossings jx..jx_end of the x planes (and y) lie in [tbeg, t1]
+        int jx = 0, jy = 0, jx_end = -1, jy_end = -1;
+        double tx = 0.0, ty = 0.0;
         if (dx != 0.0) {
-            jx = first_crossing(g.d_pix, g.nx, px, r.x0, dx, r.rdx, tbeg, g.xb0);
-            if (jx <= g.nx) tx = cross_t(g.d_pix, g.nx, jx, px, r.x0, dx, r.rdx);
-            if (tx > r.t1) tx = INF;
+            jx = first_crossing(g.d_pix, g.nx, px, r.x0, dx, r.rdx, tbeg, g.xb0, etx);
+            jx_end = last_crossing(g.d_pix, g.nx, px, r.x0, dx, r.rdx, r.t1, g.xb0, etx);
+            if (jx <= jx_end) tx = cross_t(g.d_pix, g.nx, jx, px, r.x0, dx, r.rdx, etx);
         }
         if (dy != 0.0) {
-            jy = first_crossing(g.d_pix, g.ny, py, r.y0, dy, r.rdy, tbeg, g.yb0);
-            if (jy <= g.ny) ty = cross_t(g.d_pix, g.ny, jy, py, r.y0, dy, r.rdy);
-            if (ty > r.t1) ty = INF;
+            jy = first_crossing(g.d_pix, g.ny, py, r.y0, dy, r.rdy, tbeg, g.yb0, ety);
+            jy_end = last_crossing(g.d_pix, g.ny, py, r.y0, dy, r.rdy, r.t1, g.yb0, ety);
+            if (jy <= jy_end) ty = cross_t(g.d_pix, g.ny, jy, py, r.y0, dy, r.rdy, ety);
         }
-        double tprev = INF;
+        bool xa = jx <= jx_end, ya = jy <= jy_end;  // axes with crossings left
+        bool have_prev = false;
+        double tprev = 0.0;
         // A segment's voxel is vir's floor of its midpoint.  The midpoint lies at
         // least h |d| / 2 (h = tn - tprev) from the cell's boundaries along each
         // axis (less the crossings' own rounding), and its computed coordinates
@@ -195,23 +228,22 @@ siddon2d_fp_kernel(SidGeom g, const float *__restrict__ img, const double *__res
         const int sx = px ? 1 : -1, sy = py ? 1 : -1;
         // bounded: every step consumes one of nx + ny + 2 crossings
         for (int step = 0; step < g.nx + g.ny + 4; ++step) {
+            if (!xa && !ya) break;
+            // the earlier crossing; ties take the x plane first
+            const bool xcross = xa && (!ya || tx <= ty);
             double tn;
-            bool xcross;
-            if (tx <= ty) {
+            if (xcross) {
                 tn = tx;
-                if (tn == INF) break;
-                xcross = true;
                 ++jx;
-                tx = jx <= g.nx ? cross_t(g.d_pix, g.nx, jx, px, r.x0, dx, r.rdx) : INF;
-                if (tx > r.t1) tx = INF;
+                xa = jx <= jx_end;
+                if (xa) tx = cross_t(g.d_pix, g.nx, jx, px, r.x0, dx, r.rdx, etx);
             } else {
                 tn = ty;
-                xcross = false;
                 ++jy;
-                ty = jy <= g.ny ? cross_t(g.d_pix, g.ny, jy, py, r.y0, dy, r.rdy) : INF;
-                if (ty > r.t1) ty = INF;
+                ya = jy <= jy_end;
+                if (ya) ty = cross_t(g.d_pix, g.ny, jy, py, r.y0, dy, r.rdy, ety);
             }
-            if (tprev != INF && tn > tprev) {
+            if (have_prev && tn > tprev) {
                 const double h = d_sub(tn, tprev);
                 int ix, iy;
                 if (walk_cell && h > thr) {
@@ -250,6 +282,7 @@ siddon2d_fp_kernel(SidGeom g, const float *__restrict__ img, const double *__res
                 else cy += sy;
             }
             tprev = tn;
+            have_prev = true;
             if (P > 1 && tprev >= tend) break;  // the next segment starts in the next part
         }
     }
