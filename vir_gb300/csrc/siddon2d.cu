@@ -94,6 +94,15 @@ __device__ __forceinline__ double cross_t(double d_pix, int n, int j, bool pos, 
     return div_by(d_sub(e, o), d, rd);
 }
 
+// The crossings' comparisons run on integers: ord64 maps doubles (no NaN)
+// to int64 in the same order, -0 and +0 alike, so x <= y <=> ord64(x) <=
+// ord64(y) (FP64 compares use the slow FP64 pipe, integer compares do not).
+__device__ __forceinline__ long long ord64(double x) {
+    long long b = __double_as_longlong(x);
+    if (b == (long long)0x8000000000000000ULL) b = 0;
+    return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
+}
+
 // First traversal index whose crossing is >= t0 (n + 1 when none).
 __device__ int first_crossing(double d_pix, int n, bool pos, double o, double d, double rd,
                               double t0, double b0, const double *et = nullptr) {
@@ -198,19 +207,28 @@ siddon2d_fp_kernel(SidGeom g, const float *__restrict__ img, const double *__res
         // crossings jx..jx_end of the x planes (and y) lie in [tbeg, t1]
         int jx = 0, jy = 0, jx_end = -1, jy_end = -1;
         double tx = 0.0, ty = 0.0;
+        long long ox = 0, oy = 0;  // ord64 of tx, ty
         if (dx != 0.0) {
             jx = first_crossing(g.d_pix, g.nx, px, r.x0, dx, r.rdx, tbeg, g.xb0, etx);
             jx_end = last_crossing(g.d_pix, g.nx, px, r.x0, dx, r.rdx, r.t1, g.xb0, etx);
-            if (jx <= jx_end) tx = cross_t(g.d_pix, g.nx, jx, px, r.x0, dx, r.rdx, etx);
+            if (jx <= jx_end) {
+                tx = cross_t(g.d_pix, g.nx, jx, px, r.x0, dx, r.rdx, etx);
+                ox = ord64(tx);
+            }
         }
         if (dy != 0.0) {
             jy = first_crossing(g.d_pix, g.ny, py, r.y0, dy, r.rdy, tbeg, g.yb0, ety);
             jy_end = last_crossing(g.d_pix, g.ny, py, r.y0, dy, r.rdy, r.t1, g.yb0, ety);
-            if (jy <= jy_end) ty = cross_t(g.d_pix, g.ny, jy, py, r.y0, dy, r.rdy, ety);
+            if (jy <= jy_end) {
+                ty = cross_t(g.d_pix, g.ny, jy, py, r.y0, dy, r.rdy, ety);
+                oy = ord64(ty);
+            }
         }
         bool xa = jx <= jx_end, ya = jy <= jy_end;  // axes with crossings left
         bool have_prev = false;
         double tprev = 0.0;
+        long long oprev = 0;
+        const long long oend = ord64(tend);
         // A segment's voxel is vir's floor of its midpoint.  The midpoint lies at
         // least h |d| / 2 (h = tn - tprev) from the cell's boundaries along each
         // axis (less the crossings' own rounding), and its computed coordinates
@@ -230,20 +248,29 @@ siddon2d_fp_kernel(SidGeom g, const float *__restrict__ img, const double *__res
         for (int step = 0; step < g.nx + g.ny + 4; ++step) {
             if (!xa && !ya) break;
             // the earlier crossing; ties take the x plane first
-            const bool xcross = xa && (!ya || tx <= ty);
+            const bool xcross = xa && (!ya || ox <= oy);
             double tn;
+            long long on;
             if (xcross) {
                 tn = tx;
+                on = ox;
                 ++jx;
                 xa = jx <= jx_end;
-                if (xa) tx = cross_t(g.d_pix, g.nx, jx, px, r.x0, dx, r.rdx, etx);
+                if (xa) {
+                    tx = cross_t(g.d_pix, g.nx, jx, px, r.x0, dx, r.rdx, etx);
+                    ox = ord64(tx);
+                }
             } else {
                 tn = ty;
+                on = oy;
                 ++jy;
                 ya = jy <= jy_end;
-                if (ya) ty = cross_t(g.d_pix, g.ny, jy, py, r.y0, dy, r.rdy, ety);
+                if (ya) {
+                    ty = cross_t(g.d_pix, g.ny, jy, py, r.y0, dy, r.rdy, ety);
+                    oy = ord64(ty);
+                }
             }
-            if (have_prev && tn > tprev) {
+            if (have_prev && on > oprev) {
                 const double h = d_sub(tn, tprev);
                 int ix, iy;
                 if (walk_cell && h > thr) {
@@ -282,8 +309,9 @@ siddon2d_fp_kernel(SidGeom g, const float *__restrict__ img, const double *__res
                 else cy += sy;
             }
             tprev = tn;
+            oprev = on;
             have_prev = true;
-            if (P > 1 && tprev >= tend) break;  // the next segment starts in the next part
+            if (P > 1 && oprev >= oend) break;  // the next segment starts in the next part
         }
     }
     if (MODE == 0 && P > 1) {
