@@ -57,26 +57,34 @@ def prepare(src, trg, nPixels=128, dPixels=1.0, origin=0.0, epsilon=1e-5):
     pN = np.array([Xb[-1], Yb[-1], Zb[-1]], dtype=np.float32)
     dST = trg - src
     distance = np.linalg.norm(dST, axis=-1)
+    # the reference's alpha range (siddon.py:681-751), each element computed as
+    # it computes it; where it evaluates both branches of np.where, only the
+    # selected operand is evaluated here (same values, elementwise)
     with np.errstate(divide="ignore", invalid="ignore"):
-        alpha0 = np.where(dST != 0.0, (p0 - src) / dST, (p0 - src) / epsilon)
-        alphaN = np.where(dST != 0.0, (pN - src) / dST, (pN - src) / epsilon)
+        den = np.where(dST != 0.0, dST, np.float32(epsilon))
+        alpha0 = (p0 - src) / den
+        alphaN = (pN - src) / den
     m_min = np.zeros(shape + (4,), dtype=np.float32)
     m_max = np.ones(shape + (4,), dtype=np.float32)
     lt, gt = alpha0 < alphaN, alpha0 > alphaN
-    m_min[..., 1:][lt] = alpha0[lt]
-    m_max[..., 1:][lt] = alphaN[lt]
-    m_min[..., 1:][gt] = alphaN[gt]
-    m_max[..., 1:][gt] = alpha0[gt]
+    m_min[..., 1:] = np.where(lt, alpha0, np.where(gt, alphaN, np.float32(0)))
+    m_max[..., 1:] = np.where(lt, alphaN, np.where(gt, alpha0, np.float32(1)))
     amin = np.max(m_min, axis=-1)
     amax = np.min(m_max, axis=-1)
-    i0p = (nP + 1) - (pN - amin[..., np.newaxis] * dST - src) / dP
-    i0n = (nP + 1) - (pN - amax[..., np.newaxis] * dST - src) / dP
-    iNp = (src + amax[..., np.newaxis] * dST - p0) / dP
-    iNn = (src + amin[..., np.newaxis] * dST - p0) / dP
-    r = lambda v, f: np.where(np.isclose(v, np.round(v), atol=epsilon), np.round(v), f(v)).astype(np.int32)
+    # first / last plane index per axis, from amin / amax by the direction's sign
+    pos = dST > 0.0
+    a_lo = np.where(pos, amin[..., np.newaxis], amax[..., np.newaxis])
+    a_hi = np.where(pos, amax[..., np.newaxis], amin[..., np.newaxis])
+    v0 = (nP + 1) - (pN - a_lo * dST - src) / dP
+    vN = (src + a_hi * dST - p0) / dP
+
+    def r(v, f):
+        rv = np.round(v)
+        return np.where(np.isclose(v, rv, atol=epsilon), rv, f(v)).astype(np.int32)
+
     with np.errstate(invalid="ignore"):  # axes with dST == 0 carry inf here, unused
-        i0 = np.where(dST > 0.0, r(i0p, np.floor), r(i0n, np.floor))
-        iN = np.where(dST > 0.0, r(iNp, np.ceil), r(iNn, np.ceil))
+        i0 = r(v0, np.floor)
+        iN = r(vN, np.ceil)
     # the reference slices g.Xb[i0:iN] (:772): normalise to numpy slice bounds
     L = (nP + 1).astype(np.int64)
     sl = lambda i: np.clip(np.where(i < 0, i + L, i), 0, L).astype(np.int32)
