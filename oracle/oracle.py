@@ -663,3 +663,53 @@ def rotsum_fp(phantom, mats):
         c = np.round(np.einsum("rk,kxyz->rxyz", m[:, :3], g) + m[:, 3, None, None, None], 6)
         out[i] = map_coordinates(phantom, c, order=1, mode="constant", cval=0.0).sum(axis=1).T
     return out
+
+
+# ---- Siddon ray-list set-up (sys_mat/siddon.py:681-751) -----------------------
+
+def siddons_setup(src, trg, nPixels, dPixels=1.0, origin=0.0, epsilon=1e-5):
+    """Per-ray set-up of ``siddons`` restated step by step as siddon.py:681-751
+    computes it (float32 grid planes and rays, both branches of every
+    ``np.where`` evaluated): the alpha range (amin, amax), the first / last
+    plane index of each axis with the ``isclose`` rounding, normalised to
+    numpy slice bounds as ``g.Xb[i0:iN]`` (:772) reads them, and the validity
+    of each ray.  Returns a dict of flat per-ray arrays (float32 / int32)."""
+    def three(v, dtype):
+        v = np.array(v, dtype=dtype)
+        return np.repeat(v, 3) if v.size == 1 else v
+
+    nP, dP, oP = three(nPixels, int), three(dPixels, np.float32), three(origin, np.float32)
+    planes = [np.linspace(-nP[a], nP[a], nP[a] + 1, dtype=np.float32) * dP[a] / 2.0 + oP[a]
+              for a in range(3)]
+    src = np.array(src, dtype=np.float32).reshape(-1, 3)
+    trg = np.array(trg, dtype=np.float32).reshape(-1, 3)
+    p0 = np.array([b[0] for b in planes], dtype=np.float32)
+    pN = np.array([b[-1] for b in planes], dtype=np.float32)
+    dST = trg - src
+    with np.errstate(divide="ignore", invalid="ignore"):
+        alpha0 = np.where(dST != 0.0, (p0 - src) / dST, (p0 - src) / epsilon)
+        alphaN = np.where(dST != 0.0, (pN - src) / dST, (pN - src) / epsilon)
+    m_min = np.zeros((len(src), 4), dtype=np.float32)
+    m_max = np.ones((len(src), 4), dtype=np.float32)
+    lt, gt = alpha0 < alphaN, alpha0 > alphaN
+    m_min[:, 1:][lt] = alpha0[lt]
+    m_max[:, 1:][lt] = alphaN[lt]
+    m_min[:, 1:][gt] = alphaN[gt]
+    m_max[:, 1:][gt] = alpha0[gt]
+    amin, amax = m_min.max(-1), m_max.min(-1)
+    first_pos = (nP + 1) - (pN - amin[:, None] * dST - src) / dP
+    first_neg = (nP + 1) - (pN - amax[:, None] * dST - src) / dP
+    last_pos = (src + amax[:, None] * dST - p0) / dP
+    last_neg = (src + amin[:, None] * dST - p0) / dP
+
+    def snap(v, f):
+        return np.where(np.isclose(v, np.round(v), atol=epsilon), np.round(v), f(v)).astype(np.int32)
+
+    with np.errstate(invalid="ignore"):
+        i0 = np.where(dST > 0.0, snap(first_pos, np.floor), snap(first_neg, np.floor))
+        iN = np.where(dST > 0.0, snap(last_pos, np.ceil), snap(last_neg, np.ceil))
+    L = (nP + 1).astype(np.int64)
+    bound = lambda i: np.clip(np.where(i < 0, i + L, i), 0, L).astype(np.int32)
+    valid = (amax > amin) & ~np.isclose(amax, amin, atol=epsilon)
+    return dict(amin=amin, amax=amax, i0=bound(i0), iN=bound(iN), valid=valid.astype(np.uint8),
+                dist=np.linalg.norm(dST, axis=-1).astype(np.float32), dst=dST)
