@@ -149,9 +149,10 @@ def dist_info():
     return rank, world, local
 
 
-def cpu_sirt_iteration_rate(img_shape, angs, y, n_iter=1):
+def cpu_sirt_iteration_rate(img_shape, angs, y, n_iter=1, want_x=False):
     """vir's algorithm on the host (FP64 C restatement, all threads): seconds
-    per SIRT update on the full workload."""
+    per SIRT update on the full workload (and the iterate after n_iter
+    updates when want_x)."""
     from oracle import oracle as orc
     w = WORKLOAD
     fp = lambda x: orc.dd_fp_fan_2d(x, angs, w["nu"], w["DSO"], w["DSD"], du=w["du"],
@@ -161,9 +162,18 @@ def cpu_sirt_iteration_rate(img_shape, angs, y, n_iter=1):
     W_sino = fp(np.ones(img_shape, np.float32))
     W_img = bp(np.ones(y.shape, np.float32))
     t0 = time.perf_counter()
-    orc.sirt(y, fp, bp, img_shape, iters=n_iter + 1, W_sino=W_sino, W_img=W_img)
+    x = orc.sirt(y, fp, bp, img_shape, iters=n_iter + 1, W_sino=W_sino, W_img=W_img)
     dt = time.perf_counter() - t0
+    if want_x:
+        return dt / n_iter, orc.num_threads(), x
     return dt / n_iter, orc.num_threads()
+
+
+def arm_config(world):
+    """The `config` record both arms print (same keys and values at the same N)."""
+    return {"workload": workload_desc(), "parallelism": f"replicas x{world}",
+            "l2": "flushed between steps (256 MiB write); inputs 3.3 MB are L2-resident "
+                  "within a step", "graph": "100 updates captured as one CUDA graph"}
 
 
 def run_reference(args):
@@ -184,7 +194,7 @@ def run_reference(args):
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": sec * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": workload_desc(), "step": "1 SIRT update (bounded sample)"},
+            "config": arm_config(world),
             "cpu_baseline": {"value": val, "unit": "iter/s", "cores": cores, "kind": "port",
                              "sample": "1 SIRT update (FP + BP) of the full 512^2 x 720-view "
                                        "workload per step, median over steps"},
@@ -741,7 +751,10 @@ def main():
     x_final = sirt.x.detach().cpu().numpy()
     rmse = float(np.sqrt(np.mean((x_final - img) ** 2)))
 
-    # ---- per-kernel timing of the two fused kernels (same stream, events) --
+    # ---- per-kernel timing of the two halves of the update, launched exactly
+    # as the captured graph launches them (the forward projection with its
+    # residual / table epilogue, the back projection with its update
+    # epilogue), CUDA events on the launch stream between them -------------
     g = sirt.g
     from vir_gb300 import _lib
     launches_per_update = _lib.load().vg_dd2d_sirt_launches(ctypes.byref(g))
@@ -750,17 +763,21 @@ def main():
     fp_ms, bp_ms = [], []
     for i in range(reps + 2):
         e[0].record(stream)
-        call("vg_dd2d_fp", ctypes.byref(g), _core.ptr(sirt.x), _core.ptr(sirt.xT),
-             _core.ptr(sirt.trig), _core.ptr(sirt.r), _core.stream(dev))
+        call("vg_dd2d_sirt_residual", ctypes.byref(g), _core.ptr(sirt.y), _core.ptr(sirt.inv_ws),
+             _core.ptr(sirt.trig), _core.ptr(sirt.x), _core.ptr(sirt.xT), _core.ptr(sirt.r),
+             _core.ptr(sirt.ws), sirt.ws.numel(), _core.stream(dev))
         e[1].record(stream)
-        call("vg_dd2d_bp", ctypes.byref(g), _core.ptr(sirt.r), _core.ptr(sirt.trig),
-             _core.ptr(flush), _core.ptr(sirt.ws), sirt.ws.numel(), _core.stream(dev))
+        call("vg_dd2d_sirt_update", ctypes.byref(g), _core.ptr(sirt.inv_wi),
+             ctypes.c_float(sirt.gamma), _core.ptr(sirt.trig), _core.ptr(sirt.x),
+             _core.ptr(sirt.xT), _core.ptr(sirt.r), _core.ptr(sirt.ws), sirt.ws.numel(),
+             _core.stream(dev))
         e[2].record(stream)
         torch.cuda.synchronize(dev)
         if i >= 2:
             fp_ms.append(e[0].elapsed_time(e[1]))
             bp_ms.append(e[1].elapsed_time(e[2]))
     t_fp, t_bp = statistics.median(fp_ms), statistics.median(bp_ms)
+    in_graph_ms = total_ms / (K * U)
     units = w["na"] * w["n"] * w["n"]                    # voxel-view updates per projector call
     alg_bytes = 4.0 * units
     dom_name, t_dom = ("dd2d_bp_kernel<fan>", t_bp) if t_bp >= t_fp else ("dd2d_fp_kernel<fan>", t_fp)
@@ -806,11 +823,13 @@ def main():
         "metric": METRIC, "value": value, "unit": "iter/s", "n_gpus": world, "steps": K,
         "warmup": Wm, "ms_per_step": total_ms / K, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": workload_desc(), "parallelism": f"replicas x{world}",
-                   "l2": "flushed between steps (256 MiB write); inputs 3.3 MB are L2-resident "
-                         "within a step", "graph": "100 updates captured as one CUDA graph"},
+        "config": arm_config(world),
         "fwd_back_gups": 2 * units / ((t_fp + t_bp) / 1e3) / 1e9,
-        "kernel_ms": {"dd2d_fp_kernel<fan>": t_fp, "dd2d_bp_kernel<fan>": t_bp},
+        "kernel_ms": {"dd2d_fp_kernel<fan>": t_fp, "dd2d_bp_kernel<fan>": t_bp,
+                      "update_in_graph": in_graph_ms,
+                      "note": "each half timed as the graph launches it: the forward "
+                              "projection with its residual and table epilogue, the back "
+                              "projection with its update epilogue"},
         "rmse_vs_phantom": rmse,
         "plain_fp32": {"value": plain_val, "unit": "iter/s", "rmse_vs_phantom": rmse_plain,
                        "path": "unfused: drop-in FP and BP calls + torch elementwise ops, "
@@ -829,11 +848,21 @@ def main():
         "clocks": clk.summary(),
     }
     if rank == 0 and not args.no_cpu_baseline:
-        sec, cores = cpu_sirt_iteration_rate(img.shape, angs, y, 1)
+        # the whole step on the host cores: the FP64 C restatement of
+        # dd.py/sirt_dd.py runs the same 100 updates; its iterate also pins
+        # the GPU's against the accuracy criterion (1e-4 relative)
+        sec, cores, x_orc = cpu_sirt_iteration_rate(img.shape, angs, y, U, want_x=True)
         line["cpu_baseline"] = {"value": 1.0 / sec, "unit": "iter/s", "cores": cores,
                                 "kind": "port",
-                                "sample": "1 SIRT update (FP + BP) of the full workload, FP64 C "
-                                          "restatement of dd.py/sirt_dd.py, OpenMP"}
+                                "sample": f"the whole step: {U} SIRT updates (FP + BP) of the full "
+                                          "workload, FP64 C restatement of dd.py/sirt_dd.py, "
+                                          "OpenMP"}
+        r_orc = float(np.sqrt(np.mean((x_orc - img) ** 2)))
+        line["oracle_rel"] = {
+            "iterate_rel_l2": float(np.linalg.norm(x_final - x_orc) / np.linalg.norm(x_orc)),
+            "rmse_vs_phantom_rel": abs(rmse - r_orc) / r_orc,
+            "rmse_vs_phantom_oracle": r_orc, "criterion": 1e-4,
+            "what": f"the GPU iterate after {U} updates vs the FP64 oracle's"}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -191,10 +191,13 @@ int vg_dd2d_bp(const vg_dd2d_geom *g, const float *sino, const double *trig,
  * an addition of this library.  The workspace is a fixed 32 MiB array in
  * the library's device memory (vg_dd2d_noalloc_scratch_bytes()), held on
  * every device that loads the library until exit; geometries needing more
- * are rejected with VG_ERR_ARG.  The first call on a device (that device
- * current) looks the array's address up and should come before any stream
- * capture.  All calls share the array: calls that overlap on the GPU race.
- * Nothing in the array needs clearing between calls. */
+ * are rejected with VG_ERR_ARG.  The first call in a CUDA context (that
+ * context current; normally a device's primary context) looks the array's
+ * address up, caches it under the context's process-unique id (cuCtxGetId),
+ * and should come before any stream capture; a context made later (after a
+ * device reset, or a non-primary one) gets its own lookup.  All calls share
+ * the array: calls that overlap on the GPU race.  Nothing in the array needs
+ * clearing between calls. */
 int vg_dd2d_bp_noalloc(const vg_dd2d_geom *g, const float *sino,
                        const double *trig, float *img, void *stream);
 size_t vg_dd2d_noalloc_scratch_bytes(void);
@@ -210,6 +213,23 @@ int vg_dd2d_sirt_iter(const vg_dd2d_geom *g, const float *y,
                       float gamma, const double *trig, float *x, float *xT,
                       float *r, void *workspace, size_t workspace_bytes,
                       void *stream);
+
+/* The two halves of vg_dd2d_sirt_iter, launched exactly as it launches them
+ * (vg_dd2d_sirt_iter is vg_dd2d_sirt_residual then vg_dd2d_sirt_update on
+ * the same stream and workspace), for callers that time them or put other
+ * work between them:
+ *   vg_dd2d_sirt_residual: r = (y - FP x) * inv_w_sino (sirt_dd.py:51-62);
+ *     when the forward projection's block holds whole views, it also writes
+ *     the back projection's tables of r into the workspace;
+ *   vg_dd2d_sirt_update: x += gamma * (BP r) * inv_w_img (sirt_dd.py:64-72),
+ *     x and xT in place; it builds r's tables itself where the residual
+ *     launch did not. */
+int vg_dd2d_sirt_residual(const vg_dd2d_geom *g, const float *y, const float *inv_w_sino,
+                          const double *trig, const float *x, const float *xT, float *r,
+                          void *workspace, size_t workspace_bytes, void *stream);
+int vg_dd2d_sirt_update(const vg_dd2d_geom *g, const float *inv_w_img, float gamma,
+                        const double *trig, float *x, float *xT, const float *r,
+                        void *workspace, size_t workspace_bytes, void *stream);
 
 /* Kernel launches vg_dd2d_sirt_iter makes per update for this geometry: 2
  * when the forward projection's epilogue writes the back projection's

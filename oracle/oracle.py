@@ -35,13 +35,15 @@ _fp = ctypes.POINTER(ctypes.c_float)
 _ip = ctypes.POINTER(ctypes.c_int32)
 
 
-def build(force: bool = False) -> str:
-    """Compile vir_oracle.c (and, when the vir tree is present, the
-    reference's C into oracle/_ref) with the Makefile beside this file."""
-    if force or not os.path.exists(_LIB_PATH) or (
-        os.path.getmtime(_LIB_PATH) < os.path.getmtime(os.path.join(_HERE, "vir_oracle.c"))
-    ):
-        subprocess.check_call(["make", "-s", "-C", _HERE, "all"])
+def build(force: bool = False, ref: str = None) -> str:
+    """Compile vir_oracle.c (and, when a vir source tree is given as ``ref``
+    or by the VIR_REF environment variable, the reference's C into
+    oracle/_ref) with the Makefile beside this file."""
+    ref = ref or os.environ.get("VIR_REF", "")
+    stale = force or not os.path.exists(_LIB_PATH) or (
+        os.path.getmtime(_LIB_PATH) < os.path.getmtime(os.path.join(_HERE, "vir_oracle.c")))
+    if stale or ref:
+        subprocess.check_call(["make", "-s", "-C", _HERE, "all", f"REF={ref}"])
     return _LIB_PATH
 
 
@@ -495,6 +497,189 @@ def filter_sino(sino, du=1.0, filter_type="ramp", cutoff=0.5, real_space=True):
     F = np.fft.rfft(np.asarray(sino, np.float64), axis=-1, n=z)
     F *= 2.0 * H
     return np.fft.irfft(F, n=z, axis=-1)[..., :nu]
+
+
+# --- FBP / FDK: weights and pixel-driven backprojection ---------------------
+#
+# vir's fan FBP (processing/reconstruction.py:7-67) cannot run (stale imports
+# and keyword arguments), but its parts can: the pre-weight cosine_weighting
+# (:99-107) and the 1/L^2-weighted linear-interpolation pixel backprojection
+# fan_backproject_hsieh (processing/proj2.py:580-616).  Both are restated
+# here as written and pinned against the reference's own functions
+# (golden fixtures).  The product reconstructs on vir's flat-detector
+# distance-driven geometry instead of Hsieh's equiangular one; fbp2d_bp and
+# fdk restate that geometry with the same weights and the same interpolation
+# step (_lerp), in float64.
+
+def cosine_weighting(sino, cols, src_iso, det_off=0.0, equispaced=False):
+    """processing/reconstruction.py:99-107: each detector column times
+    (src_iso - det_off cols / src_iso) / sqrt(src_iso^2 + cols^2)
+    (equispaced: cols are positions at the isocentre) or
+    src_iso cos(cols) - det_off sin(cols) (equiangular: cols are angles)."""
+    cols = np.asarray(cols, np.float64)
+    if equispaced:
+        w = (src_iso - det_off * cols / src_iso) / np.sqrt(src_iso ** 2 + cols ** 2)
+    else:
+        w = src_iso * np.cos(cols) - det_off * np.sin(cols)
+    return w * np.asarray(sino, np.float64)
+
+
+def _lerp(row, t, clip):
+    """(1 - a) row[j] + a row[j + 1] with j = floor(t), a = t - j
+    (proj2.py:607-613).  clip: indices clipped to the row (Hsieh's rule);
+    else samples outside the row are zero (the flat-detector kernels)."""
+    j = np.floor(t).astype(np.int64)
+    a = t - j
+    n = row.shape[-1]
+    if clip:
+        return (1.0 - a) * row[..., np.clip(j, 0, n - 1)] + a * row[..., np.clip(j + 1, 0, n - 1)]
+    pad = np.zeros(row.shape[:-1] + (n + 2,), np.float64)
+    pad[..., 1:-1] = row
+    v0 = pad[..., np.clip(j, -1, n) + 1]
+    v1 = pad[..., np.clip(j + 1, -1, n) + 1]
+    return v0 + a * (v1 - v0)
+
+
+def fan_backproject_hsieh(Sino, Views, Cols, src_iso, dPixels=(1.0, 1.0), nPixels=(512, 512),
+                          detOff=0.0, pixOff=(0.0, 0.0)):
+    """processing/proj2.py:580-616 (pixel grid of calc_image_arrays,
+    proj2.py:912-923): filtered rows times cos^2(Cols), then per view the
+    equiangular column of every pixel by arctan, linear interpolation with
+    clipped indices, weight 1 / (src_iso - X cos + Y sin)^2."""
+    Sino = np.asarray(Sino, np.float64)
+    nViews, nRows, nCols = Sino.shape
+    Cols = np.asarray(Cols, np.float64)
+    dCol = Cols[1] - Cols[0]
+    Col0 = Cols[0]
+    Sino = Sino * (np.cos(Cols) ** 2)
+    sv, cv = np.sin(Views), np.cos(Views)
+    nX, nY = nPixels
+    dX, dY = dPixels
+    X = np.linspace(1 - nX, nX - 1, nX) * dX / 2.0
+    Y = np.linspace(1 - nY, nY - 1, nY) * dY / 2.0
+    X, Y = np.meshgrid(X + pixOff[1], Y + pixOff[0])
+    image = np.zeros((nRows, nX, nY))
+    for l in range(nViews):
+        Yf = src_iso - X * cv[l] + Y * sv[l]
+        t = (np.arctan((X * sv[l] + Y * cv[l] - detOff) / Yf) - Col0) / dCol
+        for k in range(nRows):
+            image[k] += _lerp(Sino[l, k], t, clip=True) / Yf ** 2
+    return np.squeeze(image)
+
+
+def fan_preweight(nu, du=1.0, su=0.0, DSO=1.0, DSD=1.0):
+    """The equispaced cosine_weighting of the flat detector: bin centres
+    du (j - nu/2 + 0.5 + su) scaled to the isocentre by DSO / DSD."""
+    s = du * (np.arange(nu) - nu / 2.0 + 0.5 + su) * DSO / DSD
+    return cosine_weighting(np.ones(nu), s, DSO, equispaced=True)
+
+
+def fbp2d_bp(q, ang_arr, img_shape, fan=False, DSO=0.0, DSD=0.0, du=1.0, su=0.0, d_pix=1.0):
+    """Pixel-driven FBP backprojection on vir's distance-driven geometry
+    (dd.py:486-494, 527-585; source direction (cos, sin), detector axis
+    (-sin, cos)): img = pi / (2 na) sum_views Q(s) / U^2 with o = c x + s y,
+    p = -s x + c y; parallel s = p, U = 1; fan s = DSD p / (DSO - o),
+    U = (DSO - o) / DSO (the 1/L^2 weight of proj2.py:606-613 normalised at
+    the isocentre); Q linear between bin centres du (j - nu/2 + 0.5 + su),
+    zero outside the detector.  Geometry values are taken as given (pass the
+    float32-rounded values a float32 kernel sees)."""
+    q = np.asarray(q, np.float64)
+    c, s = _dd_trig(ang_arr)
+    na, nu = q.shape
+    nx, ny = img_shape
+    x = (d_pix * (np.arange(nx) + 0.5 - 0.5 * nx))[:, None]
+    y = (d_pix * (np.arange(ny) + 0.5 - 0.5 * ny))[None, :]
+    img = np.zeros((nx, ny))
+    off = 0.5 * nu - 0.5 - su
+    for ia in range(na):
+        p = -s[ia] * x + c[ia] * y
+        w = 1.0
+        if fan:
+            d = DSO - (c[ia] * x + s[ia] * y)
+            p = DSD * p / d
+            w = (DSO / d) ** 2
+        img += w * _lerp(q[ia], p / du + off, clip=False)
+    return img * (np.pi / (2.0 * na))
+
+
+def fbp_2d(sino, ang_arr, img_shape, fan=False, DSO=0.0, DSD=0.0, du=1.0, su=0.0, d_pix=1.0,
+           filter_type="ramp", cutoff=0.5, real_space=True):
+    """Full-scan FBP: (fan) the equispaced pre-weight, filter_sino at the bin
+    pitch (fan: at the isocentre, du DSO / DSD), fbp2d_bp."""
+    y = np.asarray(sino, np.float64)
+    if fan:
+        y = y * fan_preweight(y.shape[1], du, su, DSO, DSD)[None, :]
+        q = filter_sino(y, du * DSO / DSD, filter_type, cutoff, real_space)
+    else:
+        q = filter_sino(y, du, filter_type, cutoff, real_space)
+    return fbp2d_bp(q, ang_arr, img_shape, fan, DSO, DSD, du, su, d_pix)
+
+
+def fbp_par_dd(sino, ang_arr, img_shape, du=1.0, su=0.0, d_pix=1.0, filter_type="ramp",
+               cutoff=0.5, real_space=True):
+    """vir's working parallel FBP over 180 degrees: (pi / 2)
+    dd_bp_par_2d(filter_sino(y)) (filtration.py:238-309, dd.py:666-672)."""
+    q = filter_sino(np.asarray(sino, np.float64), du, filter_type, cutoff, real_space)
+    return (np.pi / 2.0) * dd_bp_par_2d(q.astype(np.float32), ang_arr, img_shape, du, su, d_pix)
+
+
+def fdk_preweight(nu, nv, du, dv, su, sv, DSD):
+    """FDK pre-weight DSD / sqrt(DSD^2 + u^2 + v^2) at the (u, v) bin
+    centres: cosine_weighting's equispaced weight on the flat 2D detector."""
+    u = du * (np.arange(nu) - 0.5 * nu + 0.5 + su)
+    v = dv * (np.arange(nv) - 0.5 * nv + 0.5 + sv)
+    return DSD / np.sqrt(DSD ** 2 + u[:, None] ** 2 + v[None, :] ** 2)
+
+
+def fdk(sino, ang_arr, img_shape, DSO, DSD, du=1.0, dv=1.0, su=0.0, sv=0.0, d_pix=1.0,
+        filter_type="ramp", cutoff=0.5, real_space=True, box=None):
+    """FDK on the circular cone geometry of dd_fp_cone_3d, sino (na, nu, nv):
+    pre-weight (fdk_preweight), filter_sino along u at the isocentre pitch
+    du DSO / DSD, then vol = pi / (2 na) sum_views Q(u, v) / U^2 with
+    o = c x + s y, p = -s x + c y, U = (DSO - o) / DSO, u = DSD p / (DSO - o),
+    v = DSD z / (DSO - o), Q bilinear between bin centres (zero outside).
+    ``box`` = ((x0, x1), (y0, y1), (z0, z1)) voxel index ranges returns that
+    sub-volume only; per view only the detector rows the box reaches are
+    filtered (rows are filtered independently, so this is exact)."""
+    sino = np.asarray(sino)
+    na, nu, nv = sino.shape
+    nx, ny, nz = img_shape
+    box = box or ((0, nx), (0, ny), (0, nz))
+    (x0, x1), (y0, y1), (z0, z1) = box
+    c, s = _dd_trig(ang_arr)
+    X = (d_pix * (np.arange(x0, x1) + 0.5 - 0.5 * nx))[:, None, None]
+    Y = (d_pix * (np.arange(y0, y1) + 0.5 - 0.5 * ny))[None, :, None]
+    Z = (d_pix * (np.arange(z0, z1) + 0.5 - 0.5 * nz))[None, None, :]
+    W = fdk_preweight(nu, nv, du, dv, su, sv, DSD)
+    pitch = du * DSO / DSD
+    iu_off, iv_off = 0.5 * nu - 0.5 - su, 0.5 * nv - 0.5 - sv
+    vol = np.zeros((x1 - x0, y1 - y0, z1 - z0))
+    for ia in range(na):
+        d = DSO - (c[ia] * X + s[ia] * Y)
+        tu = DSD * (-s[ia] * X + c[ia] * Y) / d / du + iu_off
+        tv = DSD * Z / d / dv + iv_off
+        tu, tv = np.broadcast_arrays(tu, tv)
+        k0 = max(int(np.floor(tv.min())), 0)
+        k1 = min(int(np.floor(tv.max())) + 2, nv)
+        if k1 <= k0:
+            continue
+        rows = (sino[ia, :, k0:k1].astype(np.float64) * W[:, k0:k1]).T   # (rows, nu)
+        Q = filter_sino(rows, pitch, filter_type, cutoff, real_space)    # (rows, nu)
+        # bilinear: along u in each needed row, then along v
+        ju = np.floor(tu).astype(np.int64)
+        au = tu - ju
+        jv = np.floor(tv).astype(np.int64)
+        av = tv - jv
+        padQ = np.zeros((nv + 2, nu + 2))
+        padQ[k0 + 1:k1 + 1, 1:-1] = Q
+        cu0, cu1 = np.clip(ju, -1, nu) + 1, np.clip(ju + 1, -1, nu) + 1
+        cv0, cv1 = np.clip(jv, -1, nv) + 1, np.clip(jv + 1, -1, nv) + 1
+        q00, q10 = padQ[cv0, cu0], padQ[cv0, cu1]   # (v = jv, u = ju / ju + 1)
+        q01, q11 = padQ[cv1, cu0], padQ[cv1, cu1]   # (v = jv + 1)
+        a = q00 + av * (q01 - q00)
+        b = q10 + av * (q11 - q10)
+        vol += (a + au * (b - a)) * (DSO / d) ** 2
+    return vol * (np.pi / (2.0 * na))
 
 
 # --- SIRT (sys_mat/sirt_dd.py:23-76) ---------------------------------------

@@ -1,9 +1,10 @@
 """Generates the golden fixtures in this directory by running the reference
 (vargasp/vir) itself, imported from its source tree.
 
-Run in a container that holds the vir tree (default ``/root/reference``):
+Run in a container that holds the vir tree, named by ``--ref`` or by the
+VIR_REF environment variable:
 
-    python tests/golden/make_golden.py [--ref /path/to/vir]
+    python tests/golden/make_golden.py --ref /path/to/vir
 
 The reference is imported through three shims and nothing else: a ``vir``
 symlink to the tree on ``sys.path`` (every module imports ``vir.*``), an
@@ -93,8 +94,11 @@ def ellipse_image(n, n_ell, seed, vmax=0.02):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("VIR_REF"),
+                    help="the vir source tree (default: $VIR_REF)")
     args = ap.parse_args()
+    if not args.ref:
+        ap.error("give the vir source tree with --ref or VIR_REF")
     ref = args.ref
     import_reference(ref)
     import vir.sys_mat.dd as dd
@@ -193,20 +197,28 @@ def main():
             ([2.0, .25, .25], [-1.9, .25, .25]), ([2.0, .25, .25], [-2.1, .25, .25]),
             ([.25, 4.0, .25], [.25, 4.0, .25]), ([-4.0, .25, .25], [-4.0, .25, .25]),
             ([2.0, -2.0, 0.0], [-2.0, -2.0, 0.0]), ([2.0, -1.0, 0.0], [-2.0, -1.0, 0.0]),
-            ([2.0, 0.0, 0.0], [-2.0, 0.0, 0.0])]
+            ([2.0, 0.0, 0.0], [-2.0, 0.0, 0.0]),
+            # a zero-length ray inside the grid: it enters the alpha range but
+            # keeps no positive length, so the object forms hold empty arrays
+            ([.25, .25, .25], [.25, .25, .25])]
     srcs = np.array([e[0] for e in edge], np.float32)
     trgs = np.array([e[1] for e in edge], np.float32)
     ind, ln, off = sd.siddons(srcs, trgs, (4, 4, 1), 1.0, flat=True)
+    # which rays the object form leaves None (rays that miss the grid)
+    obj = sd.siddons(srcs, trgs, (4, 4, 1), 1.0, ravel=True).reshape(-1)
     out["siddons_edge"] = dict(src=srcs, trg=trgs, nPixels=np.array([4, 4, 1], np.int32),
-                               dPixels=np.array([1.0, 1.0, 1.0]), ind=ind, len=ln, off=off)
+                               dPixels=np.array([1.0, 1.0, 1.0]), ind=ind, len=ln, off=off,
+                               obj_none=np.array([r is None for r in obj]))
     # a circular parallel geometry (proj_geom.geom_circular) on a 16x16x1 grid
     dets = (np.arange(23) - 11).astype(np.float64) * 0.9
     views = np.linspace(0, np.pi, 12, endpoint=False)
     src, trg = pg.geom_circular(dets, views, geom="par")
     ind, ln, off = sd.siddons(src, trg, (16, 16, 1), 1.0, flat=True)
+    obj = sd.siddons(src, trg, (16, 16, 1), 1.0, ravel=True).reshape(-1)
     out["siddons_par"] = dict(src=src.astype(np.float32), trg=trg.astype(np.float32),
                               nPixels=np.array([16, 16, 1], np.int32),
-                              dPixels=np.array([1.0, 1.0, 1.0]), ind=ind, len=ln, off=off)
+                              dPixels=np.array([1.0, 1.0, 1.0]), ind=ind, len=ln, off=off,
+                              obj_none=np.array([r is None for r in obj]))
     # a fan geometry in 3D (cone with one z row offset) on a 12x10x6 grid
     dets = (np.arange(15) - 7).astype(np.float64) * 1.1
     dz = (np.arange(5) - 2).astype(np.float64) * 1.2
@@ -310,6 +322,34 @@ def main():
                               gem_prms=np.array(prms[0]), img_prms=np.array(prms[1]),
                               src_prms=np.array(prms[2]), det_prms=np.array(prms[3]),
                               srt_prms=np.array(prms[4]))
+
+    # --- fan FBP parts (processing/reconstruction.py:99-107, proj2.py:580-616) --
+    # vir's fan_fbp cannot run; its pre-weight and its Hsieh backprojector can,
+    # executed from their own source (the modules' imports are stale)
+    rec = function_from_source(os.path.join(ref, "processing", "reconstruction.py"),
+                               ["cosine_weighting"])
+    p2 = function_from_source(os.path.join(ref, "processing", "proj2.py"),
+                              ["fan_backproject_hsieh", "calc_image_arrays"],
+                              extra_globals={"sys": types.SimpleNamespace(
+                                  stdout=types.SimpleNamespace(write=lambda *a: None,
+                                                               flush=lambda: None))})
+    p2["fan_backproject_hsieh"].__globals__["calc_image_arrays"] = p2["calc_image_arrays"]
+    rng = np.random.default_rng(41)
+    sino_w = rng.random((3, 31))
+    cols_pos = (np.arange(31) - 15.0) * 1.3
+    cols_ang = (np.arange(31) - 15.0) * 0.01
+    out["fbp_weights"] = dict(
+        sino=sino_w, cols_pos=cols_pos, cols_ang=cols_ang, src_iso=500.0, det_off=1.5,
+        equispaced=rec["cosine_weighting"](sino_w, cols_pos, 500.0, detOff=1.5, equispaced=True),
+        equiangular=rec["cosine_weighting"](sino_w, cols_ang, 500.0, detOff=1.5, equispaced=False))
+    sino_h = rng.random((5, 2, 41))
+    views_h = np.linspace(0, 2 * np.pi, 5, endpoint=False) + 0.1
+    cols_h = (np.arange(41) - 20.0) * 0.012
+    img_h = p2["fan_backproject_hsieh"](sino_h, views_h, cols_h, 60.0, dPixels=(1.1, 1.1),
+                                        nPixels=(16, 16), detOff=0.3, pixOff=(0.2, -0.1))
+    out["fbp_hsieh"] = dict(sino=sino_h, views=views_h, cols=cols_h, src_iso=60.0,
+                            dPixels=np.array([1.1, 1.1]), nPixels=np.array([16, 16], np.int32),
+                            detOff=0.3, pixOff=np.array([0.2, -0.1]), img=img_h)
 
     # --- Siddon list algebra (siddon.py:12-633) on the cone fixture's lists ---
     import copy

@@ -18,21 +18,29 @@ def test_siddons_flat_bit_exact(vg, golden, case):
     assert np.array_equal(ln, g["len"])   # same float32 bits
 
 
-def test_siddons_object_forms(vg, golden):
+@pytest.mark.parametrize("case", ["siddons_par", "siddons_edge"])
+def test_siddons_object_forms(vg, golden, case):
+    """Object forms: None exactly where the reference leaves a ray None (it
+    misses the grid); a ray that enters the grid but keeps no positive length
+    (the zero-length ray of the edge fixture) holds empty int32 / float32
+    arrays, as the reference stores them."""
     from vir_gb300.sys_mat import siddon
-    g = golden["siddons_par"]
+    g = golden[case]
     rays = siddon.siddons(g["src"], g["trg"], g["nPixels"], g["dPixels"], ravel=True)
     assert rays.shape == g["src"].shape[:-1]
     flat = rays.reshape(-1)
+    none = np.array([r is None for r in flat])
+    assert np.array_equal(none, g["obj_none"])
     for r in range(flat.size):
         a, b = g["off"][r], g["off"][r + 1]
-        if a == b:
-            assert flat[r] is None
-        else:
+        if not none[r]:
+            assert flat[r][0].dtype == np.int32 and flat[r][1].dtype == np.float32
             assert np.array_equal(flat[r][0], g["ind"][a:b])
             assert np.array_equal(flat[r][1], g["len"][a:b])
+    if case == "siddons_edge":
+        assert any(not none[r] and g["off"][r] == g["off"][r + 1] for r in range(flat.size))
     un = siddon.siddons(g["src"], g["trg"], g["nPixels"], g["dPixels"], ravel=False)
-    r = next(i for i in range(flat.size) if flat[i] is not None)
+    r = next(i for i in range(flat.size) if flat[i] is not None and flat[i][0].size)
     x, y, z = np.unravel_index(flat[r][0], tuple(g["nPixels"]))
     assert np.array_equal(un.reshape(-1)[r][0], x) and np.array_equal(un.reshape(-1)[r][2], z)
 
@@ -117,18 +125,3 @@ def test_numba_list_entry_points(vg, golden):
     out = np.zeros(nr, np.float32)
     proj_numba.fast_forward_project_p(c["phantom"].ravel(), d["ind"], d["len"], d["off"], out)
     assert np.abs(out - ref).max() <= 2e-6 * np.abs(ref).max()
-
-
-def test_mp_list_entry_points(vg, golden):
-    """proj_mp drop-ins on an unraveled object-array list."""
-    from vir_gb300.projection import proj_mp
-    from vir_gb300.sys_mat import siddon as sd
-    d, c = golden["siddons_cone"], golden["list_c"]
-    nP = tuple(int(v) for v in d["nPixels"])
-    sdl = sd.siddons(d["src"], d["trg"], nP, tuple(d["dPixels"]))
-    s = proj_mp.mp_sd_f_proj(c["phantom"], sdl)
-    assert s.shape == sdl.shape
-    ref = c["sino"].reshape(sdl.shape).astype(np.float64)
-    assert np.abs(s - ref).max() <= 2e-6 * np.abs(ref).max()
-    b = proj_mp.mpc_sd_b_proj(c["y"].reshape(sdl.shape), sdl, nP)
-    assert np.abs(b - c["bp"]).max() <= 2e-6 * np.abs(c["bp"]).max()

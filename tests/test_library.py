@@ -100,3 +100,31 @@ def test_drop_in_table_resolves_and_installs():
                 sys.modules.pop(k, None)
             else:
                 sys.modules[k] = v
+
+
+def _autotune_writer(args):
+    path, tag, n = args
+    os.environ["VIR_GB300_AUTOTUNE"] = path
+    from vir_gb300 import autotune
+    for i in range(n):
+        with autotune._file_lock():
+            c = autotune._read()
+            c[f"{tag}-{i}"] = {"variant": i}
+            autotune._write(c)
+    return tag
+
+
+def test_autotune_cache_writes_from_two_processes(tmp_path):
+    """Two processes updating the autotune cache at once keep each other's
+    entries and leave no temporary files behind (file lock around the
+    read-modify-write, a private temporary file per write)."""
+    import multiprocessing as mp
+    path = str(tmp_path / "autotune.json")
+    with mp.get_context("spawn").Pool(2) as pool:
+        tags = pool.map(_autotune_writer, [(path, "a", 25), (path, "b", 25)])
+    assert sorted(tags) == ["a", "b"]
+    import json
+    with open(path) as fh:
+        c = json.load(fh)
+    assert len(c) == 50
+    assert not [f for f in os.listdir(tmp_path) if f.endswith(".tmp")]

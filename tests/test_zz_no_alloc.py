@@ -30,12 +30,17 @@ def _run_pair(L, g, sino, trig, dev):
     out = torch.full((g.nx, g.ny), float("nan"), dtype=torch.float32, device=dev)
     torch.cuda.synchronize(dev)
     before = torch.cuda.memory_allocated(dev)
+    # free device bytes as the driver counts them (cudaMemGetInfo): a
+    # cudaMalloc inside the library would show here, where torch's own
+    # counter cannot see it
+    free0 = torch.cuda.mem_get_info(dev)[0]
     st = L.vg_dd2d_bp_noalloc(ctypes.byref(g), ctypes.c_void_p(sino.data_ptr()),
                               ctypes.c_void_p(trig.data_ptr()), ctypes.c_void_p(out.data_ptr()),
                               _core.stream(dev))
     assert st == 0, L.vg_last_error()
     torch.cuda.synchronize(dev)
     assert torch.cuda.memory_allocated(dev) == before
+    assert torch.cuda.mem_get_info(dev)[0] == free0
     return ref.cpu().numpy(), out.cpu().numpy()
 
 
@@ -52,6 +57,12 @@ def test_noalloc_bp_matches_workspace_bp(vg):
         # parallel, different sizes, so the second call rewrites the array differently
         (DD2DGeom(200, 150, 181, 260, 1.0, 0.25, 1.1, 0.0, 0.0, 0), np.pi),
     ]
+    # a geometry whose workspace nearly fills the 32 MiB array
+    near = DD2DGeom(512, 512, 2800, 1200, 1.2, 0.0, 0.9, 500.0, 1000.0, 1)
+    need = L.vg_dd2d_workspace_bytes(ctypes.byref(near))
+    cap = L.vg_dd2d_noalloc_scratch_bytes()
+    assert 0.9 * cap < need <= cap
+    cases.append((near, 2 * np.pi))
     for g, span in cases:
         angs = np.linspace(0, span, g.na, endpoint=False)
         trig = _core.trig_cache.get(angs, np.float32, dev)

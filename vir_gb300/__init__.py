@@ -53,9 +53,6 @@ _DROP_INS = {
                               for n in ("fast_forward_project", "fast_forward_project_p",
                                         "sd_f_proj_numba", "sd_f_proj_numba_p")},
     "projection.proj_cuda": {"sd_f_proj_numba_g": "vir_gb300.projection.proj_numba:sd_f_proj_numba_g"},
-    "projection.proj_mp": {n: "vir_gb300.projection.proj_mp:" + n
-                           for n in ("mp_sd_f_proj", "mp_sd_b_proj", "mpc_sd_f_proj",
-                                     "mpc_sd_b_proj")},
     "trajectory": {n: "vir_gb300.trajectory:" + n
                    for n in ("sino_axl2hel", "sino_hel2axl", "sino_hel2axl180", "sino_hel2hel",
                              "sino_hel_subset", "forward_project_phantom")},

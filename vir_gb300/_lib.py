@@ -93,6 +93,10 @@ _PROTOS = {
                    c_void_p],
     "vg_dd2d_sirt_iter": [ctypes.POINTER(DD2DGeom), c_void_p, c_void_p, c_void_p, c_float,
                           c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_size_t, c_void_p],
+    "vg_dd2d_sirt_residual": [ctypes.POINTER(DD2DGeom), c_void_p, c_void_p, c_void_p, c_void_p,
+                              c_void_p, c_void_p, c_void_p, c_size_t, c_void_p],
+    "vg_dd2d_sirt_update": [ctypes.POINTER(DD2DGeom), c_void_p, c_float, c_void_p, c_void_p,
+                            c_void_p, c_void_p, c_void_p, c_size_t, c_void_p],
     "vg_dd2d_bp_noalloc": [ctypes.POINTER(DD2DGeom), c_void_p, c_void_p, c_void_p, c_void_p],
     "vg_fbp2d_bp": [ctypes.POINTER(DD2DGeom), c_void_p, c_void_p, c_void_p, c_void_p],
     "vg_dd3d_fp": [ctypes.POINTER(DD3DGeom), c_void_p, c_void_p, c_void_p, c_void_p, c_size_t,

@@ -10,9 +10,11 @@ name, library version); later calls read the cache.  The cache lives in
 """
 from __future__ import annotations
 
+import contextlib
 import ctypes
 import json
 import os
+import tempfile
 import threading
 
 import numpy as np
@@ -38,13 +40,42 @@ def _read():
         return {}
 
 
+@contextlib.contextmanager
+def _file_lock():
+    """Exclusive lock on a lock file beside the cache, across processes (the
+    replica ranks of one job may tune at the same time); the threading lock
+    covers the threads of one process."""
+    path = cache_path() + ".lock"
+    os.makedirs(os.path.dirname(path), exist_ok=True)
+    with _lock, open(path, "a") as fh:
+        try:
+            import fcntl
+            fcntl.flock(fh, fcntl.LOCK_EX)
+        except (ImportError, OSError):
+            pass  # no flock on this platform: the thread lock still holds
+        try:
+            yield
+        finally:
+            try:
+                fcntl.flock(fh, fcntl.LOCK_UN)
+            except (NameError, OSError):
+                pass
+
+
 def _write(d):
+    """Write the cache through a temporary file of its own, then rename it
+    into place (call with the file lock held)."""
     path = cache_path()
     os.makedirs(os.path.dirname(path), exist_ok=True)
-    tmp = path + ".tmp"
-    with open(tmp, "w") as fh:
-        json.dump(d, fh, indent=1, sort_keys=True)
-    os.replace(tmp, path)
+    fd, tmp = tempfile.mkstemp(dir=os.path.dirname(path), prefix=".autotune.", suffix=".tmp")
+    try:
+        with os.fdopen(fd, "w") as fh:
+            json.dump(d, fh, indent=1, sort_keys=True)
+        os.replace(tmp, path)
+    except BaseException:
+        with contextlib.suppress(OSError):
+            os.unlink(tmp)
+        raise
 
 
 def _key(g, dev):
@@ -86,7 +117,7 @@ def best_fp_variant(g, dev=None) -> int:
     """The fastest forward-projector variant for g's geometry class (cached)."""
     dev = dev or torch.device("cuda", torch.cuda.current_device())
     key = _key(g, dev)
-    with _lock:
+    with _file_lock():
         c = _read()
         if key in c:
             return int(c[key]["variant"])
@@ -94,7 +125,7 @@ def best_fp_variant(g, dev=None) -> int:
     if not t:
         return 0
     best = min(t, key=t.get)
-    with _lock:
+    with _file_lock():  # read-modify-write under the lock: entries of other processes are kept
         c = _read()
         c[key] = {"variant": int(best), "ms": {str(k): round(v, 4) for k, v in t.items()}}
         _write(c)

@@ -735,29 +735,58 @@ extern "C" int vg_dd2d_bp(const vg_dd2d_geom *g, const float *sino, const double
                      as_stream(stream));
 }
 
+namespace {
+int check_sirt_ws(const vg_dd2d_geom *g, const void *workspace, size_t workspace_bytes) {
+    VG_REQUIRE(workspace != nullptr && workspace_bytes >= bp_ws_bytes(g),
+               "dd2d_sirt: workspace of %zu bytes needed (vg_dd2d_workspace_bytes)",
+               bp_ws_bytes(g));
+    VG_REQUIRE(((uintptr_t)workspace & 255) == 0, "dd2d_sirt: workspace must be 256-byte aligned");
+    return VG_OK;
+}
+// the residual's back-projection tables come from the forward projection's
+// epilogue when its block holds whole views (no separate table launch)
+bool sirt_fused(const vg_dd2d_geom *g) { return VG_SIRT_FUSED_TABLES && fp_builds_bp_tables(g); }
+}  // namespace
+
+extern "C" int vg_dd2d_sirt_residual(const vg_dd2d_geom *g, const float *y,
+                                     const float *inv_w_sino, const double *trig, const float *x,
+                                     const float *xT, float *r, void *workspace,
+                                     size_t workspace_bytes, void *stream) {
+    int st = check_geom(g);
+    if (st) return st;
+    VG_REQUIRE(y && inv_w_sino && trig && x && xT && r, "dd2d_sirt_residual: null pointer");
+    st = check_sirt_ws(g, workspace, workspace_bytes);
+    if (st) return st;
+    return launch_fp(g, x, xT, trig, r, sirt_fused(g) ? 2 : 1, y, inv_w_sino, as_stream(stream),
+                     bp_ws(g, workspace));
+}
+
+extern "C" int vg_dd2d_sirt_update(const vg_dd2d_geom *g, const float *inv_w_img, float gamma,
+                                   const double *trig, float *x, float *xT, const float *r,
+                                   void *workspace, size_t workspace_bytes, void *stream) {
+    int st = check_geom(g);
+    if (st) return st;
+    VG_REQUIRE(inv_w_img && trig && x && xT && r, "dd2d_sirt_update: null pointer");
+    st = check_sirt_ws(g, workspace, workspace_bytes);
+    if (st) return st;
+    return launch_bp(g, r, trig, x, 1, inv_w_img, gamma, xT, workspace, workspace_bytes,
+                     as_stream(stream), !sirt_fused(g));
+}
+
 extern "C" int vg_dd2d_sirt_iter(const vg_dd2d_geom *g, const float *y, const float *inv_w_sino,
                                  const float *inv_w_img, float gamma, const double *trig,
                                  float *x, float *xT, float *r, void *workspace,
                                  size_t workspace_bytes, void *stream) {
-    int st = check_geom(g);
+    int st = vg_dd2d_sirt_residual(g, y, inv_w_sino, trig, x, xT, r, workspace, workspace_bytes,
+                                   stream);
     if (st) return st;
-    VG_REQUIRE(y && inv_w_sino && inv_w_img && trig && x && xT && r, "dd2d_sirt_iter: null pointer");
-    cudaStream_t s = as_stream(stream);
-    VG_REQUIRE(workspace != nullptr && workspace_bytes >= bp_ws_bytes(g),
-               "dd2d_sirt_iter: workspace of %zu bytes needed (vg_dd2d_workspace_bytes)",
-               bp_ws_bytes(g));
-    VG_REQUIRE(((uintptr_t)workspace & 255) == 0, "dd2d_sirt_iter: workspace must be 256-byte aligned");
-    // the residual's back-projection tables come from the forward projection's
-    // epilogue when its block holds whole views (no separate table launch)
-    const bool fused = VG_SIRT_FUSED_TABLES && fp_builds_bp_tables(g);
-    st = launch_fp(g, x, xT, trig, r, fused ? 2 : 1, y, inv_w_sino, s, bp_ws(g, workspace));
-    if (st) return st;
-    return launch_bp(g, r, trig, x, 1, inv_w_img, gamma, xT, workspace, workspace_bytes, s, !fused);
+    return vg_dd2d_sirt_update(g, inv_w_img, gamma, trig, x, xT, r, workspace, workspace_bytes,
+                               stream);
 }
 
 extern "C" int vg_dd2d_sirt_launches(const vg_dd2d_geom *g) {
     if (check_geom(g) != VG_OK) return 0;
-    return (VG_SIRT_FUSED_TABLES && fp_builds_bp_tables(g)) ? 2 : 3;
+    return sirt_fused(g) ? 2 : 3;
 }
 
 // ---------------------------------------------------------------------------
@@ -776,8 +805,11 @@ extern "C" int vg_dd2d_sirt_launches(const vg_dd2d_geom *g) {
 // - The caller still passes the sinogram and the output image.
 // - Geometries whose workspace (vg_dd2d_workspace_bytes) exceeds 32 MiB are
 //   rejected with VG_ERR_ARG.
-// - The first call on a device, with that device current, looks up the
-//   array's device address (cudaGetSymbolAddress) and caches it; make that
+// - The first call in a CUDA context (normally a device's primary context),
+//   with that context current, looks up the array's device address
+//   (cudaGetSymbolAddress) and caches it under the context's unique id
+//   (cuCtxGetId, never reused within a process, so a context created after a
+//   device reset or a non-primary context gets its own lookup); make that
 //   first call before any stream capture.
 // - Every call shares the one array: calls whose executions overlap on the
 //   GPU (different streams, or concurrent host threads) race and corrupt
@@ -788,7 +820,7 @@ extern "C" int vg_dd2d_sirt_launches(const vg_dd2d_geom *g) {
 // ---------------------------------------------------------------------------
 
 #define VG_NOALLOC_SCRATCH_BYTES (32u << 20)
-#define VG_NOALLOC_MAX_DEVICES 64
+#define VG_NOALLOC_MAX_CONTEXTS 64
 
 static __device__ __align__(256) unsigned char g_dd2d_scratch[VG_NOALLOC_SCRATCH_BYTES];
 
@@ -796,22 +828,73 @@ static __device__ __align__(256) unsigned char g_dd2d_scratch[VG_NOALLOC_SCRATCH
 
 namespace {
 std::mutex g_scratch_mu;
-void *g_scratch_addr[VG_NOALLOC_MAX_DEVICES] = {};
+struct ScratchEntry {
+    unsigned long long ctx_id;
+    void *addr;
+};
+ScratchEntry g_scratch_cache[VG_NOALLOC_MAX_CONTEXTS] = {};
+int g_scratch_n = 0;
 
-// Device address of g_dd2d_scratch on the current device (looked up once).
-int scratch_address(void **out) {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return cuda_status(e, "dd2d_bp_noalloc: cudaGetDevice");
-    VG_REQUIRE(dev >= 0 && dev < VG_NOALLOC_MAX_DEVICES, "dd2d_bp_noalloc: device %d out of range", dev);
-    std::lock_guard<std::mutex> lk(g_scratch_mu);
-    if (!g_scratch_addr[dev]) {
-        void *p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_dd2d_scratch);
-        if (e != cudaSuccess) return cuda_status(e, "dd2d_bp_noalloc: cudaGetSymbolAddress");
-        g_scratch_addr[dev] = p;
+// cuCtxGetCurrent / cuCtxGetId through the runtime's driver entry points (the
+// library links only the CUDA runtime, so it loads where libcuda is absent).
+typedef int (*CtxGetCurrentFn)(void **);
+typedef int (*CtxGetIdFn)(void *, unsigned long long *);
+CtxGetCurrentFn g_ctx_get_current = nullptr;
+CtxGetIdFn g_ctx_get_id = nullptr;
+
+// Unique id of the current context; with none current yet, the current
+// device's primary context is made current first (cudaSetDevice does that).
+int current_context_id(unsigned long long *id) {
+    cudaError_t e;
+    if (!g_ctx_get_current || !g_ctx_get_id) {
+        void *f0 = nullptr, *f1 = nullptr;
+        cudaDriverEntryPointQueryResult q0, q1;
+        e = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f0, 12000, cudaEnableDefault, &q0);
+        if (e != cudaSuccess || q0 != cudaDriverEntryPointSuccess || !f0)
+            return cuda_status(e != cudaSuccess ? e : cudaErrorNotSupported,
+                               "dd2d_bp_noalloc: cuCtxGetCurrent entry point");
+        e = cudaGetDriverEntryPointByVersion("cuCtxGetId", &f1, 12000, cudaEnableDefault, &q1);
+        if (e != cudaSuccess || q1 != cudaDriverEntryPointSuccess || !f1)
+            return cuda_status(e != cudaSuccess ? e : cudaErrorNotSupported,
+                               "dd2d_bp_noalloc: cuCtxGetId entry point");
+        g_ctx_get_current = reinterpret_cast<CtxGetCurrentFn>(f0);
+        g_ctx_get_id = reinterpret_cast<CtxGetIdFn>(f1);
     }
-    *out = g_scratch_addr[dev];
+    void *ctx = nullptr;
+    VG_REQUIRE(g_ctx_get_current(&ctx) == 0, "dd2d_bp_noalloc: cuCtxGetCurrent failed");
+    if (!ctx) {
+        int dev = 0;
+        e = cudaGetDevice(&dev);
+        if (e == cudaSuccess) e = cudaSetDevice(dev);
+        if (e != cudaSuccess) return cuda_status(e, "dd2d_bp_noalloc: device context");
+        VG_REQUIRE(g_ctx_get_current(&ctx) == 0 && ctx, "dd2d_bp_noalloc: no current CUDA context");
+    }
+    VG_REQUIRE(g_ctx_get_id(ctx, id) == 0, "dd2d_bp_noalloc: cuCtxGetId failed");
+    return VG_OK;
+}
+
+// Device address of g_dd2d_scratch in the current context (looked up once
+// per context, keyed on the context's process-unique id).
+int scratch_address(void **out) {
+    std::lock_guard<std::mutex> lk(g_scratch_mu);
+    unsigned long long id = 0;
+    int st = current_context_id(&id);
+    if (st) return st;
+    for (int i = 0; i < g_scratch_n; ++i)
+        if (g_scratch_cache[i].ctx_id == id) {
+            *out = g_scratch_cache[i].addr;
+            return VG_OK;
+        }
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_dd2d_scratch);
+    if (e != cudaSuccess) return cuda_status(e, "dd2d_bp_noalloc: cudaGetSymbolAddress");
+    // a full table drops its oldest entry (that context's next call looks up again)
+    if (g_scratch_n == VG_NOALLOC_MAX_CONTEXTS) {
+        for (int i = 1; i < g_scratch_n; ++i) g_scratch_cache[i - 1] = g_scratch_cache[i];
+        --g_scratch_n;
+    }
+    g_scratch_cache[g_scratch_n++] = ScratchEntry{id, p};
+    *out = p;
     return VG_OK;
 }
 }  // namespace

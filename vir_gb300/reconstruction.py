@@ -149,13 +149,28 @@ def fan_preweight(nu, du, su, DSO, DSD):
 
 
 def fbp_2d(sino, ang_arr, img_shape, geom="par", DSO=0.0, DSD=0.0, du=1.0, su=0.0, d_pix=1.0,
-           filter_type="ramp", cutoff=0.5, real_space=True):
-    """Filtered backprojection of a full scan (pi parallel, 2 pi fan)."""
+           filter_type="ramp", cutoff=0.5, real_space=True, method="pixel"):
+    """Filtered backprojection of a full scan (pi parallel, 2 pi fan).
+
+    method="pixel": the pixel-driven 1/U^2-weighted backprojection
+    (vg_fbp2d_bp).  method="dd" (parallel only): vir's working parallel FBP
+    over 180 degrees, (pi / 2) dd_bp_par_2d(filter_sino(y)), on the GPU
+    distance-driven backprojector."""
     dev = _core.device_of(sino)
     y = _core.to_device(sino, dev)
     trig = _core.trig_cache.get(ang_arr, np.float32, dev)
     na, nu = y.shape
     fan = 1 if geom == "fan" else 0
+    if method == "dd":
+        if fan:
+            raise ValueError("fbp_2d: method='dd' is vir's parallel-beam route")
+        from .sys_mat import dd
+        q = filter_rows_device(y, du, filter_type, cutoff, real_space)
+        img = dd.dd_bp_par_2d(q, ang_arr, img_shape, du=du, su=su, d_pix=d_pix)
+        img.mul_(float(np.pi / 2.0))
+        return _core.to_host_like(img, sino)
+    if method != "pixel":
+        raise ValueError(f"fbp_2d: unknown method {method!r}")
     if fan:
         w = torch.from_numpy(fan_preweight(nu, float(np.float32(du)), float(np.float32(su)),
                                            float(np.float32(DSO)),

@@ -98,7 +98,7 @@ def prepare(src, trg, nPixels=128, dPixels=1.0, origin=0.0, epsilon=1e-5):
                   amax=np.ascontiguousarray(amax.reshape(n), dtype=np.float32),
                   i0=flat(i0, 3).astype(np.int32), iN=flat(iN, 3).astype(np.int32),
                   valid=np.ascontiguousarray(valid.reshape(n)).astype(np.uint8))
-    grid = dict(n=nP, d=dP, Xb=Xb, Yb=Yb, Zb=Zb)
+    grid = dict(n=nP, d=dP, Xb=Xb, Yb=Yb, Zb=Zb, valid=arrays["valid"])
     return shape, grid, arrays
 
 
@@ -145,10 +145,13 @@ def siddons(src, trg, nPixels=128, dPixels=1.0, origin=0.0, ravel=False, flat=Fa
     nP = tuple(int(v) for v in grid["n"])
     rays = np.empty(shape, dtype=object)
     flat_rays = rays.reshape(-1)
+    valid = grid["valid"]
     for r in range(flat_rays.size):
+        if not valid[r]:
+            continue  # a ray that misses the grid stays None, as in the reference
         a, b = off[r], off[r + 1]
-        if a == b:
-            continue  # a ray outside the grid stays None, as in the reference
+        # a ray that enters the grid but keeps no positive length gets empty
+        # arrays (siddon.py:758-820 stores them for every such ray)
         R, L = ind[a:b], ln[a:b]
         if ravel:
             flat_rays[r] = [R.astype(np.int32), L]

@@ -14,8 +14,24 @@ import numpy as np
 from . import phantoms as ph
 
 
+def problem_shapes(n_problems=64, seed=3, sizes=(128, 256, 512, 1024), na_range=(90, 1440)):
+    """(side, views, fan) of each problem of the set, without building any
+    (the same random draws as batched_problems)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for p in range(n_problems):
+        n = int(rng.choice(sizes))
+        na = int(rng.integers(na_range[0], na_range[1] + 1))
+        fan = bool(rng.integers(0, 2))
+        rng.integers(1 << 30)
+        out.append((n, na, fan))
+    return out
+
+
 def batched_problems(n_problems=64, seed=3, sizes=(128, 256, 512, 1024), na_range=(90, 1440),
-                     with_truth=False):
+                     with_truth=False, only=None):
+    """The problem set; ``only`` (problem indices) builds just those problems,
+    each identical to its entry in the full set."""
     rng = np.random.default_rng(seed)
     out, truth = [], []
     for p in range(n_problems):
@@ -23,7 +39,10 @@ def batched_problems(n_problems=64, seed=3, sizes=(128, 256, 512, 1024), na_rang
         na = int(rng.integers(na_range[0], na_range[1] + 1))
         fan = bool(rng.integers(0, 2))
         nu = int(round(1.5 * n))
-        img, e = ph.ellipse_phantom(n, 10, seed=int(rng.integers(1 << 30)), d_pix=1.0, sub=2)
+        pseed = int(rng.integers(1 << 30))
+        if only is not None and p not in only:
+            continue
+        img, e = ph.ellipse_phantom(n, 10, seed=pseed, d_pix=1.0, sub=2)
         if fan:
             DSO = 1.5 * n
             DSD = 2.0 * DSO
