@@ -45,6 +45,18 @@
 #define VG_FAST_DIV 1
 #endif
 
+// VG_FP_MAGIC / VG_BP_MAGIC = 1: the forward projection's inverse edge map
+// and the back projection's table lookups take their floor by a round-down
+// add of 1.5 * 2^23 (an FMA-pipe add whose bit pattern holds the integer)
+// instead of a float-to-int conversion on the XU pipe (the same integer for
+// |x| < 2^22, clamped in the integer domain beyond).
+#ifndef VG_FP_MAGIC
+#define VG_FP_MAGIC 1
+#endif
+#ifndef VG_BP_MAGIC
+#define VG_BP_MAGIC 1
+#endif
+
 namespace {
 
 using namespace vg;
@@ -184,15 +196,16 @@ BpWork bp_ws(const vg_dd2d_geom *g, void *ws) {
 }
 
 // Prefix table of view ia's sinogram row (row[j], global or shared memory)
-// and the view's line scales, by one block of 256 threads.
-template <bool FAN>
+// and the view's line scales, by one block of NT threads (a multiple of 32;
+// wsum holds NT / 32 doubles).
+template <bool FAN, int NT = 256>
 __device__ __forceinline__ void bp_prep_view(const vg_dd2d_geom &g, const float *row, int ia,
                                              const double *__restrict__ trig, BpWork w,
                                              double *wsum) {
     float2 *ts = w.ts + (size_t)ia * (g.nu + 1);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     // contiguous segment per thread
-    const int per = (g.nu + 255) / 256;
+    const int per = (g.nu + NT - 1) / NT;
     const int j0 = threadIdx.x * per;
     double loc = 0.0;
     for (int i = 0; i < per; ++i)
@@ -217,13 +230,13 @@ __device__ __forceinline__ void bp_prep_view(const vg_dd2d_geom &g, const float 
             run += (double)sv;
         }
     }
-    if (threadIdx.x == 255) ts[g.nu] = make_float2((float)(run * du), 0.f);
+    if (threadIdx.x == NT - 1) ts[g.nu] = make_float2((float)(run * du), 0.f);
     // line scales of this view, negated for lines whose edges project in
     // decreasing order (the pixel's interval is then [P(b+1), P(b)])
     const ViewGeo v = view_geo(trig, ia);
     const int no = v.xdrv ? g.ny : g.nx;
     const int nd = v.xdrv ? g.nx : g.ny;
-    for (int io = threadIdx.x; io < no; io += 256) {
+    for (int io = threadIdx.x; io < no; io += NT) {
         const Line L = line_geo<FAN>(g, v, centre_coord(g.d_pix, io, no));
         const float P0 = proj<FAN>(g, v, L.cp, L.co, edge_coord(g.d_pix, 0, nd));
         const float P1 = proj<FAN>(g, v, L.cp, L.co, edge_coord(g.d_pix, nd, nd));
@@ -376,7 +389,14 @@ dd2d_fp_kernel(vg_dd2d_geom g, const float *__restrict__ img, const float *__res
         if (guard) sidx = uc.x <= Pf ? -1.f : (uc.x >= Pl ? (float)nd : sidx);
         // slot of pixel floor(sidx): sentinel below the line, closing edge
         // above (the conversion saturates, so the clamp also bounds +-inf)
+#if VG_FP_MAGIC
+        // floor from the bit pattern of a round-down add of 1.5 * 2^23, clamped
+        // in the integer domain (NaN and +-inf land on a sentinel)
+        const int kb = __float_as_int(__fadd_rd(sidx, 12582912.0f));
+        const int k = min(max(kb, 0x4B400000 - 1), 0x4B400000 + nd) - (0x4B400000 - 1);
+#else
         const int k = min(max(__float2int_rd(sidx), -1), nd) + 1;
+#endif
         const float2 t = Eb[pad_idx(k)];
         return fmaf(t.y, uc.x, t.x);
     };
@@ -487,10 +507,18 @@ __device__ __forceinline__ float rcp_approx(float x) {
 
 __device__ __forceinline__ float bp_G(const float2 *__restrict__ ts, int nu, float t) {
     // t: position in bins from U_0.  Before U_0 entry 0 gives x_0 = 0; past
-    // U_nu entry nu holds (T_nu, 0); the conversion saturates.
+    // U_nu entry nu holds (T_nu, 0).
     const float tc = fmaxf(t, 0.f);
+#if VG_BP_MAGIC
+    // floor from the bit pattern of a round-down add of 1.5 * 2^23 (FMA pipe),
+    // clamped in the integer domain (huge t lands on entry nu)
+    const int jb = min(__float_as_int(__fadd_rd(tc, 12582912.0f)), 0x4B400000 + nu);
+    const float2 e = __ldg(ts + (jb - 0x4B400000));
+#else
+    // the conversion saturates
     const int j = min(__float2int_rz(tc), nu);
     const float2 e = __ldg(ts + j);
+#endif
     return fmaf(e.y, tc, e.x);
 }
 
@@ -666,10 +694,13 @@ int launch_fp_fan(int v, const vg_dd2d_geom *g, const float *img, const float *i
     }
 }
 
+// Variant in use: the caller's, else the tile heuristic.
+int fp_variant_used(const vg_dd2d_geom *g) { return g->variant ? g->variant : fp_variant_for(g); }
+
 int launch_fp(const vg_dd2d_geom *g, const float *img, const float *imgT, const double *trig,
               float *out, int mode, const float *y, const float *inv_w, cudaStream_t st,
               BpWork pw = BpWork{nullptr, nullptr}) {
-    const int v = g->variant ? g->variant : fp_variant_for(g);
+    const int v = fp_variant_used(g);
     return g->fan ? launch_fp_fan<true>(v, g, img, imgT, trig, out, mode, y, inv_w, st, pw)
                   : launch_fp_fan<false>(v, g, img, imgT, trig, out, mode, y, inv_w, st, pw);
 }
@@ -677,7 +708,7 @@ int launch_fp(const vg_dd2d_geom *g, const float *img, const float *imgT, const 
 // The SIRT forward projection can also write the back projection's tables
 // (mode 2) when one block of 8 warps holds all bins of a view.
 bool fp_builds_bp_tables(const vg_dd2d_geom *g) {
-    const int v = g->variant ? g->variant : fp_variant_for(g);
+    const int v = fp_variant_used(g);
     if (v < 1 || v > FP_NVARIANTS) return false;
     return FP_VARIANTS[v - 1].warps == 8 && 32 * FP_VARIANTS[v - 1].maxb >= g->nu;
 }
@@ -718,7 +749,7 @@ extern "C" int vg_dd2d_fp(const vg_dd2d_geom *g, const float *img, const float *
 extern "C" int vg_dd2d_fp_variants(void) { return FP_NVARIANTS; }
 
 extern "C" int vg_dd2d_fp_default_variant(const vg_dd2d_geom *g) {
-    return check_geom(g) ? 0 : fp_variant_for(g);
+    return check_geom(g) ? 0 : fp_variant_used(g);
 }
 
 extern "C" size_t vg_dd2d_workspace_bytes(const vg_dd2d_geom *g) {
