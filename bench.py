@@ -226,10 +226,11 @@ EXTRA = {
           "180 views over pi, 367 bins of 1 mm",
     "c3": "batched SIRT: 64 parallel/fan problems (seed 3), sides in {128,256,512,1024}, "
           "90-1440 views, 1.5x detectors; 50 updates, one CUDA graph vs one launch per step",
-    "c4": "3D cone DD FP + BP + FDK: 512^3 volume of 20 random ellipsoids, 0.5 mm voxels, "
-          "720 views over 2pi, 1024x768 detector at 0.8 mm, DSO 600 mm, DSD 1100 mm",
-    "c5": "3D cone DD FP + BP: 256^3 volume of 20 random ellipsoids, 1 mm voxels, 360 views "
-          "over 2pi, 512x384 detector at 1.6 mm, DSO 600 mm, DSD 1100 mm",
+    "c4": "3D cone DD and separable-footprint FP + BP, FDK: 512^3 volume of 20 random "
+          "ellipsoids, 0.5 mm voxels, 720 views over 2pi, 1024x768 detector at 0.8 mm, DSO 600 mm, "
+          "DSD 1100 mm",
+    "c5": "3D cone DD and separable-footprint FP + BP: 256^3 volume of 20 random ellipsoids, "
+          "1 mm voxels, 360 views over 2pi, 512x384 detector at 1.6 mm, DSO 600 mm, DSD 1100 mm",
     "bh": "beam-hardening pre-correction of a 720 x 1024 x 768 float32 logged sinogram (the "
           "C4 detector): water polynomial with np.polyfit coefficients (float64 result) and with "
           "Python-float coefficients (float32 result), 1000-entry spectrum table (interp1d), "
@@ -664,6 +665,17 @@ def run_workload(args):
     line.update({"kernel_ms": {"fp": t_fp, "bp": t_bp},
                  "fwd_back_gups": 2 * units / ((t_fp + t_bp) / 1e3) / 1e9,
                  "roofline_fp": _roof(units, t_fp, peak), "roofline_bp": _roof(units, t_bp, peak)})
+    if wl in ("c4", "c5"):
+        # the separable-footprint pair (SF-TR) on the same cone geometry
+        from vir_gb300.sys_mat import sp
+        sfp = lambda: sp.sf_fp_cone_3d(x, angs, nu, nv, 600.0, 1100.0, **kw)
+        sbp = lambda: sp.sf_bp_cone_3d(y, angs, (n, n, n), 600.0, 1100.0, **kw)
+        s_fp, s_bp = _event_ms(sfp, reps, stream), _event_ms(sbp, reps, stream)
+        line["sf"] = {"kernel_ms": {"fp": s_fp, "bp": s_bp},
+                      "fwd_back_gups": 2 * units / ((s_fp + s_bp) / 1e3) / 1e9,
+                      "roofline_fp": _roof(units, s_fp, peak),
+                      "roofline_bp": _roof(units, s_bp, peak),
+                      "note": "BP time includes the l_theta weighting of the sinogram"}
     if wl == "c4":
         from vir_gb300 import autograd as ag
         from vir_gb300 import reconstruction as rc

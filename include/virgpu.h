@@ -276,6 +276,30 @@ int vg_dd3d_bp(const vg_dd3d_geom *g, const float *sino, const double *trig,
                float *vol, void *workspace, size_t workspace_bytes,
                void *stream);
 
+/* ---- 3D cone-beam separable footprint (SF-TR) --------------------------- */
+
+/* The separable-footprint cone projector that vir's sys_mat/sp.py:93-211
+ * (CTGeometry, footprint1D, forward_project, back_project: no rotation
+ * angles) sketches: trapezoid transaxial and rectangle axial footprints with
+ * the A2 amplitude of Long, Fessler & Balter (IEEE TMI 29(11), 2010), on the
+ * circular cone geometry of vg_dd3d_geom (dd_fp_cone_3d, dd.py:815).  Voxel
+ * (x, y, z) adds f l_phi0 l_theta F1 F2 to cell (u, v): F1 the unit
+ * trapezoid through the projections of the column's four corners, F2 the
+ * rectangle [M (z - d/2), M (z + d/2)], M = DSD / (DSO - o), both averaged
+ * over the cell; l_phi0 = d |r| / max(|r_x|, |r_y|) for the transaxial ray r
+ * through the column centre, l_theta = sqrt(1 + v^2 / (u^2 + DSD^2)) at the
+ * cell centre.
+ * vg_sf3d_fp: sino (na, nu, nv) = the line integrals above, gather form.
+ * vg_sf3d_bp: vol = its exact adjoint; workspace of
+ *   vg_sf3d_workspace_bytes(g) bytes (the l_theta-weighted sinogram of a
+ *   chunk of views, at most 256 MiB or one view), 4-byte aligned.
+ * The volume must lie inside the source circle (half diagonal below DSO). */
+size_t vg_sf3d_workspace_bytes(const vg_dd3d_geom *g);
+int vg_sf3d_fp(const vg_dd3d_geom *g, const float *vol, const double *trig, float *sino,
+               void *stream);
+int vg_sf3d_bp(const vg_dd3d_geom *g, const float *sino, const double *trig, float *vol,
+               void *workspace, size_t workspace_bytes, void *stream);
+
 /* ---- translational "square" geometry ------------------------------------ */
 
 /* dd_fp_square / dd_bp_square (sys_mat/dd.py:903, 1104): an n x n x nz

@@ -682,6 +682,124 @@ def fdk(sino, ang_arr, img_shape, DSO, DSD, du=1.0, dv=1.0, su=0.0, sv=0.0, d_pi
     return vol * (np.pi / (2.0 * na))
 
 
+# --- 3D cone-beam separable footprint (SF-TR) ------------------------------
+#
+# vir's sys_mat/sp.py:93-211 (CTGeometry, footprint1D, forward_project,
+# back_project) is a toy with no rotation angles.  This restates the
+# separable-footprint cone projector it stands in for -- trapezoid
+# transaxial and rectangle axial footprints with the "A2" amplitude of
+# Long, Fessler & Balter, "3D forward and back-projection for X-ray CT using
+# separable footprints", IEEE TMI 29(11), 2010 -- on vir's circular cone
+# geometry of dd_fp_cone_3d (dd.py:815-888): source at DSO (cos b, sin b),
+# o = c x + s y, p = -s x + c y, u = DSD p / (DSO - o), v = DSD z / (DSO - o),
+# cells u_j = du (j - nu/2 + su), v_l = dv (l - nv/2 + sv) (edges), volume
+# (nx, ny, nz) of cubic voxels d_pix, sinogram (na, nu, nv).  Per voxel and
+# view:
+#   F1: trapezoid through the sorted projections tau0..tau3 of the column's
+#       four corners, height 1, averaged over each u cell;
+#   F2: rectangle [M (z - d/2), M (z + d/2)], M = DSD / (DSO - o_centre),
+#       averaged over each v cell;
+#   amplitude l_phi0 l_theta: l_phi0 = d |r| / max(|r_x|, |r_y|) with r the
+#       transaxial ray from the source to the column centre, and
+#       l_theta = sqrt(1 + v_c^2 / (u_c^2 + DSD^2)) at the cell centre.
+# FP: sino[j, l] = sum_voxels f l_phi0 l_theta(j, l) F1(j) F2(l) (line
+# integrals); BP: its exact adjoint.  numpy float64, one view at a time.
+# The geometry agrees with vir's detector-area-averaged analytic cone-beam
+# sphere (analytic_sino.py:563, a golden fixture): the projection of a
+# voxelised sphere is within the voxelisation error of it.
+
+def _sf_trap_cum(u, t0, t1, t2, t3):
+    """Integral of the unit-height trapezoid (t0, t1, t2, t3) from -inf to u."""
+    r1 = np.maximum(t1 - t0, 1e-300)
+    r3 = np.maximum(t3 - t2, 1e-300)
+    a = np.where(u <= t0, 0.0, np.where(u <= t1, (u - t0) ** 2 / (2 * r1), 0.0))
+    b = np.where((u > t1) & (u <= t2), 0.5 * (t1 - t0) + (u - t1), 0.0)
+    c = np.where((u > t2) & (u <= t3), 0.5 * (t1 - t0) + (t2 - t1) + 0.5 * (t3 - t2)
+                 - (t3 - u) ** 2 / (2 * r3), 0.0)
+    d = np.where(u > t3, 0.5 * (t1 - t0) + (t2 - t1) + 0.5 * (t3 - t2), 0.0)
+    return a + b + c + d
+
+
+def _sf_cone_view(c, s, shape, nu, nv, du, dv, su, sv, d_pix, DSO, DSD):
+    """Cells and weights of one view: per voxel and (u cell t, v cell r) the
+    cell (j, l) and weight, flattened voxel-major."""
+    nx, ny, nz = shape
+    d = d_pix
+    X = (d * (np.arange(nx) + 0.5 - 0.5 * nx))[:, None]
+    Y = (d * (np.arange(ny) + 0.5 - 0.5 * ny))[None, :]
+    h = 0.5 * d
+    us = []
+    for ex in (-h, h):
+        for ey in (-h, h):
+            o = c * (X + ex) + s * (Y + ey)
+            p = -s * (X + ex) + c * (Y + ey)
+            us.append(DSD * p / (DSO - o))
+    tau = np.sort(np.stack(np.broadcast_arrays(*us), -1), axis=-1)       # (nx, ny, 4)
+    oc = c * X + s * Y
+    M = np.broadcast_to(DSD / (DSO - oc), (nx, ny))
+    rx, ry = np.broadcast_arrays(X - DSO * c, Y - DSO * s)
+    lphi = d * np.sqrt(rx ** 2 + ry ** 2) / np.maximum(np.abs(rx), np.abs(ry))
+    U0, V0 = du * (-0.5 * nu + su), dv * (-0.5 * nv + sv)
+    j0 = np.floor((tau[..., 0] - U0) / du).astype(np.int64)
+    j3 = np.floor((tau[..., 3] - U0) / du).astype(np.int64)
+    K = int((j3 - j0).max()) + 1
+    uj, uw = [], []
+    for t in range(K):
+        j = j0 + t
+        a = U0 + du * j
+        tt = np.moveaxis(tau, -1, 0)
+        w = (_sf_trap_cum(a + du, *tt) - _sf_trap_cum(a, *tt)) / du
+        w = np.where((j >= 0) & (j < nu) & (j <= j3), w * lphi, 0.0)
+        uj.append(np.clip(j, 0, nu - 1))
+        uw.append(w)
+    uj, uw = np.stack(uj, -1), np.stack(uw, -1)                          # (nx, ny, K)
+    Z = d * (np.arange(nz) - 0.5 * nz)                                    # slice lower edges
+    vs = M[..., None] * Z[None, None, :]
+    ve = M[..., None] * (Z + d)[None, None, :]
+    q0 = np.floor((vs - V0) / dv).astype(np.int64)
+    q1 = np.floor((ve - V0) / dv).astype(np.int64)
+    R = int((q1 - q0).max()) + 1
+    vq, vw = [], []
+    for r in range(R):
+        q = q0 + r
+        lo, hi = V0 + dv * q, V0 + dv * (q + 1)
+        ov = (np.minimum(ve, hi) - np.maximum(vs, lo)) / dv
+        ov = np.where((q >= 0) & (q < nv) & (q <= q1) & (ov > 0), ov, 0.0)
+        vq.append(np.clip(q, 0, nv - 1))
+        vw.append(ov)
+    vq, vw = np.stack(vq, -1), np.stack(vw, -1)                          # (nx, ny, nz, R)
+    uc = U0 + du * (np.arange(nu) + 0.5)
+    vc = V0 + dv * (np.arange(nv) + 0.5)
+    lth = np.sqrt(1.0 + vc[None, :] ** 2 / (uc[:, None] ** 2 + DSD ** 2))  # (nu, nv)
+    J = np.broadcast_to(uj[:, :, None, :, None], (nx, ny, nz, K, R))
+    Q = np.broadcast_to(vq[:, :, :, None, :], (nx, ny, nz, K, R))
+    W = uw[:, :, None, :, None] * vw[:, :, :, None, :] * lth[J, Q]
+    return J.reshape(nx * ny * nz, -1), Q.reshape(nx * ny * nz, -1), W.reshape(nx * ny * nz, -1)
+
+
+def sf_fp_cone_3d(img, ang_arr, nu, nv, DSO, DSD, du=1.0, dv=1.0, su=0.0, sv=0.0, d_pix=1.0):
+    f = np.asarray(img, np.float64)
+    c_, s_ = _dd_trig(ang_arr)
+    out = np.zeros((c_.size, nu, nv))
+    fv = f.reshape(-1, 1)
+    for ia in range(c_.size):
+        J, Q, W = _sf_cone_view(c_[ia], s_[ia], f.shape, nu, nv, du, dv, su, sv, d_pix, DSO, DSD)
+        np.add.at(out[ia], (J.ravel(), Q.ravel()), (W * fv).ravel())
+    return out
+
+
+def sf_bp_cone_3d(sino, ang_arr, img_shape, DSO, DSD, du=1.0, dv=1.0, su=0.0, sv=0.0, d_pix=1.0):
+    y = np.asarray(sino, np.float64)
+    c_, s_ = _dd_trig(ang_arr)
+    na, nu, nv = y.shape
+    vol = np.zeros(int(np.prod(img_shape)))
+    for ia in range(na):
+        J, Q, W = _sf_cone_view(c_[ia], s_[ia], tuple(img_shape), nu, nv, du, dv, su, sv, d_pix,
+                                DSO, DSD)
+        vol += (W * y[ia][J, Q]).sum(-1)
+    return vol.reshape(img_shape)
+
+
 # --- SIRT (sys_mat/sirt_dd.py:23-76) ---------------------------------------
 
 def sirt(sino, fp, bp, img_shape, gamma=1.0, iters=100, x0=1e-5, W_sino=None, W_img=None):

@@ -55,3 +55,25 @@ def vg():
     import vir_gb300
     vir_gb300.load()
     return vir_gb300
+
+
+def voxel_sphere(n, d, sphere, sub=4, mu=1.0):
+    """(n, n, n) volume of cubic voxels d (centred grid) holding a sphere
+    (x0, y0, z0, r) of attenuation mu, each voxel the fraction of its sub^3
+    sample points inside."""
+    ax = d * (np.arange(n) + 0.5 - n / 2)
+    off = ((np.arange(sub) + 0.5) / sub - 0.5) * d
+    x0, y0, z0, r = (float(v) for v in sphere)
+    vol = np.zeros((n, n, n))
+    for a in off:
+        dx2 = (ax + a - x0)[:, None, None] ** 2
+        for b in off:
+            dy2 = (ax + b - y0)[None, :, None] ** 2
+            for c in off:
+                vol += (dx2 + dy2 + (ax + c - z0)[None, None, :] ** 2) <= r * r
+    return vol * (mu / sub ** 3)
+
+
+@pytest.fixture(scope="session")
+def sphere_vol():
+    return voxel_sphere

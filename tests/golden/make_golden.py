@@ -323,6 +323,19 @@ def main():
                               src_prms=np.array(prms[2]), det_prms=np.array(prms[3]),
                               srt_prms=np.array(prms[4]))
 
+    # --- analytic cone-beam sphere, detector-area averaged (analytic_sino.py:563) --
+    # the pin of the separable-footprint cone projector (vir has no working one)
+    import vir.sys_mat.analytic_sino as an
+    sph = np.array([2.0, -3.0, 1.5, 7.0])
+    a_sf = np.linspace(0, 2 * np.pi, 8, endpoint=False)
+    nu_s, nv_s, du_s, dv_s, DSO_s, DSD_s = 64, 48, 0.8, 0.8, 60.0, 110.0
+    u_s = du_s * (np.arange(nu_s) + 0.5 - nu_s / 2)
+    v_s = dv_s * (np.arange(nv_s) + 0.5 - nv_s / 2)
+    out["sphere_cone_vol"] = dict(sphere=sph, angs=a_sf, nu=np.int32(nu_s), nv=np.int32(nv_s),
+                                  du=du_s, dv=dv_s, DSO=DSO_s, DSD=DSD_s,
+                                  proj=an.analytic_sino_sphere_cone_vol(sph, a_sf, u_s, v_s, DSO_s,
+                                                                        DSD_s))
+
     # --- fan FBP parts (processing/reconstruction.py:99-107, proj2.py:580-616) --
     # vir's fan_fbp cannot run; its pre-weight and its Hsieh backprojector can,
     # executed from their own source (the modules' imports are stale)

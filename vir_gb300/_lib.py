@@ -101,6 +101,9 @@ _PROTOS = {
     "vg_fbp2d_bp": [ctypes.POINTER(DD2DGeom), c_void_p, c_void_p, c_void_p, c_void_p],
     "vg_dd3d_fp": [ctypes.POINTER(DD3DGeom), c_void_p, c_void_p, c_void_p, c_void_p, c_size_t,
                    c_void_p],
+    "vg_sf3d_fp": [ctypes.POINTER(DD3DGeom), c_void_p, c_void_p, c_void_p, c_void_p],
+    "vg_sf3d_bp": [ctypes.POINTER(DD3DGeom), c_void_p, c_void_p, c_void_p, c_void_p, c_size_t,
+                   c_void_p],
     "vg_dd3d_bp": [ctypes.POINTER(DD3DGeom), c_void_p, c_void_p, c_void_p, c_void_p, c_size_t,
                    c_void_p],
     "vg_dd_square_fp": [ctypes.POINTER(DDSquareGeom), c_void_p, c_void_p, c_void_p],
@@ -172,6 +175,8 @@ def load(build_if_missing: bool = True):
         L.vg_dd2d_workspace_bytes.restype = c_size_t
         L.vg_dd3d_workspace_bytes.argtypes = [ctypes.POINTER(DD3DGeom)]
         L.vg_dd3d_workspace_bytes.restype = c_size_t
+        L.vg_sf3d_workspace_bytes.argtypes = [ctypes.POINTER(DD3DGeom)]
+        L.vg_sf3d_workspace_bytes.restype = c_size_t
         L.vg_dd_square_workspace_bytes.argtypes = [ctypes.POINTER(DDSquareGeom)]
         L.vg_dd_square_workspace_bytes.restype = c_size_t
         L.vg_compact_blocks.argtypes = [ctypes.c_longlong]
@@ -199,7 +204,7 @@ def exported_symbols():
     return list(_PROTOS) + ["vg_version", "vg_last_error", "vg_status_string",
                             "vg_dd2d_workspace_bytes", "vg_dd2d_noalloc_scratch_bytes",
                             "vg_dd2d_fp_variants", "vg_dd2d_fp_default_variant", "vg_dd2d_sirt_launches",
-                            "vg_list_bp_workspace_bytes", "vg_dd3d_workspace_bytes",
+                            "vg_list_bp_workspace_bytes", "vg_dd3d_workspace_bytes", "vg_sf3d_workspace_bytes",
                             "vg_dd_square_workspace_bytes", "vg_compact_blocks",
                             "vg_siddon2d_bp_workspace_bytes"]
 

@@ -1,0 +1,540 @@
+// 3D cone-beam separable-footprint projector pair (SF-TR, amplitude A2).
+//
+// vir's sys_mat/sp.py:93-211 (CTGeometry, footprint1D, forward_project,
+// back_project) sketches a separable-footprint cone projector without
+// rotation angles.  This is the method it stands in for, the trapezoid /
+// rectangle separable footprints of Long, Fessler & Balter, "3D forward and
+// back-projection for X-ray CT using separable footprints", IEEE TMI 29(11),
+// 2010, on vir's circular cone geometry of dd_fp_cone_3d (sys_mat/dd.py:815):
+// source at DSO (cos b, sin b), o = c x + s y, p = -s x + c y,
+// u = DSD p / (DSO - o), v = DSD z / (DSO - o); cell edges
+// U_j = du (j - nu/2 + su), V_l = dv (l - nv/2 + sv); volume (nx, ny, nz) of
+// cubic voxels d; sinogram (na, nu, nv), v fastest.  Voxel (x, y, z) adds
+//     f * l_phi0 * l_theta(j, l) * F1(j) * F2(l)
+// to cell (j, l), where
+//   F1(j): the unit trapezoid through the sorted projections tau0..tau3 of
+//          the column's four corners (x +- d/2, y +- d/2), averaged over u cell j;
+//   F2(l): the rectangle [M (z - d/2), M (z + d/2)], M = DSD / (DSO - o(x, y)),
+//          averaged over v cell l;
+//   l_phi0 = d |r| / max(|r_x|, |r_y|), r = (x, y) - DSO (c, s): the path
+//          length of the transaxial ray through the column centre;
+//   l_theta(j, l) = sqrt(1 + v_l^2 / (u_j^2 + DSD^2)) at the cell centre.
+// The forward projection returns these line integrals; the back projection
+// is its exact adjoint (vir has no back projector for this footprint).
+//
+//  FP (sf3d_fp_kernel): block = (view, 32 u x 64 v cells), thread = 4 u
+//    cells (warp) x 2 v cells (lanes).  For each orthogonal pixel line whose
+//    columns reach the tile, the block tabulates in shared memory the
+//    columns' footprints, the covering columns and F1 weights of each u
+//    cell, and each column's v profile over the tile's v cells
+//    g(c, l) = sum_z f(c, z) F2(l; c, z); each cell then adds
+//    F1 * l_phi0 * g over its 1-6 covering columns.  Lines where a u cell
+//    meets more columns, or the tile more than 64, take a per-cell path.
+//  BP (sf3d_bp_kernel): the sinogram is first multiplied by l_theta
+//    (sf3d_weight, into the workspace, a chunk of views at a time); block =
+//    8 x 8 columns x 32 slices, thread = one slice of 8 columns; per view a
+//    table of the columns' u cells and F1 l_phi0 weights (at most 4 u cells
+//    per column, else a per-voxel path), then each voxel gathers its 1-3 v
+//    cells x 4 u cells.
+#include "vg_common.cuh"
+
+namespace {
+
+using namespace vg;
+
+__device__ __forceinline__ float2 view_cs(const double *__restrict__ trig, int ia) {
+    return make_float2((float)__ldg(trig + 2 * ia), (float)__ldg(trig + 2 * ia + 1));
+}
+
+__device__ __forceinline__ float ucen(const vg_dd3d_geom &g, int j) {
+    return g.du * ((float)j + 0.5f - 0.5f * g.nu + g.su);
+}
+__device__ __forceinline__ float uedge(const vg_dd3d_geom &g, int j) {
+    return g.du * ((float)j - 0.5f * g.nu + g.su);
+}
+__device__ __forceinline__ float vedge(const vg_dd3d_geom &g, int l) {
+    return g.dv * ((float)l - 0.5f * g.nv + g.sv);
+}
+__device__ __forceinline__ float vcen(const vg_dd3d_geom &g, int l) {
+    return g.dv * ((float)l + 0.5f - 0.5f * g.nv + g.sv);
+}
+__device__ __forceinline__ float vox(float d, int i, int n) { return d * ((float)i + 0.5f - 0.5f * n); }
+
+// Footprint of column (x, y): sorted corner projections, l_phi0 and the
+// slice height on the detector M d.
+struct SfCol {
+    float t0, t1, t2, t3, lphi, mz;
+};
+
+__device__ __forceinline__ void cswap(float &a, float &b) {
+    const float lo = fminf(a, b), hi = fmaxf(a, b);
+    a = lo;
+    b = hi;
+}
+
+__device__ __forceinline__ SfCol sf_col(const vg_dd3d_geom &g, float c, float s, float x, float y) {
+    const float h = 0.5f * g.d_pix;
+    float u[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const float xx = x + ((q & 1) ? h : -h), yy = y + ((q & 2) ? h : -h);
+        const float o = fmaf(c, xx, s * yy), p = fmaf(-s, xx, c * yy);
+        u[q] = g.DSD * p / (g.DSO - o);
+    }
+    cswap(u[0], u[1]);
+    cswap(u[2], u[3]);
+    cswap(u[0], u[2]);
+    cswap(u[1], u[3]);
+    cswap(u[1], u[2]);
+    SfCol C;
+    C.t0 = u[0]; C.t1 = u[1]; C.t2 = u[2]; C.t3 = u[3];
+    const float rx = x - g.DSO * c, ry = y - g.DSO * s;
+    C.lphi = g.d_pix * sqrtf(rx * rx + ry * ry) / fmaxf(fabsf(rx), fabsf(ry));
+    C.mz = g.DSD * g.d_pix / (g.DSO - fmaf(c, x, s * y));
+    return C;
+}
+
+// Integral of the unit trapezoid (t0, t1, t2, t3) from -inf to u.
+__device__ __forceinline__ float trap_cum(float u, const SfCol &C) {
+    if (u <= C.t0) return 0.f;
+    const float a = 0.5f * (C.t1 - C.t0);
+    if (u <= C.t1) {
+        const float e = u - C.t0;
+        return e * e / (2.f * (C.t1 - C.t0));
+    }
+    if (u <= C.t2) return a + (u - C.t1);
+    const float b = a + (C.t2 - C.t1);
+    const float r = 0.5f * (C.t3 - C.t2);
+    if (u <= C.t3) {
+        const float e = C.t3 - u;
+        return b + r - e * e / (2.f * (C.t3 - C.t2));
+    }
+    return b + r;
+}
+
+// F1 averaged over [ua, ub] (cell width du), times l_phi0
+__device__ __forceinline__ float uweight(const SfCol &C, float ua, float ub, float inv_du) {
+    return (trap_cum(ub, C) - trap_cum(ua, C)) * inv_du * C.lphi;
+}
+
+// sum_z f(z) |[M d (z - nz/2), M d (z + 1 - nz/2)] ∩ [va, vb]| / dv for one
+// column (f at col, slices contiguous)
+__device__ __forceinline__ float vprofile(const vg_dd3d_geom &g, const float *__restrict__ col,
+                                          float mz, float va, float vb, float inv_dv) {
+    const float hz = 0.5f * g.nz;
+    const float sa = va / mz + hz, sb = vb / mz + hz;
+    const int z0 = max((int)floorf(sa), 0), z1 = min((int)floorf(sb), g.nz - 1);
+    float acc = 0.f;
+    for (int z = z0; z <= z1; ++z) {
+        const float lo = fmaxf(va, mz * ((float)z - hz)), hi = fminf(vb, mz * ((float)z + 1.f - hz));
+        const float ov = hi - lo;
+        if (ov > 0.f) acc = fmaf(__ldg(col + z), ov, acc);
+    }
+    return acc * inv_dv;
+}
+
+// Fractional pixel index, along the driving axis, of the point of the line
+// at orthogonal coordinate `cen` that projects to u (x, y = (b, cen) when
+// X-driven, else (cen, b)):  b (DSD pd + u od) = u (DSO - oc) - DSD pc.
+__device__ __forceinline__ float unproj_idx(const vg_dd3d_geom &g, float c, float s, bool xdrv,
+                                            float cen, float u, int nd) {
+    const float pd = xdrv ? -s : c, od = xdrv ? c : s;
+    const float pc = xdrv ? c * cen : -s * cen, oc = xdrv ? s * cen : c * cen;
+    const float b = (u * (g.DSO - oc) - g.DSD * pc) / (g.DSD * pd + u * od);
+    return b / g.d_pix + 0.5f * nd;
+}
+
+// ---------------------------------------------------------------------------
+// Forward projection
+// ---------------------------------------------------------------------------
+constexpr int SU = 32, SV = 64, SCMAX = 64, SKMAX = 6;
+
+struct SfFpTab {
+    SfCol col[SCMAX];
+    int off[SCMAX];     // voxel index of (column, z = 0)
+    int cf[SU], cn[SU]; // covering columns (table index, count) per u cell
+    float w[SU][SKMAX]; // F1 l_phi0 weights of those columns
+    float gv[SCMAX][SV];
+    int wide;
+};
+
+// one cell's share of one line, straight from global memory (any geometry)
+__device__ __noinline__ float sf_cell_line(const vg_dd3d_geom &g, const float *__restrict__ vol,
+                                           float c, float s, bool xdrv, int nd, int no, int io,
+                                           int kA, int kB, float Ua, float Ub, float Va, float Vb) {
+    const float inv_du = 1.0f / g.du, inv_dv = 1.0f / g.dv;
+    const float cen = vox(g.d_pix, io, no);
+    float part = 0.f;
+    for (int k = kA; k <= kB; ++k) {
+        const float b = vox(g.d_pix, k, nd);
+        const float x = xdrv ? b : cen, y = xdrv ? cen : b;
+        const SfCol C = sf_col(g, c, s, x, y);
+        if (C.t3 <= Ua || C.t0 >= Ub) continue;
+        const float w = uweight(C, Ua, Ub, inv_du);
+        if (w == 0.f) continue;
+        const int ix = xdrv ? k : io, iy = xdrv ? io : k;
+        part = fmaf(w, vprofile(g, vol + ((size_t)ix * g.ny + iy) * g.nz, C.mz, Va, Vb, inv_dv), part);
+    }
+    return part;
+}
+
+__global__ void __launch_bounds__(256)
+sf3d_fp_kernel(vg_dd3d_geom g, const float *__restrict__ vol, const double *__restrict__ trig,
+               float *__restrict__ sino) {
+    __shared__ SfFpTab T;
+    const int ia = blockIdx.z;
+    const int u0 = blockIdx.y * SU, v0 = blockIdx.x * SV;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const float2 cs = view_cs(trig, ia);
+    const float c = cs.x, s = cs.y;
+    const bool xdrv = fabsf(s) >= fabsf(c);
+    const int nd = xdrv ? g.nx : g.ny, no = xdrv ? g.ny : g.nx;
+    const float inv_du = 1.0f / g.du, inv_dv = 1.0f / g.dv;
+    const int nuT = min(SU, g.nu - u0), nvT = min(SV, g.nv - v0);
+    const float TUa = uedge(g, u0), TUb = uedge(g, u0 + nuT);
+    // the inverse edge map has a pole at u = -DSD pd / od; a tile holding it
+    // (or within a cell of it) cannot bound its columns through the map
+    const float pd = xdrv ? -s : c, od = xdrv ? c : s;
+    bool tile_pole = false;
+    if (od != 0.f) {
+        const float up = -g.DSD * pd / od;
+        tile_pole = up >= TUa - 2.f * g.du && up <= TUb + 2.f * g.du;
+    }
+    float acc[8], grp[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) acc[q] = grp[q] = 0.f;
+    int ngrp = 0;
+    for (int io = 0; io < no; ++io) {
+        const float cen = vox(g.d_pix, io, no);
+        // columns of this line whose footprint can reach the tile: the map
+        // of the tile's u edges (widened by a cell) on both boundaries of
+        // the line, one column of margin each side
+        int kA = 0, kB = nd - 1;
+        if (!tile_pole) {
+            const float h = 0.5f * g.d_pix;
+            const float a0 = unproj_idx(g, c, s, xdrv, cen - h, TUa - g.du, nd);
+            const float a1 = unproj_idx(g, c, s, xdrv, cen + h, TUa - g.du, nd);
+            const float b0 = unproj_idx(g, c, s, xdrv, cen - h, TUb + g.du, nd);
+            const float b1 = unproj_idx(g, c, s, xdrv, cen + h, TUb + g.du, nd);
+            const float lo = fminf(fminf(a0, a1), fminf(b0, b1)), hi = fmaxf(fmaxf(a0, a1), fmaxf(b0, b1));
+            kA = max((int)floorf(fmaxf(lo, -2.f)) - 1, 0);
+            kB = min((int)floorf(fminf(hi, (float)nd + 2.f)) + 1, nd - 1);
+        }
+        if (kA > kB) continue;  // block-uniform
+        const int nk = kB - kA + 1;
+        const bool big = nk > SCMAX;
+        __syncthreads();  // the previous line's tables are no longer read
+        if (!big) {
+            if (tid < nk) {
+                const int k = kA + tid;
+                const float b = vox(g.d_pix, k, nd);
+                T.col[tid] = sf_col(g, c, s, xdrv ? b : cen, xdrv ? cen : b);
+                const int ix = xdrv ? k : io, iy = xdrv ? io : k;
+                T.off[tid] = (ix * g.ny + iy) * g.nz;
+            }
+            if (tid == 0) T.wide = 0;
+        }
+        __syncthreads();
+        if (!big) {
+            // covering columns and weights of each u cell (the columns'
+            // footprints move monotonically along the line, so the covering
+            // ones are consecutive)
+            if (tid < nuT) {
+                const float ua = uedge(g, u0 + tid), ub = uedge(g, u0 + tid + 1);
+                int first = -1, n = 0;
+                for (int t = 0; t < nk; ++t) {
+                    const SfCol &C = T.col[t];
+                    if (C.t3 > ua && C.t0 < ub) {
+                        if (first < 0) first = t;
+                        if (n < SKMAX) T.w[tid][n] = uweight(C, ua, ub, inv_du);
+                        ++n;
+                    } else if (first >= 0) {
+                        break;
+                    }
+                }
+                if (n > SKMAX) T.wide = 1;
+                T.cf[tid] = max(first, 0);
+                T.cn[tid] = min(n, SKMAX);
+            }
+            // v profiles of the table's columns over the tile's v cells
+            for (int p = tid; p < nk * SV; p += 256) {
+                const int t = p / SV, l = p % SV;
+                float gval = 0.f;
+                if (l < nvT)
+                    gval = vprofile(g, vol + T.off[t], T.col[t].mz, vedge(g, v0 + l),
+                                    vedge(g, v0 + l + 1), inv_dv);
+                T.gv[t][l] = gval;
+            }
+        }
+        __syncthreads();
+        float part[8];
+        if (!big && !T.wide) {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int j = 4 * warp + q;
+                float pa = 0.f, pb = 0.f;
+                if (j < nuT) {
+                    const int f0 = T.cf[j], n = T.cn[j];
+                    for (int m = 0; m < n; ++m) {
+                        const float w = T.w[j][m];
+                        pa = fmaf(w, T.gv[f0 + m][lane], pa);
+                        pb = fmaf(w, T.gv[f0 + m][32 + lane], pb);
+                    }
+                }
+                part[2 * q] = pa;
+                part[2 * q + 1] = pb;
+            }
+        } else {
+#pragma unroll 1
+            for (int q = 0; q < 4; ++q) {
+                const int j = u0 + 4 * warp + q;
+#pragma unroll 1
+                for (int hh = 0; hh < 2; ++hh) {
+                    const int l = v0 + 32 * hh + lane;
+                    part[2 * q + hh] = (j < g.nu && l < g.nv)
+                        ? sf_cell_line(g, vol, c, s, xdrv, nd, no, io, kA, kB, uedge(g, j),
+                                       uedge(g, j + 1), vedge(g, l), vedge(g, l + 1))
+                        : 0.f;
+                }
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < 8; ++q) grp[q] += part[q];
+        if (++ngrp == 16) {
+#pragma unroll
+            for (int q = 0; q < 8; ++q) { acc[q] += grp[q]; grp[q] = 0.f; }
+            ngrp = 0;
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int j = u0 + 4 * warp + q;
+#pragma unroll
+        for (int hh = 0; hh < 2; ++hh) {
+            const int l = v0 + 32 * hh + lane;
+            if (j < g.nu && l < g.nv) {
+                const float uc = ucen(g, j), vc = vcen(g, l);
+                const float lth = sqrtf(1.f + vc * vc / (uc * uc + g.DSD * g.DSD));
+                sino[((size_t)ia * g.nu + j) * g.nv + l] = (acc[2 * q + hh] + grp[2 * q + hh]) * lth;
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Back projection
+// ---------------------------------------------------------------------------
+
+// out[a - a0] = sino[a] * l_theta, views a0 .. a0 + cnt - 1
+__global__ void sf3d_weight(vg_dd3d_geom g, const float *__restrict__ sino, int a0, int cnt,
+                            float *__restrict__ out) {
+    const size_t n = (size_t)cnt * g.nu * g.nv;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x) {
+        const int l = (int)(i % g.nv);
+        const int j = (int)((i / g.nv) % g.nu);
+        const float uc = ucen(g, j), vc = vcen(g, l);
+        const float lth = sqrtf(1.f + vc * vc / (uc * uc + g.DSD * g.DSD));
+        out[i] = sino[(size_t)a0 * g.nu * g.nv + i] * lth;
+    }
+}
+
+constexpr int BT = 8, BZ = 32, BKU = 4;
+
+struct SfBpTab {
+    float4 w[2][BT * BT];   // F1 l_phi0 of u cells j0 .. j0 + 3
+    int j0[2][BT * BT];
+    float mz[2][BT * BT];
+    int wide[2];
+};
+
+// one voxel, one view, straight from the weighted sinogram (any geometry)
+__device__ __noinline__ float sf_voxel_view(const vg_dd3d_geom &g, const float *__restrict__ q,
+                                            const SfCol &C, int iz) {
+    const float inv_du = 1.0f / g.du, inv_dv = 1.0f / g.dv;
+    const float U0 = uedge(g, 0), V0 = vedge(g, 0);
+    const int ja = max((int)floorf((C.t0 - U0) * inv_du), 0);
+    const int jb = min((int)floorf((C.t3 - U0) * inv_du), g.nu - 1);
+    const float va = C.mz * ((float)iz - 0.5f * g.nz), vb = va + C.mz;
+    const int la = max((int)floorf((va - V0) * inv_dv), 0);
+    const int lb = min((int)floorf((vb - V0) * inv_dv), g.nv - 1);
+    float part = 0.f;
+    for (int j = ja; j <= jb; ++j) {
+        const float w = uweight(C, uedge(g, j), uedge(g, j + 1), inv_du);
+        if (w == 0.f) continue;
+        float r = 0.f;
+        for (int l = la; l <= lb; ++l) {
+            const float ov = fminf(vb, vedge(g, l + 1)) - fmaxf(va, vedge(g, l));
+            if (ov > 0.f) r = fmaf(__ldg(q + (size_t)j * g.nv + l), ov, r);
+        }
+        part = fmaf(w, r, part);
+    }
+    return part * inv_dv;
+}
+
+__global__ void __launch_bounds__(256, 4)
+sf3d_bp_kernel(vg_dd3d_geom g, const float *__restrict__ qw, const double *__restrict__ trig, int a0,
+               int cnt, int accumulate, float *__restrict__ vol) {
+    __shared__ SfBpTab T;
+    const int z0 = blockIdx.x * BZ, y0 = blockIdx.y * BT, x0 = blockIdx.z * BT;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int iz = z0 + lane, iy = y0 + warp;
+    const float inv_du = 1.0f / g.du, inv_dv = 1.0f / g.dv;
+    const float U0 = uedge(g, 0), V0 = vedge(g, 0);
+    const float hz = 0.5f * g.nz;
+    Kahan acc[BT];
+    float grp[BT];
+#pragma unroll
+    for (int i = 0; i < BT; ++i) grp[i] = 0.f;
+    int ngrp = 0;
+    // T.wide[b] == a marks view a for the per-voxel path; writers only ever
+    // store that marker, so no reset races with them
+    if (tid < 2) T.wide[tid] = -1;
+    __syncthreads();
+    for (int a = 0; a < cnt; ++a) {
+        const int b = a & 1;
+        const float2 cs = view_cs(trig, a0 + a);
+        if (tid < BT * BT) {
+            const int ix = x0 + (tid & 7), jy = y0 + (tid >> 3);
+            float4 w = make_float4(0.f, 0.f, 0.f, 0.f);
+            int j0 = 0;
+            float mz = 1.f;
+            if (ix < g.nx && jy < g.ny) {
+                const SfCol C = sf_col(g, cs.x, cs.y, vox(g.d_pix, ix, g.nx), vox(g.d_pix, jy, g.ny));
+                const int ja = (int)floorf((C.t0 - U0) * inv_du), jb = (int)floorf((C.t3 - U0) * inv_du);
+                if (jb - ja >= BKU && jb >= 0 && ja < g.nu) T.wide[b] = a;
+                j0 = ja;
+                float ww[BKU];
+#pragma unroll
+                for (int t = 0; t < BKU; ++t) {
+                    const int j = ja + t;
+                    ww[t] = (j >= 0 && j < g.nu && j <= jb)
+                        ? uweight(C, uedge(g, j), uedge(g, j + 1), inv_du) : 0.f;
+                }
+                w = make_float4(ww[0], ww[1], ww[2], ww[3]);
+                mz = C.mz;
+            }
+            T.w[b][tid] = w;
+            T.j0[b][tid] = j0;
+            T.mz[b][tid] = mz;
+        }
+        __syncthreads();
+        const float *q = qw + (size_t)a * g.nu * g.nv;
+        if (iy < g.ny && iz < g.nz) {
+            if (T.wide[b] != a) {
+#pragma unroll
+                for (int i = 0; i < BT; ++i) {
+                    const int col = i + BT * warp;
+                    const float mz = T.mz[b][col];
+                    const float4 w = T.w[b][col];
+                    const int j0 = T.j0[b][col];
+                    const float va = mz * ((float)iz - hz), vb = va + mz;
+                    const int la = max((int)floorf((va - V0) * inv_dv), 0);
+                    const int lb = min((int)floorf((vb - V0) * inv_dv), g.nv - 1);
+                    const float wt[BKU] = {w.x, w.y, w.z, w.w};
+                    float part = 0.f;
+                    for (int l = la; l <= lb; ++l) {
+                        const float ov = fminf(vb, vedge(g, l + 1)) - fmaxf(va, vedge(g, l));
+                        if (ov <= 0.f) continue;
+                        float r = 0.f;
+#pragma unroll
+                        for (int t = 0; t < BKU; ++t)
+                            if (wt[t] != 0.f) r = fmaf(wt[t], __ldg(q + (size_t)(j0 + t) * g.nv + l), r);
+                        part = fmaf(r, ov, part);
+                    }
+                    grp[i] = fmaf(part, inv_dv, grp[i]);
+                }
+            } else {
+#pragma unroll 1
+                for (int i = 0; i < BT; ++i) {
+                    const int ix = x0 + i;
+                    if (ix >= g.nx) continue;
+                    const SfCol C = sf_col(g, cs.x, cs.y, vox(g.d_pix, ix, g.nx), vox(g.d_pix, iy, g.ny));
+                    grp[i] += sf_voxel_view(g, q, C, iz);
+                }
+            }
+        }
+        if (++ngrp == 16) {
+#pragma unroll
+            for (int i = 0; i < BT; ++i) { acc[i].add(grp[i]); grp[i] = 0.f; }
+            ngrp = 0;
+        }
+    }
+    if (iy >= g.ny || iz >= g.nz) return;
+#pragma unroll
+    for (int i = 0; i < BT; ++i) {
+        const int ix = x0 + i;
+        if (ix >= g.nx) continue;
+        acc[i].add(grp[i]);
+        float *o = vol + ((size_t)ix * g.ny + iy) * g.nz + iz;
+        *o = accumulate ? *o + acc[i].s : acc[i].s;
+    }
+}
+
+int check(const vg_dd3d_geom *g) {
+    VG_REQUIRE(g, "sf3d: null geometry");
+    VG_REQUIRE(g->nx > 0 && g->ny > 0 && g->nz > 0 && g->na > 0 && g->nu > 0 && g->nv > 0,
+               "sf3d: sizes must be positive");
+    VG_REQUIRE(g->na < 65536 && ceil_div(g->nx, BT) < 65536 && ceil_div(g->ny, BT) < 65536 &&
+                   ceil_div(g->nu, SU) < 65536, "sf3d: sizes too large");
+    VG_REQUIRE((double)g->nx * g->ny * g->nz < 2147483648.0, "sf3d: volume above 2^31 voxels");
+    VG_REQUIRE(g->du > 0.f && g->dv > 0.f && g->d_pix > 0.f && g->DSO > 0.f && g->DSD > 0.f,
+               "sf3d: pitches and distances must be positive");
+    // every voxel in front of the source (its footprint's projections are
+    // then finite): the volume's half diagonal in the plane below DSO
+    const float hx = 0.5f * g->nx * g->d_pix, hy = 0.5f * g->ny * g->d_pix;
+    VG_REQUIRE(hx * hx + hy * hy < g->DSO * g->DSO,
+               "sf3d: the volume must lie inside the source circle (half diagonal below DSO)");
+    return VG_OK;
+}
+
+constexpr size_t SF_CHUNK_BYTES = (size_t)256 << 20;
+
+size_t chunk_views(const vg_dd3d_geom *g) {
+    const size_t per = (size_t)g->nu * g->nv * sizeof(float);
+    size_t n = SF_CHUNK_BYTES / per;
+    if (n < 1) n = 1;
+    if (n > (size_t)g->na) n = g->na;
+    return n;
+}
+
+}  // namespace
+
+extern "C" size_t vg_sf3d_workspace_bytes(const vg_dd3d_geom *g) {
+    if (check(g)) return 0;
+    return chunk_views(g) * (size_t)g->nu * g->nv * sizeof(float);
+}
+
+extern "C" int vg_sf3d_fp(const vg_dd3d_geom *g, const float *vol, const double *trig, float *sino,
+                          void *stream) {
+    int st = check(g);
+    if (st) return st;
+    VG_REQUIRE(vol && trig && sino, "sf3d_fp: null pointer");
+    dim3 grid(ceil_div(g->nv, SV), ceil_div(g->nu, SU), g->na);
+    sf3d_fp_kernel<<<grid, 256, 0, as_stream(stream)>>>(*g, vol, trig, sino);
+    return launch_status("sf3d_fp");
+}
+
+extern "C" int vg_sf3d_bp(const vg_dd3d_geom *g, const float *sino, const double *trig, float *vol,
+                          void *workspace, size_t workspace_bytes, void *stream) {
+    int st = check(g);
+    if (st) return st;
+    VG_REQUIRE(sino && trig && vol, "sf3d_bp: null pointer");
+    const size_t nch = chunk_views(g);
+    const size_t need = nch * (size_t)g->nu * g->nv * sizeof(float);
+    VG_REQUIRE(workspace && workspace_bytes >= need,
+               "sf3d_bp: workspace of %zu bytes needed (vg_sf3d_workspace_bytes)", need);
+    cudaStream_t s = as_stream(stream);
+    float *qw = static_cast<float *>(workspace);
+    dim3 grid(ceil_div(g->nz, BZ), ceil_div(g->ny, BT), ceil_div(g->nx, BT));
+    for (int a0 = 0; a0 < g->na; a0 += (int)nch) {
+        const int cnt = (int)((size_t)(g->na - a0) < nch ? (size_t)(g->na - a0) : nch);
+        sf3d_weight<<<1216, 256, 0, s>>>(*g, sino, a0, cnt, qw);
+        st = launch_status("sf3d_weight");
+        if (st) return st;
+        sf3d_bp_kernel<<<grid, 256, 0, s>>>(*g, qw, trig, a0, cnt, a0 > 0, vol);
+        st = launch_status("sf3d_bp");
+        if (st) return st;
+    }
+    return VG_OK;
+}
