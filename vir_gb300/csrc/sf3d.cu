@@ -28,7 +28,7 @@
 //    columns' footprints, the covering columns and F1 weights of each u
 //    cell, and each column's v profile over the tile's v cells
 //    g(c, l) = sum_z f(c, z) F2(l; c, z); each cell then adds
-//    F1 * l_phi0 * g over its 1-6 covering columns.  Lines where a u cell
+//    F1 * l_phi0 * g over its 1-8 covering columns.  Lines where a u cell
 //    meets more columns, or the tile more than 64, take a per-cell path.
 //  BP (sf3d_bp_kernel): the sinogram is first multiplied by l_theta
 //    (sf3d_weight, into the workspace, a chunk of views at a time); block =
@@ -63,7 +63,7 @@ __device__ __forceinline__ float vox(float d, int i, int n) { return d * ((float
 // Footprint of column (x, y): sorted corner projections, l_phi0 and the
 // slice height on the detector M d.
 struct SfCol {
-    float t0, t1, t2, t3, lphi, mz;
+    float t0, t1, t2, t3, lphi, mz, inv_mz;
 };
 
 __device__ __forceinline__ void cswap(float &a, float &b) {
@@ -91,6 +91,7 @@ __device__ __forceinline__ SfCol sf_col(const vg_dd3d_geom &g, float c, float s,
     const float rx = x - g.DSO * c, ry = y - g.DSO * s;
     C.lphi = g.d_pix * sqrtf(rx * rx + ry * ry) / fmaxf(fabsf(rx), fabsf(ry));
     C.mz = g.DSD * g.d_pix / (g.DSO - fmaf(c, x, s * y));
+    C.inv_mz = (g.DSO - fmaf(c, x, s * y)) / (g.DSD * g.d_pix);
     return C;
 }
 
@@ -120,9 +121,9 @@ __device__ __forceinline__ float uweight(const SfCol &C, float ua, float ub, flo
 // sum_z f(z) |[M d (z - nz/2), M d (z + 1 - nz/2)] ∩ [va, vb]| / dv for one
 // column (f at col, slices contiguous)
 __device__ __forceinline__ float vprofile(const vg_dd3d_geom &g, const float *__restrict__ col,
-                                          float mz, float va, float vb, float inv_dv) {
+                                          float mz, float inv_mz, float va, float vb, float inv_dv) {
     const float hz = 0.5f * g.nz;
-    const float sa = va / mz + hz, sb = vb / mz + hz;
+    const float sa = fmaf(va, inv_mz, hz), sb = fmaf(vb, inv_mz, hz);
     const int z0 = max((int)floorf(sa), 0), z1 = min((int)floorf(sb), g.nz - 1);
     float acc = 0.f;
     for (int z = z0; z <= z1; ++z) {
@@ -147,15 +148,16 @@ __device__ __forceinline__ float unproj_idx(const vg_dd3d_geom &g, float c, floa
 // ---------------------------------------------------------------------------
 // Forward projection
 // ---------------------------------------------------------------------------
-constexpr int SU = 32, SV = 64, SCMAX = 64, SKMAX = 6;
+constexpr int SU = 32, SV = 64, SCMAX = 64, SKMAX = 8;
 
+// per-line tables, double-buffered by line parity
 struct SfFpTab {
-    SfCol col[SCMAX];
-    int off[SCMAX];     // voxel index of (column, z = 0)
-    int cf[SU], cn[SU]; // covering columns (table index, count) per u cell
-    float w[SU][SKMAX]; // F1 l_phi0 weights of those columns
-    float gv[SCMAX][SV];
-    int wide;
+    SfCol col[2][SCMAX];
+    int off[2][SCMAX];      // voxel index of (column, z = 0)
+    int cf[2][SU], cn[2][SU];  // covering columns (table index, count) per u cell
+    float w[2][SU][SKMAX];  // F1 l_phi0 weights of those columns
+    float gv[2][SCMAX][SV];
+    int wide[2];
 };
 
 // one cell's share of one line, straight from global memory (any geometry)
@@ -173,12 +175,13 @@ __device__ __noinline__ float sf_cell_line(const vg_dd3d_geom &g, const float *_
         const float w = uweight(C, Ua, Ub, inv_du);
         if (w == 0.f) continue;
         const int ix = xdrv ? k : io, iy = xdrv ? io : k;
-        part = fmaf(w, vprofile(g, vol + ((size_t)ix * g.ny + iy) * g.nz, C.mz, Va, Vb, inv_dv), part);
+        part = fmaf(w, vprofile(g, vol + ((size_t)ix * g.ny + iy) * g.nz, C.mz, C.inv_mz, Va, Vb, inv_dv),
+                    part);
     }
     return part;
 }
 
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 3)
 sf3d_fp_kernel(vg_dd3d_geom g, const float *__restrict__ vol, const double *__restrict__ trig,
                float *__restrict__ sino) {
     __shared__ SfFpTab T;
@@ -193,17 +196,20 @@ sf3d_fp_kernel(vg_dd3d_geom g, const float *__restrict__ vol, const double *__re
     const int nuT = min(SU, g.nu - u0), nvT = min(SV, g.nv - v0);
     const float TUa = uedge(g, u0), TUb = uedge(g, u0 + nuT);
     // the inverse edge map has a pole at u = -DSD pd / od; a tile holding it
-    // (or within a cell of it) cannot bound its columns through the map
+    // (or within two cells of it) cannot bound its columns through the map
     const float pd = xdrv ? -s : c, od = xdrv ? c : s;
     bool tile_pole = false;
     if (od != 0.f) {
         const float up = -g.DSD * pd / od;
         tile_pole = up >= TUa - 2.f * g.du && up <= TUb + 2.f * g.du;
     }
+    // this thread's (u cell, slot) in the weight table
+    const int wu = tid >> 3, wm = tid & 7;
     float acc[8], grp[8];
 #pragma unroll
     for (int q = 0; q < 8; ++q) acc[q] = grp[q] = 0.f;
-    int ngrp = 0;
+    int ngrp = 0, nl = 0;
+    if (tid < 2) T.wide[tid] = 0;
     for (int io = 0; io < no; ++io) {
         const float cen = vox(g.d_pix, io, no);
         // columns of this line whose footprint can reach the tile: the map
@@ -223,72 +229,83 @@ sf3d_fp_kernel(vg_dd3d_geom g, const float *__restrict__ vol, const double *__re
         if (kA > kB) continue;  // block-uniform
         const int nk = kB - kA + 1;
         const bool big = nk > SCMAX;
-        __syncthreads();  // the previous line's tables are no longer read
-        if (!big) {
-            if (tid < nk) {
-                const int k = kA + tid;
-                const float b = vox(g.d_pix, k, nd);
-                T.col[tid] = sf_col(g, c, s, xdrv ? b : cen, xdrv ? cen : b);
-                const int ix = xdrv ? k : io, iy = xdrv ? io : k;
-                T.off[tid] = (ix * g.ny + iy) * g.nz;
-            }
-            if (tid == 0) T.wide = 0;
+        const int b = nl++ & 1;
+        // phase 1: the columns' footprints (buffer b was last read two lines
+        // ago, before the previous line's second barrier)
+        if (!big && tid < nk) {
+            const int k = kA + tid;
+            const float bb = vox(g.d_pix, k, nd);
+            T.col[b][tid] = sf_col(g, c, s, xdrv ? bb : cen, xdrv ? cen : bb);
+            const int ix = xdrv ? k : io, iy = xdrv ? io : k;
+            T.off[b][tid] = (ix * g.ny + iy) * g.nz;
         }
+        if (tid == 0) T.wide[b] = 0;
         __syncthreads();
         if (!big) {
-            // covering columns and weights of each u cell (the columns'
-            // footprints move monotonically along the line, so the covering
-            // ones are consecutive)
-            if (tid < nuT) {
-                const float ua = uedge(g, u0 + tid), ub = uedge(g, u0 + tid + 1);
-                int first = -1, n = 0;
-                for (int t = 0; t < nk; ++t) {
-                    const SfCol &C = T.col[t];
-                    if (C.t3 > ua && C.t0 < ub) {
-                        if (first < 0) first = t;
-                        if (n < SKMAX) T.w[tid][n] = uweight(C, ua, ub, inv_du);
-                        ++n;
-                    } else if (first >= 0) {
-                        break;
-                    }
+            // phase 2a: covering columns of each u cell (the footprints move
+            // monotonically along the line, so they are consecutive; binary
+            // searches on the footprints' ends) and their weights, one
+            // (u cell, slot) per thread
+            if (wu < nuT) {
+                const float ua = uedge(g, u0 + wu), ub = uedge(g, u0 + wu + 1);
+                const bool inc = T.col[b][nk - 1].t0 >= T.col[b][0].t0;
+                // first covering: inc -> first t with t3 > ua; dec -> first t with t0 < ub
+                int lo = 0, hi = nk;
+                while (lo < hi) {
+                    const int mid = (lo + hi) >> 1;
+                    const bool past = inc ? (T.col[b][mid].t3 > ua) : (T.col[b][mid].t0 < ub);
+                    if (past) hi = mid; else lo = mid + 1;
                 }
-                if (n > SKMAX) T.wide = 1;
-                T.cf[tid] = max(first, 0);
-                T.cn[tid] = min(n, SKMAX);
+                const int first = lo;
+                // end (exclusive): inc -> first t with t0 >= ub; dec -> first t with t3 <= ua
+                lo = first; hi = nk;
+                while (lo < hi) {
+                    const int mid = (lo + hi) >> 1;
+                    const bool out = inc ? (T.col[b][mid].t0 >= ub) : (T.col[b][mid].t3 <= ua);
+                    if (out) hi = mid; else lo = mid + 1;
+                }
+                const int n = lo - first;
+                if (wm == 0) {
+                    T.cf[b][wu] = first;
+                    T.cn[b][wu] = min(n, SKMAX);
+                    if (n > SKMAX) T.wide[b] = 1;
+                }
+                if (wm < n && wm < SKMAX) T.w[b][wu][wm] = uweight(T.col[b][first + wm], ua, ub, inv_du);
             }
-            // v profiles of the table's columns over the tile's v cells
+            // phase 2b: v profiles of the table's columns over the tile's v cells
             for (int p = tid; p < nk * SV; p += 256) {
                 const int t = p / SV, l = p % SV;
                 float gval = 0.f;
                 if (l < nvT)
-                    gval = vprofile(g, vol + T.off[t], T.col[t].mz, vedge(g, v0 + l),
-                                    vedge(g, v0 + l + 1), inv_dv);
-                T.gv[t][l] = gval;
+                    gval = vprofile(g, vol + T.off[b][t], T.col[b][t].mz, T.col[b][t].inv_mz,
+                                    vedge(g, v0 + l), vedge(g, v0 + l + 1), inv_dv);
+                T.gv[b][t][l] = gval;
             }
         }
         __syncthreads();
+        // phase 3: each cell adds its covering columns' weighted profiles
         float part[8];
-        if (!big && !T.wide) {
+        if (!big && !T.wide[b]) {
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
                 const int j = 4 * warp + q;
                 float pa = 0.f, pb = 0.f;
                 if (j < nuT) {
-                    const int f0 = T.cf[j], n = T.cn[j];
+                    const int f0 = T.cf[b][j], n = T.cn[b][j];
                     for (int m = 0; m < n; ++m) {
-                        const float w = T.w[j][m];
-                        pa = fmaf(w, T.gv[f0 + m][lane], pa);
-                        pb = fmaf(w, T.gv[f0 + m][32 + lane], pb);
+                        const float w = T.w[b][j][m];
+                        pa = fmaf(w, T.gv[b][f0 + m][lane], pa);
+                        pb = fmaf(w, T.gv[b][f0 + m][32 + lane], pb);
                     }
                 }
                 part[2 * q] = pa;
                 part[2 * q + 1] = pb;
             }
         } else {
-#pragma unroll 1
+#pragma unroll
             for (int q = 0; q < 4; ++q) {
                 const int j = u0 + 4 * warp + q;
-#pragma unroll 1
+#pragma unroll
                 for (int hh = 0; hh < 2; ++hh) {
                     const int l = v0 + 32 * hh + lane;
                     part[2 * q + hh] = (j < g.nu && l < g.nv)
@@ -350,7 +367,8 @@ struct SfBpTab {
 
 // one voxel, one view, straight from the weighted sinogram (any geometry)
 __device__ __noinline__ float sf_voxel_view(const vg_dd3d_geom &g, const float *__restrict__ q,
-                                            const SfCol &C, int iz) {
+                                            float c, float s, float x, float y, int iz) {
+    const SfCol C = sf_col(g, c, s, x, y);
     const float inv_du = 1.0f / g.du, inv_dv = 1.0f / g.dv;
     const float U0 = uedge(g, 0), V0 = vedge(g, 0);
     const int ja = max((int)floorf((C.t0 - U0) * inv_du), 0);
@@ -370,6 +388,16 @@ __device__ __noinline__ float sf_voxel_view(const vg_dd3d_geom &g, const float *
         part = fmaf(w, r, part);
     }
     return part * inv_dv;
+}
+
+// the 8 voxels x0 .. x0 + 7 of row iy, slice iz (0 beyond the volume)
+__device__ __noinline__ void sf_voxels_view(const vg_dd3d_geom &g, const float *__restrict__ q, float c,
+                                            float s, int x0, int iy, int iz, float *out) {
+    for (int i = 0; i < BT; ++i) {
+        const int ix = x0 + i;
+        out[i] = ix < g.nx ? sf_voxel_view(g, q, c, s, vox(g.d_pix, ix, g.nx), vox(g.d_pix, iy, g.ny), iz)
+                           : 0.f;
+    }
 }
 
 __global__ void __launch_bounds__(256, 4)
@@ -445,13 +473,10 @@ sf3d_bp_kernel(vg_dd3d_geom g, const float *__restrict__ qw, const double *__res
                     grp[i] = fmaf(part, inv_dv, grp[i]);
                 }
             } else {
-#pragma unroll 1
-                for (int i = 0; i < BT; ++i) {
-                    const int ix = x0 + i;
-                    if (ix >= g.nx) continue;
-                    const SfCol C = sf_col(g, cs.x, cs.y, vox(g.d_pix, ix, g.nx), vox(g.d_pix, iy, g.ny));
-                    grp[i] += sf_voxel_view(g, q, C, iz);
-                }
+                float wv[BT];
+                sf_voxels_view(g, q, cs.x, cs.y, x0, iy, iz, wv);
+#pragma unroll
+                for (int i = 0; i < BT; ++i) grp[i] += wv[i];
             }
         }
         if (++ngrp == 16) {
