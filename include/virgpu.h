@@ -300,6 +300,17 @@ int vg_sf3d_fp(const vg_dd3d_geom *g, const float *vol, const double *trig, floa
 int vg_sf3d_bp(const vg_dd3d_geom *g, const float *sino, const double *trig, float *vol,
                void *workspace, size_t workspace_bytes, void *stream);
 
+/* One SIRT update on the cone pair, both halves fused (sys_mat/sirt_dd.py:51-72):
+ *   r  = (y - FP x) * inv_w_sino   (FP x kept where inv_w_sino == 0)
+ *   x += gamma * (BP r) * inv_w_img (BP r kept where inv_w_img == 0)
+ * with FP / BP of vg_dd3d_fp / vg_dd3d_bp (vir's scalings); inv_w_* hold
+ * 1/W (0 where W == 0); r is a caller scratch sinogram; x is updated in
+ * place.  Three launches: the per-view tables, the forward projection with
+ * the residual epilogue, the back projection with the update epilogue. */
+int vg_dd3d_sirt_iter(const vg_dd3d_geom *g, const float *y, const float *inv_w_sino,
+                      const float *inv_w_img, float gamma, const double *trig, float *x,
+                      float *r, void *workspace, size_t workspace_bytes, void *stream);
+
 /* ---- translational "square" geometry ------------------------------------ */
 
 /* dd_fp_square / dd_bp_square (sys_mat/dd.py:903, 1104): an n x n x nz

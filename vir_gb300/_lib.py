@@ -101,6 +101,8 @@ _PROTOS = {
     "vg_fbp2d_bp": [ctypes.POINTER(DD2DGeom), c_void_p, c_void_p, c_void_p, c_void_p],
     "vg_dd3d_fp": [ctypes.POINTER(DD3DGeom), c_void_p, c_void_p, c_void_p, c_void_p, c_size_t,
                    c_void_p],
+    "vg_dd3d_sirt_iter": [ctypes.POINTER(DD3DGeom), c_void_p, c_void_p, c_void_p, c_float,
+                          c_void_p, c_void_p, c_void_p, c_void_p, c_size_t, c_void_p],
     "vg_sf3d_fp": [ctypes.POINTER(DD3DGeom), c_void_p, c_void_p, c_void_p, c_void_p],
     "vg_sf3d_bp": [ctypes.POINTER(DD3DGeom), c_void_p, c_void_p, c_void_p, c_void_p, c_size_t,
                    c_void_p],

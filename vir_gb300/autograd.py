@@ -122,7 +122,7 @@ def reconstruct_adam(y, geom, steps=200, lr=1e-3, lam=1e-3, x0=None, callback=No
         L.backward()
         opt.step()
         if callback is not None:
-            callback(it, x.detach(), float(L))
+            callback(it, x.detach(), float(L.detach()))
     return x.detach()
 
 

@@ -193,7 +193,8 @@ __device__ __forceinline__ void fp_cells(const float4 *uw, const int *uk, const 
 #endif
 __global__ void __launch_bounds__(256, VG_CONE_FP_MINB)
 dd3d_fp_kernel(vg_dd3d_geom g, const float *__restrict__ vol, const float4 *__restrict__ vf,
-               const float2 *__restrict__ tab, float *__restrict__ sino) {
+               const float2 *__restrict__ tab, float *__restrict__ sino, int mode,
+               const float *__restrict__ y, const float *__restrict__ inv_w) {
     __shared__ FpTables S;
     const int ia = blockIdx.z;
     const int u0 = blockIdx.y * FT_U, v0 = blockIdx.x * FT_V;
@@ -331,8 +332,15 @@ dd3d_fp_kernel(vg_dd3d_geom g, const float *__restrict__ vol, const float4 *__re
         for (int h = 0; h < 2; ++h) {
             const int iv = v0 + 32 * h + lane;
             acc[2 * j + h] += grp[2 * j + h];
-            if (iu < g.nu && iv < g.nv)
-                sino[((size_t)ia * g.nu + iu) * g.nv + iv] = acc[2 * j + h] * f;
+            if (iu < g.nu && iv < g.nv) {
+                const size_t o = ((size_t)ia * g.nu + iu) * g.nv + iv;
+                float fp = acc[2 * j + h] * f;
+                if (mode) {  // SIRT residual: (y - FP) / W_sino, FP kept where W_sino == 0
+                    const float wi = inv_w[o];
+                    fp = (wi != 0.f) ? (y[o] - fp) * wi : fp;
+                }
+                sino[o] = fp;
+            }
         }
     }
 }
@@ -386,7 +394,8 @@ __device__ float bp_voxel_view(const vg_dd3d_geom &g, const View3 &v, const floa
 #endif
 __global__ void __launch_bounds__(256, VG_CONE_BP_MINB)
 dd3d_bp_kernel(vg_dd3d_geom g, const float *__restrict__ sino, const float4 *__restrict__ vf,
-               const float2 *__restrict__ tab, float *__restrict__ vol) {
+               const float2 *__restrict__ tab, float *__restrict__ vol, int mode,
+               const float *__restrict__ inv_w, float gamma) {
     __shared__ BpTables T;
     const int z0 = blockIdx.x * BZ, y0 = blockIdx.y * BT, x0 = blockIdx.z * BT;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -511,8 +520,16 @@ dd3d_bp_kernel(vg_dd3d_geom g, const float *__restrict__ sino, const float4 *__r
     for (int i = 0; i < BT; ++i) {
         acc[i].add(grp[i]);
         const int ix = x0 + i;
-        if (ix < g.nx && iy < g.ny && iz < g.nz)
-            vol[((size_t)ix * g.ny + iy) * g.nz + iz] = acc[i].s * f;
+        if (ix < g.nx && iy < g.ny && iz < g.nz) {
+            const size_t o = ((size_t)ix * g.ny + iy) * g.nz + iz;
+            const float bp = acc[i].s * f;
+            if (mode) {  // SIRT update: x += gamma BP / W_img, BP where W_img == 0
+                const float wi = inv_w[o];
+                vol[o] += gamma * ((wi != 0.f) ? bp * wi : bp);
+            } else {
+                vol[o] = bp;
+            }
+        }
     }
 }
 
@@ -556,7 +573,7 @@ extern "C" int vg_dd3d_fp(const vg_dd3d_geom *g, const float *vol, const double 
     dd3d_fp_kernel<<<grid, 256, 0, st>>>(
         *g, vol,
         reinterpret_cast<const float4 *>(static_cast<const char *>(workspace) + tab_bytes(g)),
-        reinterpret_cast<const float2 *>(workspace), sino);
+        reinterpret_cast<const float2 *>(workspace), sino, 0, nullptr, nullptr);
     return launch_status("dd3d_fp");
 }
 
@@ -572,6 +589,26 @@ extern "C" int vg_dd3d_bp(const vg_dd3d_geom *g, const float *sino, const double
     dd3d_bp_kernel<<<grid, 256, 0, st>>>(
         *g, sino,
         reinterpret_cast<const float4 *>(static_cast<const char *>(workspace) + tab_bytes(g)),
-        reinterpret_cast<const float2 *>(workspace), vol);
+        reinterpret_cast<const float2 *>(workspace), vol, 0, nullptr, 0.f);
+    return launch_status("dd3d_bp");
+}
+
+extern "C" int vg_dd3d_sirt_iter(const vg_dd3d_geom *g, const float *y, const float *inv_w_sino,
+                                 const float *inv_w_img, float gamma, const double *trig, float *x,
+                                 float *r, void *workspace, size_t workspace_bytes, void *stream) {
+    int s = check(g);
+    if (s) return s;
+    VG_REQUIRE(y && inv_w_sino && inv_w_img && trig && x && r, "dd3d_sirt_iter: null pointer");
+    cudaStream_t st = as_stream(stream);
+    s = launch_prep(g, trig, workspace, workspace_bytes, st);
+    if (s) return s;
+    const float4 *vf = reinterpret_cast<const float4 *>(static_cast<const char *>(workspace) + tab_bytes(g));
+    const float2 *tab = reinterpret_cast<const float2 *>(workspace);
+    dim3 gf(ceil_div(g->nv, FT_V), ceil_div(g->nu, FT_U), g->na);
+    dd3d_fp_kernel<<<gf, 256, 0, st>>>(*g, x, vf, tab, r, 1, y, inv_w_sino);
+    s = launch_status("dd3d_fp");
+    if (s) return s;
+    dim3 gb(ceil_div(g->nz, BZ), ceil_div(g->ny, BT), ceil_div(g->nx, BT));
+    dd3d_bp_kernel<<<gb, 256, 0, st>>>(*g, r, vf, tab, x, 1, inv_w_img, gamma);
     return launch_status("dd3d_bp");
 }

@@ -131,6 +131,98 @@ class SIRT2D:
         self.xT.fill_(float(np.float32(x0)))
 
 
+class SIRT3D:
+    """Resident SIRT state for one circular cone-beam problem (the DD cone
+    pair of dd_fp_cone_3d / dd_bp_cone_3d) on one GPU: the measured sinogram,
+    1/W_sino, 1/W_img, the iterate and the residual scratch stay in device
+    memory; one update is vg_dd3d_sirt_iter (residual in the forward
+    projection's epilogue, update in the back projection's), and a run of
+    updates is captured once as a CUDA graph and replayed."""
+
+    def __init__(self, sino, ang_arr, img_shape, DSO, DSD, du=1.0, dv=1.0, su=0.0, sv=0.0,
+                 d_pix=1.0, gamma=1.0, x0=1e-5, device=None):
+        from ._lib import dd3d_workspace
+        _core.require_cuda()
+        self.dev = device or _core.device_of(sino)
+        self.y = _core.to_device(sino, self.dev)
+        if self.y.ndim != 3:
+            raise ValueError("sino must be (na, nu, nv)")
+        self.trig = _core.trig_cache.get(ang_arr, np.float32, self.dev)
+        na = self.trig.numel() // 2
+        if self.y.shape[0] != na:
+            raise ValueError("sino rows must equal len(ang_arr)")
+        f = _core.f32
+        self.g = DD3DGeom(*(int(v) for v in img_shape), na, int(self.y.shape[1]),
+                          int(self.y.shape[2]), f(du), f(dv), f(su), f(sv), f(d_pix), f(DSO), f(DSD))
+        self.gamma = float(gamma)
+        self.ws = dd3d_workspace(self.g, self.dev)
+        shape = tuple(int(v) for v in img_shape)
+        W_sino = self._fp(torch.ones(shape, dtype=torch.float32, device=self.dev))
+        W_img = self._bp(torch.ones_like(self.y))
+        self.inv_ws = torch.where(W_sino != 0, 1.0 / W_sino, torch.zeros_like(W_sino))
+        self.inv_wi = torch.where(W_img != 0, 1.0 / W_img, torch.zeros_like(W_img))
+        del W_sino, W_img
+        self.x = torch.full(shape, float(np.float32(x0)), dtype=torch.float32, device=self.dev)
+        self.r = torch.empty_like(self.y)
+        self._graph = None
+        self._graph_n = 0
+
+    def _fp(self, x):
+        out = torch.empty((self.g.na, self.g.nu, self.g.nv), dtype=torch.float32, device=self.dev)
+        call("vg_dd3d_fp", ctypes.byref(self.g), _core.ptr(x), _core.ptr(self.trig), _core.ptr(out),
+             _core.ptr(self.ws), self.ws.numel() * 4, _core.stream(self.dev))
+        return out
+
+    def _bp(self, y):
+        out = torch.empty((self.g.nx, self.g.ny, self.g.nz), dtype=torch.float32, device=self.dev)
+        call("vg_dd3d_bp", ctypes.byref(self.g), _core.ptr(y), _core.ptr(self.trig), _core.ptr(out),
+             _core.ptr(self.ws), self.ws.numel() * 4, _core.stream(self.dev))
+        return out
+
+    def _iter(self):
+        call("vg_dd3d_sirt_iter", ctypes.byref(self.g), _core.ptr(self.y), _core.ptr(self.inv_ws),
+             _core.ptr(self.inv_wi), ctypes.c_float(self.gamma), _core.ptr(self.trig),
+             _core.ptr(self.x), _core.ptr(self.r), _core.ptr(self.ws), self.ws.numel() * 4,
+             _core.stream(self.dev))
+
+    def capture(self, n: int):
+        """Capture ``n`` updates as one CUDA graph (replayed by run())."""
+        s = torch.cuda.Stream(self.dev)
+        s.wait_stream(torch.cuda.current_stream(self.dev))
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.stream(s):
+            with torch.cuda.graph(g, stream=s):
+                for _ in range(n):
+                    self._iter()
+        torch.cuda.current_stream(self.dev).wait_stream(s)
+        self._graph, self._graph_n = g, n
+        return g
+
+    def run(self, n_updates: int, graph: bool = True):
+        """Apply ``n_updates`` SIRT updates to x (asynchronous)."""
+        if n_updates <= 0:
+            return self.x
+        if graph:
+            if self._graph is None or self._graph_n != n_updates:
+                self.capture(n_updates)
+            self._graph.replay()
+        else:
+            for _ in range(n_updates):
+                self._iter()
+        return self.x
+
+    def reset(self, x0=1e-5):
+        self.x.fill_(float(np.float32(x0)))
+
+
+def sirt_3d(sino, ang_arr, img_shape, DSO, DSD, du=1.0, dv=1.0, su=0.0, sv=0.0, d_pix=1.0,
+            gamma=1.0, iters=20, graph=True):
+    """vir's SIRT (``iters - 1`` updates, x0 = 1e-5) on the cone-beam DD pair."""
+    s = SIRT3D(sino, ang_arr, img_shape, DSO, DSD, du, dv, su, sv, d_pix, gamma)
+    x = s.run(int(iters) - 1, graph=graph)
+    return _core.to_host_like(x.clone(), sino)
+
+
 def sirt_2d(sino, ang_arr, img_shape, geom="par", DSO=0.0, DSD=0.0, du=1.0, su=0.0, d_pix=1.0,
             gamma=1.0, iters=100, W_sino=None, W_img=None, graph=True):
     """vir's SIRT (``iters - 1`` updates, x0 = 1e-5) on the parallel or fan
