@@ -225,7 +225,8 @@ EXTRA = {
     "c1": "2D parallel Siddon FP + gather BP: 256x256 random-ellipse phantom, 1 mm pixels, "
           "180 views over pi, 367 bins of 1 mm",
     "c3": "batched SIRT: 64 parallel/fan problems (seed 3), sides in {128,256,512,1024}, "
-          "90-1440 views, 1.5x detectors; 50 updates, one CUDA graph vs one launch per step",
+          "90-1440 views, 1.5x detectors; 50 updates: one persistent launch (work queue, "
+          "float32 or bfloat16 storage), one CUDA graph of per-problem chains, one launch per step",
     "c4": "3D cone DD and separable-footprint FP + BP, FDK: 512^3 volume of 20 random "
           "ellipsoids, 0.5 mm voxels, 720 views over 2pi, 1024x768 detector at 0.8 mm, DSO 600 mm, "
           "DSD 1100 mm",
@@ -293,16 +294,13 @@ def _roof(units, ms, peak):
 
 def storage_error(probs, dev, n_check=2, iters=50):
     """Final-iterate error against the FP64 oracle's SIRT, relative
-    (||x - x64|| / ||x64||), for FP32 storage (the batched kernels) and for
-    BF16 storage with FP32 arithmetic: y, the residual and the iterate are
-    rounded to bfloat16 wherever they are stored, which gives the values a
-    bf16 store / load pair would.  The smallest problems of the set are used
-    so the oracle finishes in seconds."""
-    import torch
+    (||x - x64|| / ||x64||), for each storage of the persistent batched
+    kernel: float32, bfloat16 measured sinogram, bfloat16 iterate, both (the
+    kernel reads and writes bfloat16, arithmetic float32).  The smallest
+    problems of the set are used so the oracle finishes in seconds."""
     from oracle import oracle as orc
-    from vir_gb300.reconstruction import SIRT2D
+    from vir_gb300.batched import PersistentSIRT2D
     order = sorted(range(len(probs)), key=lambda i: probs[i]["img_shape"][0] * probs[i]["sino"].shape[0])
-    bf = lambda t: t.to(torch.bfloat16).to(torch.float32)
     out = []
     for i in order[:n_check]:
         p = probs[i]
@@ -314,21 +312,15 @@ def storage_error(probs, dev, n_check=2, iters=50):
             fp = lambda x: orc.dd_fp_par_2d(x, p["ang_arr"], p["sino"].shape[1], **kw)
             bp = lambda y: orc.dd_bp_par_2d(y, p["ang_arr"], p["img_shape"], **kw)
         x64 = orc.sirt(p["sino"], fp, bp, p["img_shape"], iters=iters)
-        s = SIRT2D(device=dev, **p)
-        x32 = s.run(iters - 1, graph=False).cpu().numpy()
-        yb = bf(s.y)
-        x = bf(torch.full_like(s.x, float(np.float32(1e-5))))
-        for _ in range(iters - 1):
-            est = s.fp(x)
-            r = bf(torch.where(s.inv_ws != 0, (yb - est) * s.inv_ws, est))
-            upd = s.bp(r)
-            x = bf(x + s.gamma * torch.where(s.inv_wi != 0, upd * s.inv_wi, upd))
-        xb = x.cpu().numpy()
         nrm = np.linalg.norm(x64)
-        out.append({"problem": i, "side": int(p["img_shape"][0]), "views": int(p["sino"].shape[0]),
-                    "geom": p["geom"], "updates": iters - 1,
-                    "fp32_rel": float(np.linalg.norm(x32 - x64) / nrm),
-                    "bf16_storage_rel": float(np.linalg.norm(xb - x64) / nrm)})
+        rec = {"problem": i, "side": int(p["img_shape"][0]), "views": int(p["sino"].shape[0]),
+               "geom": p["geom"], "updates": iters - 1}
+        for st in ("fp32", "bf16y", "bf16x", "bf16"):
+            b = PersistentSIRT2D([p], device=dev, storage=st)
+            b.run(iters - 1)
+            x = b.images()[0].cpu().numpy()
+            rec[st + "_rel"] = float(np.linalg.norm(x - x64) / nrm)
+        out.append(rec)
     return out
 
 
@@ -692,17 +684,42 @@ def run_workload(args):
     elif wl == "c3":
         from vir_gb300.batched import BatchedSIRT2D
         from vir_gb300.workloads import batched_problems
+        from vir_gb300.batched import PersistentSIRT2D
         probs = batched_problems(64, seed=3)
         b = BatchedSIRT2D(probs, n_streams=16)
         res = {}
         for mode in ("graph", "plain"):
             b.reset()
             res[mode] = _event_ms(lambda: b.run(50) if mode == "graph" else b.plain(50), 1, stream)
+        b.reset()
+        b.run(50)
+        xg = [x.clone() for x in b.images()]
+        del b
+        torch.cuda.empty_cache()
+        pers = {}
+        for st in ("fp32", "bf16y", "bf16x", "bf16"):
+            pb = PersistentSIRT2D(probs, device=dev, storage=st)
+            pb.run(1)
+            pb.reset()
+            pers[st] = _event_ms(lambda: pb.run(50, wait=False), 1, stream)
+            if st == "fp32":
+                pb.reset()
+                status = pb.run(50)
+                diff = max(float((a - c).abs().max() / c.abs().max()) for a, c in zip(pb.images(), xg))
+                grid = pb.grid_blocks
+            del pb
+            torch.cuda.empty_cache()
         units = sum(p["sino"].shape[0] * p["img_shape"][0] * p["img_shape"][1] for p in probs)
         line.update({"metric": "batched SIRT iter/s (50 updates x 64 problems)",
                      "graph_ms": res["graph"], "plain_ms": res["plain"],
-                     "speedup_vs_plain": res["plain"] / res["graph"],
+                     "persistent_ms": pers, "persistent_status": status,
+                     "persistent_grid_blocks": grid,
+                     "persistent_vs_graph_max_rel_diff": diff,
+                     "speedup_vs_plain": {"graph": res["plain"] / res["graph"],
+                                          **{"persistent_" + k: res["plain"] / v
+                                             for k, v in pers.items()}},
                      "fwd_back_gups_graph": 2 * 50 * units / (res["graph"] / 1e3) / 1e9,
+                     "fwd_back_gups_persistent": 2 * 50 * units / (pers["fp32"] / 1e3) / 1e9,
                      "storage_error": storage_error(probs, dev)})
         print(json.dumps(line), flush=True)
         return 0

@@ -237,6 +237,70 @@ int vg_dd2d_sirt_update(const vg_dd2d_geom *g, const float *inv_w_img, float gam
  * geometry vg_dd2d_sirt_iter rejects. */
 int vg_dd2d_sirt_launches(const vg_dd2d_geom *g);
 
+/* ---- batched SIRT: many 2D problems in one persistent launch ----------- */
+
+/* One problem of a batch: its geometry and device buffers.  x, xT (the
+ * iterate and its transpose, (nx, ny) / (ny, nx)) and y (the measured
+ * sinogram) are float32, or bfloat16 when the run's storage flag says so;
+ * arithmetic is float32 throughout.  inv_w_* hold 1/W (0 where W == 0), r is
+ * a residual scratch (na, nu) float32, workspace has
+ * vg_dd2d_workspace_bytes(&g) bytes, 256-byte aligned. */
+typedef struct {
+    vg_dd2d_geom g;
+    const void *y;
+    const float *inv_w_sino;
+    const float *inv_w_img;
+    const double *trig;
+    void *x;
+    void *xT;
+    float *r;
+    void *workspace;
+    float gamma;
+    int pad;
+} vg_sirt2d_problem;
+
+/* Device control block of a run (40 bytes, zeroed by vg_sirt2d_batch_run):
+ * status (VG_OK, VG_ERR_CANCELLED or VG_ERR_TIMEOUT) and the number of
+ * updates every problem completed (done) are valid once the run's stream has
+ * reached its end; the other fields are the run's own. */
+typedef struct {
+    unsigned long long next;
+    int status, done;
+    int stop_p, checked;
+    unsigned exited, pad;
+    unsigned long long t0;
+} vg_sirt2d_batch_ctrl;
+
+/* Host-only: the work items of a batch (problems on the host): forward
+ * projection items (problem, view * chunks + chunk), table items (problem,
+ * view) and back projection items (problem, pixel tile), int pairs, in
+ * problem order (any order is valid; ordering by decreasing cost balances
+ * the blocks).  With null item arrays only the counts are returned. */
+int vg_sirt2d_batch_items(const vg_sirt2d_problem *probs, int n, int *fp_items, int *n_fp,
+                          int *tab_items, int *n_tab, int *bp_items, int *n_bp);
+
+/* `iters` SIRT updates (sys_mat/sirt_dd.py:51-72, as vg_dd2d_sirt_iter) of
+ * all n problems in one persistent, cooperative launch.  Every block takes
+ * the next work item from one queue (all items of update 0, then of update
+ * 1, ...); an item waits only for the items of its own problem it reads
+ * (per-problem counters, 3 n ints of device memory in `counters`), so the
+ * updates of different problems overlap.  probs_dev and the item arrays are
+ * device memory; max_nd is the largest image side of the batch.  storage:
+ * bit 0 stores the iterates, bit 1 the measured sinograms as bfloat16.
+ * cancel: NULL, or an int in pinned host memory (or device memory) that the
+ * caller may set non-zero at any time; the run then stops at the start of
+ * the next update with status VG_ERR_CANCELLED, every problem having the
+ * same number of updates.  budget_ns: a time budget (0 = none), checked at
+ * the start of every update (VG_ERR_TIMEOUT the same way).  A dependency
+ * wait longer than about two seconds stops the run with VG_ERR_TIMEOUT (the
+ * iterates are then not all at the same update).  grid_blocks (may be NULL)
+ * receives the number of resident blocks launched.  Replaces one
+ * vg_dd2d_sirt_iter launch chain per problem; vir has no batching. */
+int vg_sirt2d_batch_run(const vg_sirt2d_problem *probs_dev, int n, int max_nd, const int *fp_items,
+                        int n_fp, const int *tab_items, int n_tab, const int *bp_items, int n_bp,
+                        int iters, int storage, const int *cancel, unsigned long long budget_ns,
+                        vg_sirt2d_batch_ctrl *ctrl, int *counters, void *stream, int *grid_blocks);
+
 /* Pixel-driven FBP backprojection of a ramp-filtered sinogram q (na, nu)
  * (filtered by vg_filter_rows, i.e. filtration.filter_sino's 2H):
  *   img(x, y) = pi / (2 na) * sum_views q(s(x, y)) / U(x, y)^2,

@@ -34,6 +34,13 @@ class DD2DGeom(ctypes.Structure):
                 ("DSO", c_float), ("DSD", c_float), ("fan", c_int), ("variant", c_int)]
 
 
+class Sirt2DProblem(ctypes.Structure):
+    """vg_sirt2d_problem (include/virgpu.h)."""
+    _fields_ = [("g", DD2DGeom), ("y", c_void_p), ("inv_w_sino", c_void_p),
+                ("inv_w_img", c_void_p), ("trig", c_void_p), ("x", c_void_p), ("xT", c_void_p),
+                ("r", c_void_p), ("workspace", c_void_p), ("gamma", c_float), ("pad", c_int)]
+
+
 class SiddonRays(ctypes.Structure):
     """vg_siddon_rays (include/virgpu.h)."""
     _fields_ = [("n_rays", c_int), ("nx", c_int), ("ny", c_int), ("nz", c_int),
@@ -103,6 +110,11 @@ _PROTOS = {
                    c_void_p],
     "vg_dd3d_sirt_iter": [ctypes.POINTER(DD3DGeom), c_void_p, c_void_p, c_void_p, c_float,
                           c_void_p, c_void_p, c_void_p, c_void_p, c_size_t, c_void_p],
+    "vg_sirt2d_batch_items": [c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                              c_void_p],
+    "vg_sirt2d_batch_run": [c_void_p, c_int, c_int, c_void_p, c_int, c_void_p, c_int, c_void_p,
+                            c_int, c_int, c_int, c_void_p, ctypes.c_ulonglong, c_void_p, c_void_p,
+                            c_void_p, c_void_p],
     "vg_sf3d_fp": [ctypes.POINTER(DD3DGeom), c_void_p, c_void_p, c_void_p, c_void_p],
     "vg_sf3d_bp": [ctypes.POINTER(DD3DGeom), c_void_p, c_void_p, c_void_p, c_void_p, c_size_t,
                    c_void_p],

@@ -35,6 +35,8 @@
 // coefficient is negative the edge order is reversed, as dd.py:516-518 does.
 #include "vg_common.cuh"
 
+#include <cuda_bf16.h>
+
 // Edge projections divide with __fdividef (reciprocal + multiply, 2 ulp)
 // unless built with -DVG_FAST_DIV=0 (IEEE division).
 #ifndef VG_SIRT_FUSED_TABLES
@@ -60,6 +62,39 @@
 namespace {
 
 using namespace vg;
+
+// Storage types of the image (TX) and the measured sinogram (TY): float, or
+// bfloat16 with all arithmetic in float32 (the batched SIRT's bf16 storage).
+// COH loads (ld.global.ca) are for data written earlier in the same launch
+// (the persistent batched kernel, after an acquire fence); the others use
+// the read-only path (ld.global.nc), valid for data no launch writes meanwhile.
+template <bool COH = false, typename T> __device__ __forceinline__ T ldro(const T *p) {
+    return COH ? __ldca(p) : __ldg(p);
+}
+template <bool COH = false> __device__ __forceinline__ float ldf(const float *p) { return ldro<COH>(p); }
+template <bool COH = false> __device__ __forceinline__ float ldf(const __nv_bfloat16 *p) {
+    return __bfloat162float(ldro<COH>(p));
+}
+__device__ __forceinline__ float ldf_plain(const float *p) { return *p; }
+__device__ __forceinline__ float ldf_plain(const __nv_bfloat16 *p) { return __bfloat162float(*p); }
+__device__ __forceinline__ void stf(float *p, float v) { *p = v; }
+__device__ __forceinline__ void stf(__nv_bfloat16 *p, float v) { *p = __float2bfloat16_rn(v); }
+// 8 consecutive values from a 16-byte aligned address (float: two float4
+// loads; bfloat16: one 16-byte load)
+template <bool COH = false> __device__ __forceinline__ void ld8(const float *p, float *o) {
+    const float4 a = ldro<COH>(reinterpret_cast<const float4 *>(p));
+    const float4 b = ldro<COH>(reinterpret_cast<const float4 *>(p) + 1);
+    o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = a.w; o[4] = b.x; o[5] = b.y; o[6] = b.z; o[7] = b.w;
+}
+template <bool COH = false> __device__ __forceinline__ void ld8(const __nv_bfloat16 *p, float *o) {
+    const uint4 a = ldro<COH>(reinterpret_cast<const uint4 *>(p));
+    const unsigned w[4] = {a.x, a.y, a.z, a.w};
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        o[2 * i] = __uint_as_float(w[i] << 16);
+        o[2 * i + 1] = __uint_as_float(w[i] & 0xffff0000u);
+    }
+}
 
 struct ViewGeo {
     float pd, od;  // driving-edge coefficients: p = pd*b + cp, o = od*b + co
@@ -182,13 +217,13 @@ __host__ __device__ inline int scl_stride(const vg_dd2d_geom &g) {
     return nm + (nm & 1);
 }
 
-size_t bp_ws_ts_bytes(const vg_dd2d_geom *g) {
+__host__ __device__ inline size_t bp_ws_ts_bytes(const vg_dd2d_geom *g) {
     return ((size_t)g->na * (g->nu + 1) * sizeof(float2) + 255) & ~(size_t)255;
 }
 size_t bp_ws_bytes(const vg_dd2d_geom *g) {
     return bp_ws_ts_bytes(g) + (((size_t)g->na * scl_stride(*g) * sizeof(float) + 255) & ~(size_t)255);
 }
-BpWork bp_ws(const vg_dd2d_geom *g, void *ws) {
+__host__ __device__ inline BpWork bp_ws(const vg_dd2d_geom *g, void *ws) {
     BpWork w;
     w.ts = reinterpret_cast<float2 *>(ws);
     w.scl = reinterpret_cast<float *>(reinterpret_cast<char *>(ws) + bp_ws_ts_bytes(g));
@@ -248,30 +283,28 @@ __device__ __forceinline__ void bp_prep_view(const vg_dd2d_geom &g, const float 
 // where inv_w == 0;  mode 2: mode 1, and the block (256 threads, all bins of
 // the view) then writes the view's back-projection table and line scales
 // into pw, as dd2d_bp_prep would from the residual row.
-template <bool FAN, int FP_WARPS, int FP_MAXB, bool GUARD>
-#ifndef VG_FP_MINB8
-#define VG_FP_MINB8 3
-#endif
-// (the guarded variants of the 24-bin tiles give up occupancy rather than spill)
-__global__ void __launch_bounds__(FP_WARPS * 32, ((FP_MAXB > 24 || (GUARD && FP_MAXB == 24)) ? 1 : (FP_WARPS >= 8 ? (FP_MAXB == 24 ? VG_FP_MINB8 : 2) : 16 / FP_WARPS)))
-dd2d_fp_kernel(vg_dd2d_geom g, const float *__restrict__ img, const float *__restrict__ imgT,
-               const double *__restrict__ trig, float *__restrict__ out, int mode,
-               const float *__restrict__ y, const float *__restrict__ inv_w, BpWork pw) {
+// One block's work: view ia, bins chunk * 32 FP_MAXB ...  smem2: the line
+// buffers (FP_WARPS fp_line_entries(nd) float2, also the warps' bin sums);
+// UC: 32 FP_MAXB + 32 float2 of shared memory.
+template <bool FAN, int FP_WARPS, int FP_MAXB, bool GUARD, typename TX, typename TY, bool COH = false>
+__device__ __forceinline__ void fp_block(const vg_dd2d_geom &g, int ia, int chunk,
+                                         const TX *__restrict__ img, const TX *__restrict__ imgT,
+                                         const double *__restrict__ trig, float *__restrict__ out,
+                                         int mode, const TY *__restrict__ y,
+                                         const float *__restrict__ inv_w, BpWork pw, float2 *smem2,
+                                         float2 *UC) {
     constexpr int FP_BINS = 32 * FP_MAXB;  // bins per block
-    extern __shared__ float2 smem2[];
-    __shared__ float2 UC[FP_BINS + 32];  // per bin edge (U, C(U)); entries past nb repeat nb
-    const int ia = blockIdx.y;
     const ViewGeo v = view_geo(trig, ia);
     const int nd = v.xdrv ? g.nx : g.ny;
     const int no = v.xdrv ? g.ny : g.nx;
-    const float *base = v.xdrv ? imgT : img;  // line io is contiguous in k
+    const TX *base = v.xdrv ? imgT : img;  // line io is contiguous in k
     const bool rev = v.pd < 0.f;               // edges decreasing in k: sweep reversed
     const int stride = fp_line_entries(nd);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     // rows start on 64-byte boundaries when nd % 16 == 0 (and the image is 16-byte aligned)
     const bool vec_rows = (nd % FP_SEG == 0) && ((reinterpret_cast<uintptr_t>(base) & 15) == 0);
     float2 *E = smem2 + (size_t)warp * stride;  // this warp's line buffer
-    const int jbase = blockIdx.x * FP_BINS;
+    const int jbase = chunk * FP_BINS;
     const int nb = min(FP_BINS, g.nu - jbase);  // bins of this block
     const float half = 0.5f * (float)nd;
     // The inverse edge map has a pole at U* = -DSD pd / od (rays parallel to
@@ -316,7 +349,7 @@ dd2d_fp_kernel(vg_dd2d_geom g, const float *__restrict__ img, const float *__res
             Pf = proj<FAN>(g, v, Lg.cp, Lg.co, edge_coord(g.d_pix, rev ? nd : 0, nd));
             Pl = proj<FAN>(g, v, Lg.cp, Lg.co, edge_coord(g.d_pix, rev ? 0 : nd, nd));
         }
-        const float *row = base + (size_t)io * nd;
+        const TX *row = base + (size_t)io * nd;
         // lanes own FP_SEG consecutive pixels (edge coordinate b0 + i db along
         // a lane's segment); along the segment the projection's numerator and
         // denominator are affine in the edge number i: P_i = (n0 + i dn) / (d0 + i dd)
@@ -343,21 +376,17 @@ dd2d_fp_kernel(vg_dd2d_geom g, const float *__restrict__ img, const float *__res
             // the segment is whole and aligned, else element by element
             float tot = 0.f;
             if (vec_rows && m0 + FP_SEG <= nd) {
-                const float4 *p4 = reinterpret_cast<const float4 *>(row + (rev ? nd - FP_SEG - m0 : m0));
+                static_assert(FP_SEG == 8, "segments of 8 pixels (one 16-byte load of bfloat16)");
                 float raw[FP_SEG];
-#pragma unroll
-                for (int j = 0; j < FP_SEG / 4; ++j) {
-                    const float4 t = __ldg(p4 + j);
-                    raw[4 * j] = t.x; raw[4 * j + 1] = t.y; raw[4 * j + 2] = t.z; raw[4 * j + 3] = t.w;
-                }
+                ld8<COH>(row + (rev ? nd - FP_SEG - m0 : m0), raw);
 #pragma unroll
                 for (int i = 0; i < FP_SEG; ++i) q[i] = (rev ? raw[FP_SEG - 1 - i] : raw[i]) * Lg.scl;
             } else {
-                const float *px = row + (rev ? nd - 1 - m0 : m0);
+                const TX *px = row + (rev ? nd - 1 - m0 : m0);
                 const int step = rev ? -1 : 1;
 #pragma unroll
                 for (int i = 0; i < FP_SEG; ++i)
-                    q[i] = (m0 + i < nd) ? __ldg(px + i * step) * Lg.scl : 0.f;
+                    q[i] = (m0 + i < nd) ? ldf<COH>(px + i * step) * Lg.scl : 0.f;
             }
 #pragma unroll
             for (int i = 0; i < FP_SEG; ++i) tot = fmaf(q[i], Pv[i + 1] - Pv[i], tot);
@@ -441,7 +470,7 @@ dd2d_fp_kernel(vg_dd2d_geom g, const float *__restrict__ img, const float *__res
         const size_t o = (size_t)ia * g.nu + jbase + e;
         if (mode >= 1) {
             const float wi = inv_w[o];
-            fp = (wi != 0.f) ? (y[o] - fp) * wi : fp;
+            fp = (wi != 0.f) ? (ldf(y + o) - fp) * wi : fp;
         }
         out[o] = fp;
         if (FP_WARPS == 8 && mode == 2) resid[e] = fp;
@@ -451,6 +480,21 @@ dd2d_fp_kernel(vg_dd2d_geom g, const float *__restrict__ img, const float *__res
         __syncthreads();
         bp_prep_view<FAN>(g, resid, ia, trig, pw, wsum);
     }
+}
+
+#ifndef VG_FP_MINB8
+#define VG_FP_MINB8 3
+#endif
+// (the guarded variants of the 24-bin tiles give up occupancy rather than spill)
+template <bool FAN, int FP_WARPS, int FP_MAXB, bool GUARD>
+__global__ void __launch_bounds__(FP_WARPS * 32, ((FP_MAXB > 24 || (GUARD && FP_MAXB == 24)) ? 1 : (FP_WARPS >= 8 ? (FP_MAXB == 24 ? VG_FP_MINB8 : 2) : 16 / FP_WARPS)))
+dd2d_fp_kernel(vg_dd2d_geom g, const float *__restrict__ img, const float *__restrict__ imgT,
+               const double *__restrict__ trig, float *__restrict__ out, int mode,
+               const float *__restrict__ y, const float *__restrict__ inv_w, BpWork pw) {
+    extern __shared__ float2 smem2[];
+    __shared__ float2 UC[32 * FP_MAXB + 32];  // per bin edge (U, C(U)); entries past nb repeat nb
+    fp_block<FAN, FP_WARPS, FP_MAXB, GUARD, float, float>(g, blockIdx.y, blockIdx.x, img, imgT, trig,
+                                                           out, mode, y, inv_w, pw, smem2, UC);
 }
 
 // ---------------------------------------------------------------------------
@@ -505,6 +549,7 @@ __device__ __forceinline__ float rcp_approx(float x) {
 #endif
 }
 
+template <bool COH = false>
 __device__ __forceinline__ float bp_G(const float2 *__restrict__ ts, int nu, float t) {
     // t: position in bins from U_0.  Before U_0 entry 0 gives x_0 = 0; past
     // U_nu entry nu holds (T_nu, 0).
@@ -513,11 +558,11 @@ __device__ __forceinline__ float bp_G(const float2 *__restrict__ ts, int nu, flo
     // floor from the bit pattern of a round-down add of 1.5 * 2^23 (FMA pipe),
     // clamped in the integer domain (huge t lands on entry nu)
     const int jb = min(__float_as_int(__fadd_rd(tc, 12582912.0f)), 0x4B400000 + nu);
-    const float2 e = __ldg(ts + (jb - 0x4B400000));
+    const float2 e = ldro<COH>(ts + (jb - 0x4B400000));
 #else
     // the conversion saturates
     const int j = min(__float2int_rz(tc), nu);
-    const float2 e = __ldg(ts + j);
+    const float2 e = ldro<COH>(ts + j);
 #endif
     return fmaf(e.y, tc, e.x);
 }
@@ -528,20 +573,23 @@ __device__ __forceinline__ float bp_G(const float2 *__restrict__ ts, int nu, flo
 // lookups for its 4 pixels, and the view and line parameters are read once.
 // mode 0: img = BP;  mode 1 (SIRT update): x += gamma * BP * inv_w (BP where
 // inv_w == 0), written to x and its transpose xT.
-template <bool FAN>
-__global__ void __launch_bounds__(BP_TY * BP_TX, VG_BP_MINB)
-dd2d_bp_kernel(vg_dd2d_geom g, BpWork w, const double *__restrict__ trig,
-               float *__restrict__ img, int mode, const float *__restrict__ inv_w, float gamma,
-               float *__restrict__ xT) {
+// One block's work: the pixel tile (tile_y, tile_x) of BP_TY x BP_TX patches.
+template <bool FAN, typename TX, bool COH = false>
+__device__ __forceinline__ void bp_block(const vg_dd2d_geom &g, int tile_y, int tile_x, BpWork w,
+                                         const double *__restrict__ trig, TX *__restrict__ img,
+                                         int mode, const float *__restrict__ inv_w, float gamma,
+                                         TX *__restrict__ xT) {
     // per view: fan (DSD pd/du, -od, DSD po/du, -oo), parallel (pd/du, 0, po/du, 0):
     // an edge b on the line through cen lands at bin position
     //   t = (x b + z cen) / (DSO + y b + w cen) + t0   (fan)
     //   t = x b + z cen + t0                           (parallel)
     __shared__ float4 Vs[BP_VC];
     __shared__ int Xs[BP_VC];
-    const int tid = threadIdx.y * BP_TY + threadIdx.x;
-    const int iy = blockIdx.x * (2 * BP_TY) + 2 * threadIdx.x;  // patch origin
-    const int ix = blockIdx.y * (2 * BP_TX) + 2 * threadIdx.y;
+    // linear thread index (2D blocks of BP_TY x BP_TX, or 1D blocks of as many)
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    const int tx = tid % BP_TY, ty = tid / BP_TY;
+    const int iy = tile_y * (2 * BP_TY) + 2 * tx;  // patch origin
+    const int ix = tile_x * (2 * BP_TX) + 2 * ty;
     const bool inside = iy < g.ny && ix < g.nx;
     const int sstr = scl_stride(g);
     const float t0 = -det_edge(g, 0) / g.du;
@@ -572,7 +620,7 @@ dd2d_bp_kernel(vg_dd2d_geom g, BpWork w, const double *__restrict__ trig,
             const int no = xd ? g.ny : g.nx;
             const float2 *ts = ts_all + (size_t)(a0 + vi) * (g.nu + 1);
             // signed scales of lines io0 and io0 + 1 (io0 is even; rows padded)
-            const float2 sc2 = __ldg(reinterpret_cast<const float2 *>(w.scl + (size_t)(a0 + vi) * sstr + io0));
+            const float2 sc2 = ldro<COH>(reinterpret_cast<const float2 *>(w.scl + (size_t)(a0 + vi) * sstr + io0));
             float cL[2][2];  // [line][position along the driving axis]
 #pragma unroll
             for (int L = 0; L < 2; ++L) {
@@ -585,7 +633,7 @@ dd2d_bp_kernel(vg_dd2d_geom g, BpWork w, const double *__restrict__ trig,
                     const float b = fmaf((float)e, g.d_pix, b0);
                     const float t = FAN ? fmaf(fmaf(q.x, b, nc), rcp_approx(fmaf(q.y, b, dc)), t0)
                                         : fmaf(q.x, b, nc);
-                    G[e] = bp_G(ts, g.nu, t);
+                    G[e] = bp_G<COH>(ts, g.nu, t);
                 }
                 const float s = (io0 + L < no) ? (L ? sc2.y : sc2.x) : 0.f;
                 cL[L][0] = (G[1] - G[0]) * s;
@@ -615,13 +663,21 @@ dd2d_bp_kernel(vg_dd2d_geom g, BpWork w, const double *__restrict__ trig,
             if (mode == 1) {
                 const float wi = inv_w[o];
                 const float upd = (wi != 0.f) ? bp * wi : bp;
-                const float xn = img[o] + gamma * upd;
-                img[o] = xn;
-                xT[(size_t)py * g.nx + px] = xn;
+                const float xn = ldf_plain(img + o) + gamma * upd;
+                stf(img + o, xn);
+                stf(xT + (size_t)py * g.nx + px, xn);
             } else {
-                img[o] = bp;
+                stf(img + o, bp);
             }
         }
+}
+
+template <bool FAN>
+__global__ void __launch_bounds__(BP_TY * BP_TX, VG_BP_MINB)
+dd2d_bp_kernel(vg_dd2d_geom g, BpWork w, const double *__restrict__ trig,
+               float *__restrict__ img, int mode, const float *__restrict__ inv_w, float gamma,
+               float *__restrict__ xT) {
+    bp_block<FAN, float>(g, blockIdx.x, blockIdx.y, w, trig, img, mode, inv_w, gamma, xT);
 }
 
 int check_geom(const vg_dd2d_geom *g) {
@@ -947,4 +1003,348 @@ extern "C" int vg_dd2d_bp_noalloc(const vg_dd2d_geom *g, const float *sino, cons
     if (st) return st;
     return launch_bp(g, sino, trig, img, 0, nullptr, 0.f, nullptr, ws, VG_NOALLOC_SCRATCH_BYTES,
                      as_stream(stream));
+}
+
+namespace {
+
+using namespace vg;
+
+// ---------------------------------------------------------------------------
+// Batched SIRT: many problems in one persistent launch.
+//
+// The grid (as many blocks of 256 threads as can be resident, launched
+// cooperatively so that they all are) runs `iters` SIRT updates of every
+// problem.  One update of problem p is three kinds of work items: forward
+// projection with the residual epilogue ((p, view, bin chunk)), the back
+// projection's tables ((p, view)) and the back projection with the update
+// epilogue ((p, pixel tile)).  All items of all updates form one queue,
+// update by update and, within an update, forward items, then table items,
+// then back-projection items, each kind ordered by the host (largest first);
+// blocks take the next item with an atomic counter.  An item waits only for
+// the items of its own problem it reads from -- the tables for all of p's
+// forward items of this update, the back projection for p's tables, p's next
+// forward projection for p's back projection -- counted per problem.  Every
+// dependency lies earlier in the queue and is held by a running block, so
+// no wait can block forever; waits are still bounded (BATCH_SPIN_LIMIT polls,
+// about two seconds), after which the run stops with VG_ERR_TIMEOUT.
+//
+// The block that takes the first item of an update checks the caller's
+// cancel flag (host-mapped memory) and the time budget (nanoseconds of
+// %globaltimer since the launch, 0 = none); either stops the run before that
+// update (VG_ERR_CANCELLED / VG_ERR_TIMEOUT), and back-projection items of an
+// update wait for that check, so a run always ends between updates.  The
+// iterates and the measured sinograms may be stored as bfloat16 (arithmetic
+// in float32).
+// ---------------------------------------------------------------------------
+
+constexpr int BATCH_THREADS = 256;
+constexpr long long BATCH_SPIN_LIMIT = 1ll << 25;   // polls of 64 ns sleeps
+constexpr int BATCH_UC = 32 * 24 + 32;              // UC entries of the widest tile
+
+struct BatchCtrl {
+    unsigned long long next;  // queue head
+    int status, done;
+    int stop_p;               // 0, or INT_MAX - (the first update not run) once stopped
+    int checked;              // updates whose start has been checked
+    unsigned exited, pad;
+    unsigned long long t0;    // %globaltimer at the first item
+};
+
+__device__ __forceinline__ int batch_stop_iter(const BatchCtrl *c, int iters) {
+    const int sp = *(const volatile int *)&c->stop_p;
+    return sp ? 0x7fffffff - sp : iters;
+}
+static_assert(sizeof(BatchCtrl) == sizeof(vg_sirt2d_batch_ctrl), "control block layout");
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__host__ __device__ inline int batch_maxb(int nu) { return nu <= 192 ? 6 : (nu <= 384 ? 12 : 24); }
+__host__ __device__ inline int batch_nfp(const vg_dd2d_geom &g) {
+    const int mb = batch_maxb(g.nu);
+    return g.na * ((g.nu + 32 * mb - 1) / (32 * mb));
+}
+__host__ __device__ inline int batch_nbp(const vg_dd2d_geom &g) {
+    return ((g.ny + 2 * BP_TY - 1) / (2 * BP_TY)) * ((g.nx + 2 * BP_TX - 1) / (2 * BP_TX));
+}
+
+// thread 0: wait until *cnt >= target (bounded) for an item of update `it`;
+// false after a wait that ran out (the run then stops with VG_ERR_TIMEOUT),
+// or once the run stops before update `it`
+__device__ bool batch_wait(BatchCtrl *c, const int *cnt, long long target, int it, int iters) {
+    const volatile int *vcnt = cnt;
+    long long n = 0;
+    while ((long long)*vcnt < target) {
+        const int sp = *(volatile int *)&c->stop_p;
+        if (sp == 0 && *(volatile int *)&c->status != 0) return false;  // a wait ran out
+        if (it >= batch_stop_iter(c, iters)) return false;
+        if (++n > BATCH_SPIN_LIMIT) {
+            atomicCAS(&c->status, 0, VG_ERR_TIMEOUT);
+            return false;
+        }
+        __nanosleep(64);
+    }
+    __threadfence();
+    return true;
+}
+
+template <bool FAN, int MAXB, typename TX, typename TY>
+__device__ __forceinline__ void batch_fp(const vg_sirt2d_problem &p, int view, int chunk, float2 *lines,
+                                         float2 *UC) {
+    fp_block<FAN, 8, MAXB, false, TX, TY, true>(p.g, view, chunk, static_cast<const TX *>(p.x),
+                                          static_cast<const TX *>(p.xT), p.trig, p.r, 1,
+                                          static_cast<const TY *>(p.y), p.inv_w_sino,
+                                          BpWork{nullptr, nullptr}, lines, UC);
+}
+
+// counters: per problem 3 ints (forward, table, back-projection items done)
+template <typename TX, typename TY>
+__global__ void __launch_bounds__(BATCH_THREADS, 2)
+sirt2d_batch_kernel(const vg_sirt2d_problem *__restrict__ P, int nprob,
+                    const int2 *__restrict__ fp_items, int n_fp, const int2 *__restrict__ tab_items,
+                    int n_tab, const int2 *__restrict__ bp_items, int n_bp, int iters,
+                    const volatile int *cancel, unsigned long long budget_ns, BatchCtrl *ctrl,
+                    int *counters) {
+    extern __shared__ float2 dsm[];
+    float2 *UC = dsm, *lines = dsm + BATCH_UC;
+    __shared__ long long item_s;
+    __shared__ double wsum[BATCH_THREADS / 32];
+    const long long total = (long long)n_fp + n_tab + n_bp;
+    for (;;) {
+        __syncthreads();  // the previous item's shared memory and item_s are no longer read
+        if (threadIdx.x == 0) {
+            long long k = -1;
+            volatile BatchCtrl *vc = ctrl;
+            const bool hard = vc->stop_p == 0 && vc->status != 0;  // a wait ran out
+            if (!hard) {
+                const long long q = (long long)atomicAdd(&ctrl->next, 1ull);
+                const int it = (int)(q / total);
+                const long long r = q % total;
+                if (it < iters && it < batch_stop_iter(ctrl, iters)) {
+                    k = q;
+                    if (r == 0) {
+                        // the start of update `it`: the cancel flag and the time budget
+                        if (q == 0) atomicCAS(&ctrl->t0, 0ull, global_ns());
+                        int why = 0;
+                        const unsigned long long t0 = vc->t0;
+                        if (it > 0 && cancel && *cancel) why = VG_ERR_CANCELLED;
+                        else if (it > 0 && budget_ns && t0 && global_ns() - t0 > budget_ns)
+                            why = VG_ERR_TIMEOUT;
+                        if (why) {
+                            atomicMax(&ctrl->stop_p, 0x7fffffff - it);
+                            atomicCAS(&ctrl->status, 0, why);
+                            k = -1;
+                        }
+                        __threadfence();
+                        atomicMax(&ctrl->checked, it + 1);
+                    }
+                }
+            }
+            item_s = k;
+        }
+        __syncthreads();
+        const long long k = item_s;
+        if (k < 0) break;  // every item of an earlier update is held by a running block
+        const int it = (int)(k / total);
+        const long long r = k % total;
+        int kind, prob, sub;
+        if (r < n_fp) { kind = 0; prob = fp_items[r].x; sub = fp_items[r].y; }
+        else if (r < n_fp + n_tab) { kind = 1; prob = tab_items[r - n_fp].x; sub = tab_items[r - n_fp].y; }
+        else { kind = 2; prob = bp_items[r - n_fp - n_tab].x; sub = bp_items[r - n_fp - n_tab].y; }
+        const vg_sirt2d_problem &p = P[prob];
+        // the item's inputs: p's back projection of the previous update, p's
+        // forward projection or p's tables of this one
+        if (threadIdx.x == 0) {
+            bool ok;
+            if (kind == 0)
+                ok = batch_wait(ctrl, counters + 3 * prob + 2, (long long)it * batch_nbp(p.g), it, iters);
+            else if (kind == 1)
+                ok = batch_wait(ctrl, counters + 3 * prob, (long long)(it + 1) * batch_nfp(p.g), it, iters);
+            else
+                ok = batch_wait(ctrl, counters + 3 * prob + 1, (long long)(it + 1) * p.g.na, it, iters) &&
+                     batch_wait(ctrl, &ctrl->checked, it + 1, it, iters) &&
+                     it < batch_stop_iter(ctrl, iters);
+            item_s = ok ? k : -1;
+        }
+        __syncthreads();
+        if (item_s < 0) break;
+        if (kind == 0) {
+            const int mb = batch_maxb(p.g.nu);
+            const int nch = (p.g.nu + 32 * mb - 1) / (32 * mb);
+            const int view = sub / nch, chunk = sub % nch;
+            if (p.g.fan) {
+                if (mb == 6) batch_fp<true, 6, TX, TY>(p, view, chunk, lines, UC);
+                else if (mb == 12) batch_fp<true, 12, TX, TY>(p, view, chunk, lines, UC);
+                else batch_fp<true, 24, TX, TY>(p, view, chunk, lines, UC);
+            } else {
+                if (mb == 6) batch_fp<false, 6, TX, TY>(p, view, chunk, lines, UC);
+                else if (mb == 12) batch_fp<false, 12, TX, TY>(p, view, chunk, lines, UC);
+                else batch_fp<false, 24, TX, TY>(p, view, chunk, lines, UC);
+            }
+        } else if (kind == 1) {
+            const BpWork w = bp_ws(&p.g, p.workspace);
+            if (p.g.fan) bp_prep_view<true, BATCH_THREADS>(p.g, p.r + (size_t)sub * p.g.nu, sub, p.trig, w, wsum);
+            else bp_prep_view<false, BATCH_THREADS>(p.g, p.r + (size_t)sub * p.g.nu, sub, p.trig, w, wsum);
+        } else {
+            const int nty = (p.g.ny + 2 * BP_TY - 1) / (2 * BP_TY);
+            const BpWork w = bp_ws(&p.g, p.workspace);
+            if (p.g.fan)
+                bp_block<true, TX, true>(p.g, sub % nty, sub / nty, w, p.trig, static_cast<TX *>(p.x), 1,
+                                   p.inv_w_img, p.gamma, static_cast<TX *>(p.xT));
+            else
+                bp_block<false, TX, true>(p.g, sub % nty, sub / nty, w, p.trig, static_cast<TX *>(p.x), 1,
+                                    p.inv_w_img, p.gamma, static_cast<TX *>(p.xT));
+        }
+        __syncthreads();  // the item's writes are done
+        if (threadIdx.x == 0) {
+            __threadfence();
+            atomicAdd(counters + 3 * prob + kind, 1);
+        }
+    }
+    // the last block out records the updates every problem completed
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(&ctrl->exited, 1u) == gridDim.x - 1) {
+            int done = iters;
+            for (int q = 0; q < nprob; ++q) {
+                const int d = *(volatile int *)(counters + 3 * q + 2) / batch_nbp(P[q].g);
+                done = min(done, d);
+            }
+            ctrl->done = done;
+        }
+    }
+}
+
+size_t batch_smem(int max_nd) {
+    size_t lines = (size_t)8 * fp_line_entries(max_nd) * sizeof(float2);
+    const size_t red = (size_t)8 * 32 * 24 * sizeof(float);
+    if (lines < red) lines = red;
+    return (size_t)BATCH_UC * sizeof(float2) + lines;
+}
+
+int batch_check(const vg_sirt2d_problem *p) {
+    int st = check_geom(&p->g);
+    if (st) return st;
+    VG_REQUIRE(p->y && p->inv_w_sino && p->inv_w_img && p->trig && p->x && p->xT && p->r &&
+                   p->workspace, "sirt2d_batch: null pointer in a problem");
+    VG_REQUIRE(((uintptr_t)p->workspace & 255) == 0, "sirt2d_batch: workspace must be 256-byte aligned");
+    const float ext = fmaxf(fabsf(p->g.du * (0.f - 0.5f * p->g.nu + p->g.su)),
+                            fabsf(p->g.du * ((float)p->g.nu - 0.5f * p->g.nu + p->g.su)));
+    VG_REQUIRE(!p->g.fan || ext < p->g.DSD,
+               "sirt2d_batch: a fan detector reaching DSD from its centre is not batched");
+    return VG_OK;
+}
+
+template <typename TX, typename TY>
+int batch_launch(const vg_sirt2d_problem *probs_dev, int nprob, int max_nd, const int *fp, int n_fp,
+                 const int *tab, int n_tab, const int *bp, int n_bp, int iters, const int *cancel,
+                 unsigned long long budget_ns, void *ctrl, int *counters, cudaStream_t st,
+                 int *grid_out) {
+    auto kern = sirt2d_batch_kernel<TX, TY>;
+    const size_t smem = batch_smem(max_nd);
+    VG_REQUIRE(smem <= 200 * 1024, "sirt2d_batch: images above %d pixels a side", max_nd);
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return cuda_status(e, "sirt2d_batch: shared memory attribute");
+    int dev = 0, nsm = 0, per = 0;
+    e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, BATCH_THREADS, smem);
+    if (e != cudaSuccess) return cuda_status(e, "sirt2d_batch: occupancy");
+    VG_REQUIRE(per > 0, "sirt2d_batch: the kernel does not fit on a multiprocessor");
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(nsm * per);
+    cfg.blockDim = dim3(BATCH_THREADS);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    if (grid_out) *grid_out = nsm * per;
+    e = cudaLaunchKernelEx(&cfg, kern, probs_dev, nprob, reinterpret_cast<const int2 *>(fp), n_fp,
+                           reinterpret_cast<const int2 *>(tab), n_tab,
+                           reinterpret_cast<const int2 *>(bp), n_bp, iters,
+                           reinterpret_cast<const volatile int *>(cancel), budget_ns,
+                           static_cast<BatchCtrl *>(ctrl), counters);
+    if (e != cudaSuccess) return cuda_status(e, "sirt2d_batch: launch");
+    return launch_status("sirt2d_batch");
+}
+
+}  // namespace
+
+extern "C" int vg_sirt2d_batch_items(const vg_sirt2d_problem *probs, int n, int *fp_items,
+                                     int *n_fp, int *tab_items, int *n_tab, int *bp_items, int *n_bp) {
+    VG_REQUIRE(probs && n > 0 && n_fp && n_tab && n_bp, "sirt2d_batch_items: bad arguments");
+    long long cf = 0, ct = 0, cb = 0;
+    for (int i = 0; i < n; ++i) {
+        int st = batch_check(&probs[i]);
+        if (st) return st;
+        const vg_dd2d_geom &g = probs[i].g;
+        cf += batch_nfp(g);
+        ct += g.na;
+        cb += batch_nbp(g);
+    }
+    VG_REQUIRE(cf < (1ll << 30) && cb < (1ll << 30), "sirt2d_batch_items: too many work items");
+    if (fp_items && tab_items && bp_items) {
+        // items in problem order; the caller may reorder each list freely
+        long long a = 0, b = 0, c = 0;
+        for (int i = 0; i < n; ++i) {
+            const vg_dd2d_geom &g = probs[i].g;
+            const int nf = batch_nfp(g), nt = batch_nbp(g);
+            for (int k = 0; k < nf; ++k, ++a) { fp_items[2 * a] = i; fp_items[2 * a + 1] = k; }
+            for (int k = 0; k < g.na; ++k, ++b) { tab_items[2 * b] = i; tab_items[2 * b + 1] = k; }
+            for (int k = 0; k < nt; ++k, ++c) { bp_items[2 * c] = i; bp_items[2 * c + 1] = k; }
+        }
+    }
+    *n_fp = (int)cf;
+    *n_tab = (int)ct;
+    *n_bp = (int)cb;
+    return VG_OK;
+}
+
+extern "C" int vg_sirt2d_batch_run(const vg_sirt2d_problem *probs_dev, int n, int max_nd,
+                                   const int *fp_items, int n_fp, const int *tab_items, int n_tab,
+                                   const int *bp_items, int n_bp, int iters, int storage,
+                                   const int *cancel, unsigned long long budget_ns,
+                                   vg_sirt2d_batch_ctrl *ctrl, int *counters, void *stream,
+                                   int *grid_blocks) {
+    VG_REQUIRE(probs_dev && n > 0 && fp_items && tab_items && bp_items && ctrl && counters,
+               "sirt2d_batch_run: null pointer");
+    VG_REQUIRE((long long)(n_fp + (long long)n_tab + n_bp) * iters < (1ll << 62),
+               "sirt2d_batch_run: too many items");
+    VG_REQUIRE(n_fp > 0 && n_tab > 0 && n_bp > 0 && iters >= 0 && max_nd > 0,
+               "sirt2d_batch_run: bad counts");
+    VG_REQUIRE(storage >= 0 && storage <= 3, "sirt2d_batch_run: storage %d not in 0..3", storage);
+    cudaStream_t st = as_stream(stream);
+    if (cancel) {
+        // pinned host memory: its device address (the same pointer under unified addressing)
+        void *dp = nullptr;
+        if (cudaHostGetDevicePointer(&dp, const_cast<int *>(cancel), 0) == cudaSuccess && dp)
+            cancel = static_cast<const int *>(dp);
+        else
+            cudaGetLastError();  // not registered host memory: used as given
+    }
+    cudaError_t e = cudaMemsetAsync(ctrl, 0, sizeof(vg_sirt2d_batch_ctrl), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(counters, 0, (size_t)3 * n * sizeof(int), st);
+    if (e != cudaSuccess) return cuda_status(e, "sirt2d_batch_run: control block");
+    const bool bx = storage & 1, by = storage & 2;
+    if (!bx && !by)
+        return batch_launch<float, float>(probs_dev, n, max_nd, fp_items, n_fp, tab_items, n_tab,
+                                          bp_items, n_bp, iters, cancel, budget_ns, ctrl, counters, st,
+                                          grid_blocks);
+    if (bx && !by)
+        return batch_launch<__nv_bfloat16, float>(probs_dev, n, max_nd, fp_items, n_fp, tab_items,
+                                                  n_tab, bp_items, n_bp, iters, cancel, budget_ns, ctrl,
+                                                  counters, st, grid_blocks);
+    if (!bx && by)
+        return batch_launch<float, __nv_bfloat16>(probs_dev, n, max_nd, fp_items, n_fp, tab_items,
+                                                  n_tab, bp_items, n_bp, iters, cancel, budget_ns, ctrl,
+                                                  counters, st, grid_blocks);
+    return batch_launch<__nv_bfloat16, __nv_bfloat16>(probs_dev, n, max_nd, fp_items, n_fp,
+                                                      tab_items, n_tab, bp_items, n_bp, iters, cancel,
+                                                      budget_ns, ctrl, counters, st, grid_blocks);
 }
