@@ -191,9 +191,10 @@ __device__ __forceinline__ void fp_cells(const float4 *uw, const int *uk, const 
 #ifndef VG_CONE_FP_MINB
 #define VG_CONE_FP_MINB 3
 #endif
+template <int MODE>  // 0: projection; 1: SIRT residual epilogue
 __global__ void __launch_bounds__(256, VG_CONE_FP_MINB)
 dd3d_fp_kernel(vg_dd3d_geom g, const float *__restrict__ vol, const float4 *__restrict__ vf,
-               const float2 *__restrict__ tab, float *__restrict__ sino, int mode,
+               const float2 *__restrict__ tab, float *__restrict__ sino,
                const float *__restrict__ y, const float *__restrict__ inv_w) {
     __shared__ FpTables S;
     const int ia = blockIdx.z;
@@ -335,7 +336,7 @@ dd3d_fp_kernel(vg_dd3d_geom g, const float *__restrict__ vol, const float4 *__re
             if (iu < g.nu && iv < g.nv) {
                 const size_t o = ((size_t)ia * g.nu + iu) * g.nv + iv;
                 float fp = acc[2 * j + h] * f;
-                if (mode) {  // SIRT residual: (y - FP) / W_sino, FP kept where W_sino == 0
+                if (MODE) {  // SIRT residual: (y - FP) / W_sino, FP kept where W_sino == 0
                     const float wi = inv_w[o];
                     fp = (wi != 0.f) ? (y[o] - fp) * wi : fp;
                 }
@@ -392,9 +393,10 @@ __device__ float bp_voxel_view(const vg_dd3d_geom &g, const View3 &v, const floa
 #ifndef VG_CONE_BP_MINB
 #define VG_CONE_BP_MINB 5
 #endif
+template <int MODE>  // 0: back projection; 1: SIRT update epilogue
 __global__ void __launch_bounds__(256, VG_CONE_BP_MINB)
 dd3d_bp_kernel(vg_dd3d_geom g, const float *__restrict__ sino, const float4 *__restrict__ vf,
-               const float2 *__restrict__ tab, float *__restrict__ vol, int mode,
+               const float2 *__restrict__ tab, float *__restrict__ vol,
                const float *__restrict__ inv_w, float gamma) {
     __shared__ BpTables T;
     const int z0 = blockIdx.x * BZ, y0 = blockIdx.y * BT, x0 = blockIdx.z * BT;
@@ -523,7 +525,7 @@ dd3d_bp_kernel(vg_dd3d_geom g, const float *__restrict__ sino, const float4 *__r
         if (ix < g.nx && iy < g.ny && iz < g.nz) {
             const size_t o = ((size_t)ix * g.ny + iy) * g.nz + iz;
             const float bp = acc[i].s * f;
-            if (mode) {  // SIRT update: x += gamma BP / W_img, BP where W_img == 0
+            if (MODE) {  // SIRT update: x += gamma BP / W_img, BP where W_img == 0
                 const float wi = inv_w[o];
                 vol[o] += gamma * ((wi != 0.f) ? bp * wi : bp);
             } else {
@@ -570,10 +572,10 @@ extern "C" int vg_dd3d_fp(const vg_dd3d_geom *g, const float *vol, const double 
     s = launch_prep(g, trig, workspace, workspace_bytes, st);
     if (s) return s;
     dim3 grid(ceil_div(g->nv, FT_V), ceil_div(g->nu, FT_U), g->na);
-    dd3d_fp_kernel<<<grid, 256, 0, st>>>(
+    dd3d_fp_kernel<0><<<grid, 256, 0, st>>>(
         *g, vol,
         reinterpret_cast<const float4 *>(static_cast<const char *>(workspace) + tab_bytes(g)),
-        reinterpret_cast<const float2 *>(workspace), sino, 0, nullptr, nullptr);
+        reinterpret_cast<const float2 *>(workspace), sino, nullptr, nullptr);
     return launch_status("dd3d_fp");
 }
 
@@ -586,10 +588,10 @@ extern "C" int vg_dd3d_bp(const vg_dd3d_geom *g, const float *sino, const double
     s = launch_prep(g, trig, workspace, workspace_bytes, st);
     if (s) return s;
     dim3 grid(ceil_div(g->nz, BZ), ceil_div(g->ny, BT), ceil_div(g->nx, BT));
-    dd3d_bp_kernel<<<grid, 256, 0, st>>>(
+    dd3d_bp_kernel<0><<<grid, 256, 0, st>>>(
         *g, sino,
         reinterpret_cast<const float4 *>(static_cast<const char *>(workspace) + tab_bytes(g)),
-        reinterpret_cast<const float2 *>(workspace), vol, 0, nullptr, 0.f);
+        reinterpret_cast<const float2 *>(workspace), vol, nullptr, 0.f);
     return launch_status("dd3d_bp");
 }
 
@@ -605,10 +607,10 @@ extern "C" int vg_dd3d_sirt_iter(const vg_dd3d_geom *g, const float *y, const fl
     const float4 *vf = reinterpret_cast<const float4 *>(static_cast<const char *>(workspace) + tab_bytes(g));
     const float2 *tab = reinterpret_cast<const float2 *>(workspace);
     dim3 gf(ceil_div(g->nv, FT_V), ceil_div(g->nu, FT_U), g->na);
-    dd3d_fp_kernel<<<gf, 256, 0, st>>>(*g, x, vf, tab, r, 1, y, inv_w_sino);
+    dd3d_fp_kernel<1><<<gf, 256, 0, st>>>(*g, x, vf, tab, r, y, inv_w_sino);
     s = launch_status("dd3d_fp");
     if (s) return s;
     dim3 gb(ceil_div(g->nz, BZ), ceil_div(g->ny, BT), ceil_div(g->nx, BT));
-    dd3d_bp_kernel<<<gb, 256, 0, st>>>(*g, r, vf, tab, x, 1, inv_w_img, gamma);
+    dd3d_bp_kernel<1><<<gb, 256, 0, st>>>(*g, r, vf, tab, x, inv_w_img, gamma);
     return launch_status("dd3d_bp");
 }
