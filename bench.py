@@ -328,7 +328,8 @@ def run_workload(args):
     """One JSON line for a configuration other than the default C2 line:
     per-kernel CUDA-event times (median of --steps after --warmup), GUPS and
     the algorithmic-byte roofline.  With --kernels-only N the projector pair
-    is just launched N times (for ncu captures)."""
+    is just launched N times (for ncu captures): c4 / c5 then also the
+    separable-footprint pair, c3 runs N persistent launches of 2 updates."""
     import torch
     from vir_gb300 import phantoms as ph
     from vir_gb300.sys_mat import dd
@@ -686,6 +687,13 @@ def run_workload(args):
         from vir_gb300.workloads import batched_problems
         from vir_gb300.batched import PersistentSIRT2D
         probs = batched_problems(64, seed=3)
+        if args.kernels_only:  # profiling aid: N persistent launches of 2 updates each
+            pb = PersistentSIRT2D(probs, device=dev)
+            for _ in range(args.kernels_only):
+                pb.reset()
+                pb.run(2)
+            print(json.dumps({"kernels_only": args.kernels_only, "workload": wl, "ok": True}))
+            return 0
         b = BatchedSIRT2D(probs, n_streams=16)
         res = {}
         for mode in ("graph", "plain"):
@@ -726,6 +734,11 @@ def run_workload(args):
     if args.kernels_only:
         for _ in range(args.kernels_only):
             fp(); bp()
+        if wl in ("c4", "c5"):  # then the separable-footprint pair
+            from vir_gb300.sys_mat import sp
+            for _ in range(args.kernels_only):
+                sp.sf_fp_cone_3d(x, angs, nu, nv, 600.0, 1100.0, **kw)
+                sp.sf_bp_cone_3d(y, angs, (n, n, n), 600.0, 1100.0, **kw)
         torch.cuda.synchronize()
         print(json.dumps({"kernels_only": args.kernels_only, "workload": wl, "ok": True}))
         return 0
