@@ -95,9 +95,8 @@ int vg_div_rn_check(const double *a, const double *b, size_t n, double *q, void 
 
 /* ---- Siddon ray lists (3D) ------------------------------------------------ */
 
-/* Per-ray set-up of sys_mat/siddon.py:siddons (computed on the host in the
- * reference's numpy arithmetic, :681-751) and the grid planes; all arrays are
- * device pointers.  src/dst are (n_rays, 3) float32 source and target-source
+/* Per-ray set-up of sys_mat/siddon.py:siddons (:681-751, computed by
+ * vg_siddons_setup) and the grid planes; all arrays are device pointers.  src/dst are (n_rays, 3) float32 source and target-source
  * vectors, dist the float32 ray length, amin/amax the alpha range, i0/iN the
  * per-axis plane index range [i0, iN), valid the rays that cross the grid. */
 typedef struct {
@@ -110,6 +109,28 @@ typedef struct {
     const int *i0, *iN;                /* (n_rays, 3) */
     const unsigned char *valid;        /* (n_rays) */
 } vg_siddon_rays;
+
+/* Grid of the per-ray set-up: sizes, float32 pitches, the first and last
+ * plane coordinate of each axis (boundspace's float32 planes,
+ * core_funcs.py:62-81), and siddons' epsilon as float64 and float32. */
+typedef struct {
+    int nx, ny, nz;
+    float dx, dy, dz;
+    float p0[3], pN[3];
+    double epsilon;
+    float epsilon_f;
+    int pad;
+} vg_siddons_grid;
+
+/* The per-ray set-up of siddons (sys_mat/siddon.py:681-751) on the device,
+ * one thread per ray, each operation in the type numpy gives it: from
+ * src / trg ((n, 3) float32, broadcast by the caller) it writes dst = trg -
+ * src, dist (np.linalg.norm), the alpha range amin / amax, the per-axis
+ * plane index range [i0, iN) as numpy slice bounds, and valid.  Replaces the
+ * reference's vectorised numpy set-up; the outputs feed vg_siddon_rays. */
+int vg_siddons_setup(const vg_siddons_grid *g, int n, const float *src, const float *trg,
+                     float *dst, float *dist, float *amin, float *amax, int *i0, int *iN,
+                     unsigned char *valid, void *stream);
 
 /* Pass 1 of siddons (the per-ray loop, sys_mat/siddon.py:754-826): number
  * of kept (voxel, length) entries per ray into counts (n_rays ints); *err

@@ -56,11 +56,9 @@ def test_list_projection_vs_reference_c(vg, golden):
     assert np.abs(bp - c["bp"]).max() <= 2e-6 * np.abs(c["bp"]).max()
 
 
-def test_list_c1_scale_vs_oracle(vg, orc):
-    """Config C1 geometry through siddons (GPU) and list FP/BP vs the oracle."""
-    import torch
-    from vir_gb300.projection import proj
-    from vir_gb300.sys_mat import siddon
+def c1_rays():
+    """The C1 list geometry: 180 parallel views over pi, 367 rays each, a
+    256 x 256 x 1 grid of unit voxels; (src, trg, nPixels, dPixels, origin)."""
     dets = np.arange(367) - 183.0
     views = np.linspace(0, np.pi, 180, endpoint=False)
     # proj_geom.geom_circular(..., geom="par") restated: rays along x rotated by each view
@@ -70,7 +68,16 @@ def test_list_c1_scale_vs_oracle(vg, orc):
         R = np.array([[c, s], [-s, c]])
         src[i, :, :2] = np.stack([np.full(367, -36700.0), dets], -1) @ R
         trg[i, :, :2] = np.stack([np.full(367, 36700.0), dets], -1) @ R
-    ind, ln, off, shape, grid = siddon.siddons_device(src, trg, (256, 256, 1), 1.0)
+    return src, trg, (256, 256, 1), 1.0, 0.0
+
+
+def test_list_c1_scale_vs_oracle(vg, orc):
+    """Config C1 geometry through siddons (GPU) and list FP/BP vs the oracle."""
+    import torch
+    from vir_gb300.projection import proj
+    from vir_gb300.sys_mat import siddon
+    src, trg, nP, dP, _ = c1_rays()
+    ind, ln, off, shape, grid = siddon.siddons_device(src, trg, nP, dP)
     assert off.numel() == 180 * 367 + 1 and ind.numel() > 14_000_000
     x = np.random.default_rng(3).random((256, 256, 1)).astype(np.float32)
     fp = proj.list_fp_device(torch.from_numpy(x).cuda().reshape(-1), ind, ln, off).cpu().numpy()
@@ -125,3 +132,45 @@ def test_numba_list_entry_points(vg, golden):
     out = np.zeros(nr, np.float32)
     proj_numba.fast_forward_project_p(c["phantom"].ravel(), d["ind"], d["len"], d["off"], out)
     assert np.abs(out - ref).max() <= 2e-6 * np.abs(ref).max()
+
+
+def test_siddons_setup_device_matches_reference_steps(vg, golden, orc):
+    """The device set-up of siddons (vg_siddons_setup) equals the oracle's
+    step-by-step restatement of siddon.py:681-751 bit for bit: on the
+    reference's golden rays, random rays with zero direction components,
+    zero-length rays and integer end points (plane hits), and the C1 list
+    geometry.  Plane indices of axes a ray does not move along, and of rays
+    that miss the grid, are not read by the kernels; the latter can lie
+    beyond the int32 range, whose conversion numpy leaves to the platform
+    (INT_MIN on x86, saturation on Arm; the kernel gives INT_MIN)."""
+    import warnings
+    from vir_gb300.sys_mat import siddon
+    rng = np.random.default_rng(17)
+    cases = [(golden[c]["src"], golden[c]["trg"], golden[c]["nPixels"], golden[c]["dPixels"], 0.0)
+             for c in ("siddons_edge", "siddons_par", "siddons_cone")]
+    s, t = rng.uniform(-60, 60, (4000, 3)), rng.uniform(-60, 60, (4000, 3))
+    s[::7, 1] = t[::7, 1]
+    s[::11, 2] = t[::11, 2]
+    s[::13] = t[::13]
+    cases.append((s, t, (20, 18, 14), (1.1, 0.9, 1.3), (0.5, -0.3, 0.2)))
+    s, t = rng.integers(-30, 30, (3000, 3)).astype(float), rng.integers(-30, 30, (3000, 3)).astype(float)
+    cases.append((s, t, (16, 16, 16), 1.0, 0.0))
+    # a broadcast source (one point against a detector of targets)
+    t = np.stack(np.meshgrid(np.linspace(-40, 40, 61), np.linspace(-9, 9, 7), indexing="ij"), -1)
+    t = np.concatenate([np.full(t.shape[:2] + (1,), -80.0), t], -1)
+    cases.append((np.array([90.0, 0.3, -0.2]), t, (24, 24, 8), (2.0, 2.0, 1.5), 0.0))
+    cases.append(c1_rays())
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        for src, trg, nP, dP, oP in cases:
+            shape, _, a = siddon.setup_device(src, trg, nP, dP, oP, 1e-5)
+            a = {k: v.cpu().numpy() for k, v in a.items()}
+            sb = np.broadcast_to(np.asarray(src, np.float32), np.shape(trg)).reshape(-1, 3)
+            o = orc.siddons_setup(sb, np.asarray(trg).reshape(-1, 3), nP, dP, oP, 1e-5)
+            assert a["amin"].shape == (int(np.prod(shape)),)
+            moves = (o["dst"] != 0.0) & o["valid"].astype(bool)[:, None]
+            assert np.array_equal(a["dst"].view(np.uint8), np.ascontiguousarray(o["dst"]).view(np.uint8))
+            for k in ("amin", "amax", "dist", "valid"):
+                assert np.array_equal(a[k].view(np.uint8), np.ascontiguousarray(o[k]).view(np.uint8)), k
+            for k in ("i0", "iN"):
+                assert np.array_equal(np.where(moves, a[k], 0), np.where(moves, o[k], 0)), k

@@ -415,37 +415,6 @@ def test_trajectory_interpZ_batch():
                 assert np.array_equal(np.asarray(ref[k]), bat[k][i], equal_nan=True), (nV, i, k)
 
 
-def test_siddons_setup_matches_reference_steps(golden):
-    """vir_gb300's vectorised siddons set-up (selected np.where operands only)
-    equals the step-by-step restatement of siddon.py:681-751 bit for bit: on
-    the reference's golden rays and on random rays with zero direction
-    components, zero-length rays and integer end points (plane hits).  Plane
-    indices of axes the ray does not move along are not read by the kernels."""
-    import warnings
-    from oracle import oracle as orc
-    from vir_gb300.sys_mat import siddon
-    rng = np.random.default_rng(17)
-    cases = [(golden[c]["src"], golden[c]["trg"], golden[c]["nPixels"], golden[c]["dPixels"], 0.0)
-             for c in ("siddons_edge", "siddons_par", "siddons_cone")]
-    s, t = rng.uniform(-60, 60, (4000, 3)), rng.uniform(-60, 60, (4000, 3))
-    s[::7, 1] = t[::7, 1]
-    s[::11, 2] = t[::11, 2]
-    s[::13] = t[::13]
-    cases.append((s, t, (20, 18, 14), (1.1, 0.9, 1.3), (0.5, -0.3, 0.2)))
-    s, t = rng.integers(-30, 30, (3000, 3)).astype(float), rng.integers(-30, 30, (3000, 3)).astype(float)
-    cases.append((s, t, (16, 16, 16), 1.0, 0.0))
-    with warnings.catch_warnings():
-        warnings.simplefilter("ignore")
-        for src, trg, nP, dP, oP in cases:
-            _, _, a = siddon.prepare(src, trg, nP, dP, oP, 1e-5)
-            o = orc.siddons_setup(src, trg, nP, dP, oP, 1e-5)
-            moves = o["dst"] != 0.0
-            for k in ("amin", "amax", "dist", "valid"):
-                assert np.array_equal(a[k].view(np.uint8), np.ascontiguousarray(o[k]).view(np.uint8)), k
-            for k in ("i0", "iN"):
-                assert np.array_equal(np.where(moves, a[k], 0), np.where(moves, o[k], 0)), k
-
-
 def test_fbp_weights_vs_reference(golden, orc):
     """The pre-weight of vir's fan FBP (processing/reconstruction.py:99-107),
     both detector forms, against the reference's own function."""

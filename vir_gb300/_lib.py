@@ -50,6 +50,14 @@ class SiddonRays(ctypes.Structure):
                 ("amax", c_void_p), ("i0", c_void_p), ("iN", c_void_p), ("valid", c_void_p)]
 
 
+class SiddonsGrid(ctypes.Structure):
+    """vg_siddons_grid (include/virgpu.h)."""
+    _fields_ = [("nx", c_int), ("ny", c_int), ("nz", c_int),
+                ("dx", c_float), ("dy", c_float), ("dz", c_float),
+                ("p0", c_float * 3), ("pN", c_float * 3), ("epsilon", c_double),
+                ("epsilon_f", c_float), ("pad", c_int)]
+
+
 class SF2DGeom(ctypes.Structure):
     """vg_sf2d_geom (include/virgpu.h)."""
     _fields_ = [("nx", c_int), ("ny", c_int), ("na", c_int), ("nu", c_int), ("du", c_float),
@@ -90,6 +98,8 @@ _PROTOS = {
     "vg_div_rn_check": [c_void_p, c_void_p, c_size_t, c_void_p, c_void_p],
     "vg_siddon2d_bp_scatter": [c_void_p, c_int, c_int, c_void_p, c_int, c_int, c_double,
                                c_double, c_void_p, c_void_p, c_size_t, c_void_p],
+    "vg_siddons_setup": [ctypes.POINTER(SiddonsGrid), c_int, c_void_p, c_void_p, c_void_p,
+                         c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p],
     "vg_siddons_count": [ctypes.POINTER(SiddonRays), c_void_p, c_void_p, c_void_p],
     "vg_siddons_fill": [ctypes.POINTER(SiddonRays), c_void_p, c_void_p, c_void_p, c_void_p],
     "vg_list_fp": [c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_int, c_void_p],

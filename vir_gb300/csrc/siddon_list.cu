@@ -4,10 +4,10 @@
 // siddons() does its per-ray set-up vectorised (alpha range, first/last
 // plane index with isclose rounding) and spends its time in a per-ray loop
 // that sorts all plane crossings and turns consecutive pairs into (voxel,
-// length) entries.  The host computes the set-up in the reference's own
-// numpy arithmetic (vir_gb300/sys_mat/siddon.py); these kernels run the
-// per-ray loop, one thread per ray, in FP32 with the reference's operation
-// order (every op separately rounded):
+// length) entries.  siddons_setup_kernel computes the set-up, one thread per
+// ray, in the types and operation order of the reference's numpy code; the
+// count and fill kernels run the per-ray loop, one thread per ray, in FP32
+// with the reference's operation order (every op separately rounded):
 //   crossings  (b_i - src)/dST for i in [i0, iN) per axis with dST != 0     (:771-784)
 //   Alpha      sort(bounds, crossings); the first/last element dropped when
 //              isclose (|a - b| <= 1e-8 + 1e-5 |b| in float32) to its neighbour (:787-793)
@@ -239,6 +239,89 @@ __global__ void list_bp_finish_kernel(const double *__restrict__ acc, int nvox,
     x[i] = (float)((accumulate ? (double)x[i] : 0.0) + acc[i]);
 }
 
+// The per-ray set-up of siddons (siddon.py:681-751), each operation in the
+// type numpy gives it and separately rounded: float32 throughout, except the
+// first plane index (nP + 1) - (pN - a dST - src) / dP, which numpy promotes
+// to float64 (an int64 array minus a float32 one); np.isclose(v, round(v),
+// atol=epsilon) compares in v's type with atol and rtol = 1e-5 in that type;
+// np.max / np.min propagate NaN; the ray length sums the squares left to
+// right before the float32 square root, as np.linalg.norm does.
+__device__ __forceinline__ bool f_isclose_atol(float x, float y, float atol) {
+    return (fabsf(__fsub_rn(x, y)) <= __fadd_rn(atol, __fmul_rn(1e-5f, fabsf(y))) && isfinite(y)) ||
+           x == y;
+}
+__device__ __forceinline__ bool d_isclose_atol(double x, double y, double atol) {
+    return (fabs(__dsub_rn(x, y)) <= __dadd_rn(atol, __dmul_rn(1e-5, fabs(y))) && isfinite(y)) ||
+           x == y;
+}
+__device__ __forceinline__ float np_maximum(float a, float b) {
+    return (isnan(a) || isnan(b)) ? __int_as_float(0x7fc00000) : fmaxf(a, b);
+}
+__device__ __forceinline__ float np_minimum(float a, float b) {
+    return (isnan(a) || isnan(b)) ? __int_as_float(0x7fc00000) : fminf(a, b);
+}
+// astype(int32) of an integral value as numpy gives it: values outside the
+// int32 range and NaN become INT_MIN (the x86 conversion's result)
+__device__ __forceinline__ int np_int32(double v) {
+    return (v >= -2147483648.0 && v < 2147483648.0) ? (int)v : (int)0x80000000;
+}
+// g.Xb[i0:iN] slice bound of an int32 index over n + 1 planes
+__device__ __forceinline__ int slice_bound(int i, int L) {
+    const long long j = i < 0 ? (long long)i + L : (long long)i;
+    return (int)(j < 0 ? 0 : (j > L ? L : j));
+}
+
+__global__ void __launch_bounds__(128)
+siddons_setup_kernel(vg_siddons_grid G, int n, const float *__restrict__ src,
+                     const float *__restrict__ trg, float *__restrict__ dst,
+                     float *__restrict__ dist, float *__restrict__ amin_o,
+                     float *__restrict__ amax_o, int *__restrict__ i0_o, int *__restrict__ iN_o,
+                     unsigned char *__restrict__ valid_o) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    const int np[3] = {G.nx, G.ny, G.nz};
+    const float dp[3] = {G.dx, G.dy, G.dz};
+    const float epsf = G.epsilon_f;
+    float s[3], d[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        s[a] = src[3 * (size_t)r + a];
+        d[a] = __fsub_rn(trg[3 * (size_t)r + a], s[a]);
+        dst[3 * (size_t)r + a] = d[a];
+    }
+    dist[r] = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(d[0], d[0]), __fmul_rn(d[1], d[1])),
+                                   __fmul_rn(d[2], d[2])));
+    // alpha range: m_min = [0, per-axis min], m_max = [1, per-axis max]
+    float amin = 0.f, amax = 1.f;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const float den = d[a] != 0.f ? d[a] : epsf;
+        const float a0 = __fdiv_rn(__fsub_rn(G.p0[a], s[a]), den);
+        const float aN = __fdiv_rn(__fsub_rn(G.pN[a], s[a]), den);
+        const bool lt = a0 < aN, gt = a0 > aN;
+        amin = np_maximum(amin, lt ? a0 : (gt ? aN : 0.f));
+        amax = np_minimum(amax, lt ? aN : (gt ? a0 : 1.f));
+    }
+    amin_o[r] = amin;
+    amax_o[r] = amax;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const bool pos = d[a] > 0.f;
+        const float a_lo = pos ? amin : amax, a_hi = pos ? amax : amin;
+        const float t = __fdiv_rn(__fsub_rn(__fsub_rn(G.pN[a], __fmul_rn(a_lo, d[a])), s[a]), dp[a]);
+        const double v0 = __dsub_rn((double)(np[a] + 1), (double)t);
+        const float vN = __fdiv_rn(__fsub_rn(__fadd_rn(s[a], __fmul_rn(a_hi, d[a])), G.p0[a]), dp[a]);
+        const double r0 = rint(v0);
+        const float rN = rintf(vN);
+        const double f0 = d_isclose_atol(v0, r0, G.epsilon) ? r0 : floor(v0);
+        const float fN = f_isclose_atol(vN, rN, epsf) ? rN : ceilf(vN);
+        const int L = np[a] + 1;
+        i0_o[3 * (size_t)r + a] = slice_bound(np_int32(f0), L);
+        iN_o[3 * (size_t)r + a] = slice_bound(np_int32((double)fN), L);
+    }
+    valid_o[r] = (amax > amin) && !f_isclose_atol(amax, amin, epsf);
+}
+
 int check_rays(const vg_siddon_rays *R) {
     VG_REQUIRE(R, "siddons: null ray set");
     VG_REQUIRE(R->n_rays >= 0, "siddons: negative ray count");
@@ -250,6 +333,21 @@ int check_rays(const vg_siddon_rays *R) {
 }
 
 }  // namespace
+
+extern "C" int vg_siddons_setup(const vg_siddons_grid *g, int n, const float *src,
+                                const float *trg, float *dst, float *dist, float *amin,
+                                float *amax, int *i0, int *iN, unsigned char *valid,
+                                void *stream) {
+    VG_REQUIRE(g, "siddons_setup: null grid");
+    VG_REQUIRE(n >= 0, "siddons_setup: negative ray count");
+    VG_REQUIRE(g->nx > 0 && g->ny > 0 && g->nz > 0, "siddons_setup: grid sizes must be positive");
+    VG_REQUIRE(n == 0 || (src && trg && dst && dist && amin && amax && i0 && iN && valid),
+               "siddons_setup: null array");
+    if (n == 0) return VG_OK;
+    siddons_setup_kernel<<<ceil_div(n, 128), 128, 0, as_stream(stream)>>>(
+        *g, n, src, trg, dst, dist, amin, amax, i0, iN, valid);
+    return launch_status("siddons_setup");
+}
 
 extern "C" int vg_siddons_count(const vg_siddon_rays *R, int *counts, int *err, void *stream) {
     int st = check_rays(R);

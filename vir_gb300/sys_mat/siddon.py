@@ -8,12 +8,14 @@ flat=False, epsilon=1e-5)`` returns what the reference returns (siddon.py:636-83
 * otherwise an object array of ``[x_ind, y_ind, z_ind, length]`` per ray;
   rays that miss the grid are ``None``.
 
-The per-ray set-up is vectorised over rays and computed here with the
-reference's own numpy arithmetic (grid planes, alpha range, first/last plane
-index with ``isclose`` rounding: siddon.py:681-751), so it is bit-identical;
-the per-ray loop that sorts the plane crossings and emits (voxel, length)
-entries (:754-826, the hot loop) runs on the GPU (``vg_siddons_count`` /
-``vg_siddons_fill``) in FP32 with the same operation order.
+The grid planes are vir's float32 boundspace planes, built on the host.  The
+per-ray set-up (alpha range, first/last plane index with ``isclose``
+rounding: siddon.py:681-751) runs on the GPU (``vg_siddons_setup``, one
+thread per ray, each operation in the type numpy gives it, so the values are
+bit-identical to the reference's); so does the per-ray loop that sorts the
+plane crossings and emits (voxel, length) entries (:754-826, the hot loop;
+``vg_siddons_count`` / ``vg_siddons_fill``), in FP32 with the same operation
+order.
 """
 from __future__ import annotations
 
@@ -23,7 +25,7 @@ import numpy as np
 import torch
 
 from .. import _core
-from .._lib import SiddonRays, VirGpuError, call
+from .._lib import SiddonRays, SiddonsGrid, VirGpuError, call
 
 
 def _np3(v, dtype):
@@ -38,8 +40,13 @@ def _planes(n, d, c):
     return np.linspace(-n, n, n + 1, dtype=np.float32) * d / 2.0 + c
 
 
-def prepare(src, trg, nPixels=128, dPixels=1.0, origin=0.0, epsilon=1e-5):
-    """Host set-up of siddons: returns (rays shape, grid, per-ray arrays)."""
+def setup_device(src, trg, nPixels=128, dPixels=1.0, origin=0.0, epsilon=1e-5, device=None):
+    """The per-ray set-up of siddons (siddon.py:681-751) on the device
+    (vg_siddons_setup): returns (rays shape, grid, dict of per-ray CUDA
+    tensors src, dst, dist, amin, amax, i0, iN, valid).  The grid planes are
+    vir's float32 boundspace planes, built on the host."""
+    _core.require_cuda()
+    dev = device or torch.device("cuda", torch.cuda.current_device())
     nP = _np3(nPixels, int)
     dP = _np3(dPixels, np.float32)
     oP = _np3(origin, np.float32)
@@ -53,62 +60,31 @@ def prepare(src, trg, nPixels=128, dPixels=1.0, origin=0.0, epsilon=1e-5):
     if src.ndim == 1:
         src = src[np.newaxis, :]
     shape = trg.shape[:-1]
-    p0 = np.array([Xb[0], Yb[0], Zb[0]], dtype=np.float32)
-    pN = np.array([Xb[-1], Yb[-1], Zb[-1]], dtype=np.float32)
-    dST = trg - src
-    distance = np.linalg.norm(dST, axis=-1)
-    # the reference's alpha range (siddon.py:681-751), each element computed as
-    # it computes it; where it evaluates both branches of np.where, only the
-    # selected operand is evaluated here (same values, elementwise)
-    with np.errstate(divide="ignore", invalid="ignore"):
-        den = np.where(dST != 0.0, dST, np.float32(epsilon))
-        alpha0 = (p0 - src) / den
-        alphaN = (pN - src) / den
-    m_min = np.zeros(shape + (4,), dtype=np.float32)
-    m_max = np.ones(shape + (4,), dtype=np.float32)
-    lt, gt = alpha0 < alphaN, alpha0 > alphaN
-    m_min[..., 1:] = np.where(lt, alpha0, np.where(gt, alphaN, np.float32(0)))
-    m_max[..., 1:] = np.where(lt, alphaN, np.where(gt, alpha0, np.float32(1)))
-    amin = np.max(m_min, axis=-1)
-    amax = np.min(m_max, axis=-1)
-    # first / last plane index per axis, from amin / amax by the direction's sign
-    pos = dST > 0.0
-    a_lo = np.where(pos, amin[..., np.newaxis], amax[..., np.newaxis])
-    a_hi = np.where(pos, amax[..., np.newaxis], amin[..., np.newaxis])
-    v0 = (nP + 1) - (pN - a_lo * dST - src) / dP
-    vN = (src + a_hi * dST - p0) / dP
-
-    def r(v, f):
-        rv = np.round(v)
-        return np.where(np.isclose(v, rv, atol=epsilon), rv, f(v)).astype(np.int32)
-
-    with np.errstate(invalid="ignore"):  # axes with dST == 0 carry inf here, unused
-        i0 = r(v0, np.floor)
-        iN = r(vN, np.ceil)
-    # the reference slices g.Xb[i0:iN] (:772): normalise to numpy slice bounds
-    L = (nP + 1).astype(np.int64)
-    sl = lambda i: np.clip(np.where(i < 0, i + L, i), 0, L).astype(np.int32)
-    i0, iN = sl(i0), sl(iN)
-    valid = (amax > amin) & ~np.isclose(amax, amin, atol=epsilon)
     n = int(np.prod(shape))
-    flat = lambda a, k: np.ascontiguousarray(np.broadcast_to(a, shape + (k,)).reshape(n, k))
-    arrays = dict(src=flat(src, 3).astype(np.float32), dst=flat(dST, 3).astype(np.float32),
-                  dist=np.ascontiguousarray(distance.reshape(n), dtype=np.float32),
-                  amin=np.ascontiguousarray(amin.reshape(n), dtype=np.float32),
-                  amax=np.ascontiguousarray(amax.reshape(n), dtype=np.float32),
-                  i0=flat(i0, 3).astype(np.int32), iN=flat(iN, 3).astype(np.int32),
-                  valid=np.ascontiguousarray(valid.reshape(n)).astype(np.uint8))
-    grid = dict(n=nP, d=dP, Xb=Xb, Yb=Yb, Zb=Zb, valid=arrays["valid"])
-    return shape, grid, arrays
+    rows = lambda a: np.ascontiguousarray(np.broadcast_to(a, shape + (3,)).reshape(n, 3))
+    S = torch.from_numpy(rows(src)).to(dev)
+    T = torch.from_numpy(rows(trg)).to(dev)
+    f32 = lambda *s: torch.empty(s, dtype=torch.float32, device=dev)
+    i32 = lambda *s: torch.empty(s, dtype=torch.int32, device=dev)
+    A = dict(src=S, dst=f32(n, 3), dist=f32(n), amin=f32(n), amax=f32(n), i0=i32(n, 3),
+             iN=i32(n, 3), valid=torch.empty(n, dtype=torch.uint8, device=dev))
+    g = SiddonsGrid(int(nP[0]), int(nP[1]), int(nP[2]), float(dP[0]), float(dP[1]), float(dP[2]),
+                    (ctypes.c_float * 3)(Xb[0], Yb[0], Zb[0]),
+                    (ctypes.c_float * 3)(Xb[-1], Yb[-1], Zb[-1]), float(epsilon),
+                    float(np.float32(epsilon)), 0)
+    call("vg_siddons_setup", ctypes.byref(g), n, S.data_ptr(), T.data_ptr(), A["dst"].data_ptr(),
+         A["dist"].data_ptr(), A["amin"].data_ptr(), A["amax"].data_ptr(), A["i0"].data_ptr(),
+         A["iN"].data_ptr(), A["valid"].data_ptr(), _core.stream(dev))
+    grid = dict(n=nP, d=dP, Xb=Xb, Yb=Yb, Zb=Zb)
+    return shape, grid, A
 
 
 def siddons_device(src, trg, nPixels=128, dPixels=1.0, origin=0.0, epsilon=1e-5, device=None):
     """CSR list (ind, len, off) as CUDA tensors, plus the ray shape."""
     _core.require_cuda()
     dev = device or torch.device("cuda", torch.cuda.current_device())
-    shape, grid, A = prepare(src, trg, nPixels, dPixels, origin, epsilon)
+    shape, grid, T = setup_device(src, trg, nPixels, dPixels, origin, epsilon, dev)
     n = int(np.prod(shape))
-    T = {k: torch.from_numpy(v).to(dev) for k, v in A.items()}
     G = {k: torch.from_numpy(np.ascontiguousarray(grid[k], np.float32)).to(dev)
          for k in ("Xb", "Yb", "Zb")}
     nP, dP = grid["n"], grid["d"]
@@ -133,6 +109,7 @@ def siddons_device(src, trg, nPixels=128, dPixels=1.0, origin=0.0, epsilon=1e-5,
     ind = torch.empty(max(total, 1), dtype=torch.int32, device=dev)
     ln = torch.empty(max(total, 1), dtype=torch.float32, device=dev)
     call("vg_siddons_fill", ctypes.byref(R), off32.data_ptr(), ind.data_ptr(), ln.data_ptr(), st)
+    grid["valid"] = T["valid"]
     return ind[:total], ln[:total], off32, shape, grid
 
 
@@ -145,7 +122,7 @@ def siddons(src, trg, nPixels=128, dPixels=1.0, origin=0.0, ravel=False, flat=Fa
     nP = tuple(int(v) for v in grid["n"])
     rays = np.empty(shape, dtype=object)
     flat_rays = rays.reshape(-1)
-    valid = grid["valid"]
+    valid = grid["valid"].cpu().numpy()
     for r in range(flat_rays.size):
         if not valid[r]:
             continue  # a ray that misses the grid stays None, as in the reference
