@@ -286,10 +286,17 @@ def _cpu_port_ms(fp, bp):
             "kind": "port"}
 
 
-def _roof(units, ms, peak):
+def _roof(units, ms, peak, compulsory=None):
+    """Algorithmic-byte roofline (4 B per voxel-view update); with
+    `compulsory` (the launch's unique input + output bytes) also the rate
+    and fraction of those, the true lower bound of its traffic."""
     gbs = 4.0 * units / (ms / 1e3) / 1e9
-    return {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
-            "algorithmic_bytes_per_launch": 4.0 * units}
+    r = {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
+         "algorithmic_bytes_per_launch": 4.0 * units}
+    if compulsory is not None:
+        cg = compulsory / (ms / 1e3) / 1e9
+        r["compulsory"] = {"bytes_per_launch": compulsory, "achieved": cg, "frac": cg / peak}
+    return r
 
 
 def storage_error(probs, dev, n_check=2, iters=50):
@@ -349,6 +356,17 @@ def run_workload(args):
         fp = lambda: f2.siddons_fp_2d(x, angs, 367, 1.0, 1.0)
         bp = lambda: f2.siddons_bp_2d(y, angs, (256, 256), 1.0, 1.0)
         units = 180 * 256 * 256
+        compulsory = 4.0 * (256 * 256 + 180 * 367)  # image + sinogram
+        # intersections (kept segments) of the C1 rays, from the walk's trace mode
+        from vir_gb300 import _core
+        from vir_gb300._lib import call
+        trig = _core.trig_cache.get(angs, None, dev)
+        cnt = torch.empty((180, 367), dtype=torch.int32, device=dev)
+        hsh = torch.empty((180, 367), dtype=torch.int64, device=dev)
+        tln = torch.empty((180, 367), dtype=torch.float64, device=dev)
+        call("vg_siddon2d_trace", 256, 256, _core.ptr(trig), 180, 367, 1.0, 1.0, _core.ptr(cnt),
+             _core.ptr(hsh), _core.ptr(tln), _core.stream(dev))
+        n_isect = int(cnt.sum().item())
         yh = y.cpu().numpy()
         line["cpu_port"] = _cpu_port_ms(lambda: orc_mod().siddons_fp_2d(img, angs, 367, 1.0, 1.0),
                                         lambda: orc_mod().siddons_bp_2d(yh, angs, (256, 256), 1.0, 1.0))
@@ -363,6 +381,7 @@ def run_workload(args):
         fp = lambda: dd.dd_fp_cone_3d(x, angs, nu, nv, 600.0, 1100.0, **kw)
         bp = lambda: dd.dd_bp_cone_3d(y, angs, (n, n, n), 600.0, 1100.0, **kw)
         units = na * n ** 3
+        compulsory = 4.0 * (n ** 3 + na * nu * nv)  # volume + sinogram
     elif wl == "square":
         cases = {"script": (64, 64, 129, 64, 96, 10, 40.0, 72.0,
                             dict(du=1.0, dv=1.0, dsrc_p=0.5, dsrc_z=0.5, su=0.0, sv=32.0,
@@ -745,7 +764,11 @@ def run_workload(args):
     t_fp, t_bp = _event_ms(fp, reps, stream), _event_ms(bp, reps, stream)
     line.update({"kernel_ms": {"fp": t_fp, "bp": t_bp},
                  "fwd_back_gups": 2 * units / ((t_fp + t_bp) / 1e3) / 1e9,
-                 "roofline_fp": _roof(units, t_fp, peak), "roofline_bp": _roof(units, t_bp, peak)})
+                 "roofline_fp": _roof(units, t_fp, peak, compulsory),
+                 "roofline_bp": _roof(units, t_bp, peak, compulsory)})
+    if wl == "c1":
+        line["intersections"] = {"count": n_isect, "per_s_fp": n_isect / (t_fp / 1e3),
+                                 "per_s_bp": n_isect / (t_bp / 1e3)}
     if wl in ("c4", "c5"):
         # the separable-footprint pair (SF-TR) on the same cone geometry
         from vir_gb300.sys_mat import sp
@@ -754,8 +777,8 @@ def run_workload(args):
         s_fp, s_bp = _event_ms(sfp, reps, stream), _event_ms(sbp, reps, stream)
         line["sf"] = {"kernel_ms": {"fp": s_fp, "bp": s_bp},
                       "fwd_back_gups": 2 * units / ((s_fp + s_bp) / 1e3) / 1e9,
-                      "roofline_fp": _roof(units, s_fp, peak),
-                      "roofline_bp": _roof(units, s_bp, peak),
+                      "roofline_fp": _roof(units, s_fp, peak, compulsory),
+                      "roofline_bp": _roof(units, s_bp, peak, compulsory),
                       "note": "BP time includes the l_theta weighting of the sinogram"}
     if wl == "c4":
         from vir_gb300 import autograd as ag
@@ -892,6 +915,7 @@ def main():
     dom_name, t_dom = ("dd2d_bp_kernel<fan>", t_bp) if t_bp >= t_fp else ("dd2d_fp_kernel<fan>", t_fp)
     peak, peak_src = load_peaks()
     achieved = alg_bytes / (t_dom / 1e3) / 1e9
+    comp_bytes = 4.0 * (w["n"] * w["n"] + w["na"] * w["nu"])   # image + sinogram
     traffic = load_traffic()
 
     # ---- the plain FP32 path: one problem, every op its own launch -------
@@ -950,7 +974,12 @@ def main():
                      "frac": achieved / peak, "kernel": dom_name,
                      "traffic": ((traffic or {}).get("kernels", {}).get(dom_name) or {})
                                 .get("dram_bytes_per_launch"),
-                     "algorithmic_bytes_per_launch": alg_bytes, "peak_source": peak_src},
+                     "algorithmic_bytes_per_launch": alg_bytes, "peak_source": peak_src,
+                     "compulsory": {"bytes_per_launch": comp_bytes,
+                                    "achieved": comp_bytes / (t_dom / 1e3) / 1e9,
+                                    "frac": comp_bytes / (t_dom / 1e3) / 1e9 / peak,
+                                    "note": "unique inputs + outputs of the launch (image and "
+                                            "sinogram); L2-resident, so not a DRAM bound"}},
         "e2e": {"value": e2e_val, "unit": "iter/s", "h2d_bytes_per_step": int(y.nbytes),
                 "d2h_bytes_per_step": int(img.nbytes)},
         "gpu_launches": K * U * launches_per_update,      # library kernels per update (2 or 3)

@@ -378,6 +378,7 @@ int vg_dd3d_bp(const vg_dd3d_geom *g, const float *sino, const double *trig,
  * vg_sf3d_bp: vol = its exact adjoint; workspace of
  *   vg_sf3d_workspace_bytes(g) bytes (the l_theta-weighted sinogram of a
  *   chunk of views, at most 256 MiB or one view), 4-byte aligned.
+ * nx and ny at most 2048.
  * The volume must lie inside the source circle (half diagonal below DSO). */
 size_t vg_sf3d_workspace_bytes(const vg_dd3d_geom *g);
 int vg_sf3d_fp(const vg_dd3d_geom *g, const float *vol, const double *trig, float *sino,

@@ -79,7 +79,7 @@ __device__ __forceinline__ SfCol sf_col(const vg_dd3d_geom &g, float c, float s,
     for (int q = 0; q < 4; ++q) {
         const float xx = x + ((q & 1) ? h : -h), yy = y + ((q & 2) ? h : -h);
         const float o = fmaf(c, xx, s * yy), p = fmaf(-s, xx, c * yy);
-        u[q] = g.DSD * p / (g.DSO - o);
+        u[q] = __fdividef(g.DSD * p, g.DSO - o);
     }
     cswap(u[0], u[1]);
     cswap(u[2], u[3]);
@@ -89,9 +89,9 @@ __device__ __forceinline__ SfCol sf_col(const vg_dd3d_geom &g, float c, float s,
     SfCol C;
     C.t0 = u[0]; C.t1 = u[1]; C.t2 = u[2]; C.t3 = u[3];
     const float rx = x - g.DSO * c, ry = y - g.DSO * s;
-    C.lphi = g.d_pix * sqrtf(rx * rx + ry * ry) / fmaxf(fabsf(rx), fabsf(ry));
-    C.mz = g.DSD * g.d_pix / (g.DSO - fmaf(c, x, s * y));
-    C.inv_mz = (g.DSO - fmaf(c, x, s * y)) / (g.DSD * g.d_pix);
+    C.lphi = __fdividef(g.d_pix * sqrtf(rx * rx + ry * ry), fmaxf(fabsf(rx), fabsf(ry)));
+    C.mz = __fdividef(g.DSD * g.d_pix, g.DSO - fmaf(c, x, s * y));
+    C.inv_mz = __fdividef(g.DSO - fmaf(c, x, s * y), g.DSD * g.d_pix);
     return C;
 }
 
@@ -101,14 +101,14 @@ __device__ __forceinline__ float trap_cum(float u, const SfCol &C) {
     const float a = 0.5f * (C.t1 - C.t0);
     if (u <= C.t1) {
         const float e = u - C.t0;
-        return e * e / (2.f * (C.t1 - C.t0));
+        return __fdividef(e * e, 2.f * (C.t1 - C.t0));
     }
     if (u <= C.t2) return a + (u - C.t1);
     const float b = a + (C.t2 - C.t1);
     const float r = 0.5f * (C.t3 - C.t2);
     if (u <= C.t3) {
         const float e = C.t3 - u;
-        return b + r - e * e / (2.f * (C.t3 - C.t2));
+        return b + r - __fdividef(e * e, 2.f * (C.t3 - C.t2));
     }
     return b + r;
 }
@@ -134,6 +134,34 @@ __device__ __forceinline__ float vprofile(const vg_dd3d_geom &g, const float *__
     return acc * inv_dv;
 }
 
+// vprofile for a v cell [va, vb] in slice coordinates s = v / (M d) + nz / 2:
+// the cell meets slices floor(sa) .. floor(sb); when that is at most two
+// slices (the cell no taller than a slice), both are read at once and
+// weighted by their overlaps, else the slices are walked.
+__device__ __forceinline__ float vprofile2(const vg_dd3d_geom &g, const float *__restrict__ col,
+                                           float mz, float inv_mz, float va, float vb, float hz,
+                                           float nzf, float inv_dv) {
+    const float sa = fmaxf(fmaf(va, inv_mz, hz), 0.f), sb = fminf(fmaf(vb, inv_mz, hz), nzf);
+    if (!(sb > sa)) return 0.f;
+    const float fa = floorf(sa);
+    const int z0 = (int)fa;
+    float acc;
+    if (sb <= fa + 2.f) {
+        const float f0 = __ldg(col + z0);                       // z0 < nz since sa < sb <= nz
+        const float f1 = z0 + 1 < g.nz ? __ldg(col + z0 + 1) : 0.f;
+        const float w0 = fminf(sb, fa + 1.f) - sa, w1 = fmaxf(sb - (fa + 1.f), 0.f);
+        acc = fmaf(f0, w0, f1 * w1);
+    } else {
+        acc = 0.f;
+        const int z1 = min((int)floorf(sb), g.nz - 1);
+        for (int z = z0; z <= z1; ++z) {
+            const float ov = fminf(sb, (float)(z + 1)) - fmaxf(sa, (float)z);
+            if (ov > 0.f) acc = fmaf(__ldg(col + z), ov, acc);
+        }
+    }
+    return acc * (mz * inv_dv);
+}
+
 // Fractional pixel index, along the driving axis, of the point of the line
 // at orthogonal coordinate `cen` that projects to u (x, y = (b, cen) when
 // X-driven, else (cen, b)):  b (DSD pd + u od) = u (DSO - oc) - DSD pc.
@@ -141,14 +169,14 @@ __device__ __forceinline__ float unproj_idx(const vg_dd3d_geom &g, float c, floa
                                             float cen, float u, int nd) {
     const float pd = xdrv ? -s : c, od = xdrv ? c : s;
     const float pc = xdrv ? c * cen : -s * cen, oc = xdrv ? s * cen : c * cen;
-    const float b = (u * (g.DSO - oc) - g.DSD * pc) / (g.DSD * pd + u * od);
-    return b / g.d_pix + 0.5f * nd;
+    const float b = __fdividef(u * (g.DSO - oc) - g.DSD * pc, g.DSD * pd + u * od);
+    return __fdividef(b, g.d_pix) + 0.5f * nd;
 }
 
 // ---------------------------------------------------------------------------
 // Forward projection
 // ---------------------------------------------------------------------------
-constexpr int SU = 32, SV = 64, SCMAX = 64, SKMAX = 8;
+constexpr int SU = 32, SV = 64, SCMAX = 64, SKMAX = 8, SLINES = 2048;
 
 // per-line tables, double-buffered by line parity
 struct SfFpTab {
@@ -157,6 +185,8 @@ struct SfFpTab {
     int cf[2][SU], cn[2][SU];  // covering columns (table index, count) per u cell
     float w[2][SU][SKMAX];  // F1 l_phi0 weights of those columns
     float gv[2][SCMAX][SV];
+    int2 kr[SLINES];        // per line: the range [x, y] of columns that can reach the tile
+    float ve[SV + 1];       // the tile's v cell edges
     int wide[2];
 };
 
@@ -208,39 +238,62 @@ sf3d_fp_kernel(vg_dd3d_geom g, const float *__restrict__ vol, const double *__re
     float acc[8], grp[8];
 #pragma unroll
     for (int q = 0; q < 8; ++q) acc[q] = grp[q] = 0.f;
-    int ngrp = 0, nl = 0;
-    if (tid < 2) T.wide[tid] = 0;
-    for (int io = 0; io < no; ++io) {
-        const float cen = vox(g.d_pix, io, no);
-        // columns of this line whose footprint can reach the tile: the map
-        // of the tile's u edges (widened by a cell) on both boundaries of
-        // the line, one column of margin each side
+    int ngrp = 0;
+    if (tid < 2) T.wide[tid] = -1;
+    if (tid <= SV) T.ve[tid] = vedge(g, v0 + tid);
+    const float hz = 0.5f * g.nz, nzf = (float)g.nz;
+    // columns of every line whose footprints can reach the tile, one line per
+    // thread: the map of the tile's u edges (widened by a cell) on both
+    // boundaries of the line, one column of margin each side
+    for (int jo = tid; jo < no; jo += 256) {
         int kA = 0, kB = nd - 1;
         if (!tile_pole) {
-            const float h = 0.5f * g.d_pix;
-            const float a0 = unproj_idx(g, c, s, xdrv, cen - h, TUa - g.du, nd);
-            const float a1 = unproj_idx(g, c, s, xdrv, cen + h, TUa - g.du, nd);
-            const float b0 = unproj_idx(g, c, s, xdrv, cen - h, TUb + g.du, nd);
-            const float b1 = unproj_idx(g, c, s, xdrv, cen + h, TUb + g.du, nd);
-            const float lo = fminf(fminf(a0, a1), fminf(b0, b1)), hi = fmaxf(fmaxf(a0, a1), fmaxf(b0, b1));
+            const float cj = vox(g.d_pix, jo, no), h = 0.5f * g.d_pix;
+            const float a0 = unproj_idx(g, c, s, xdrv, cj - h, TUa - g.du, nd);
+            const float a1 = unproj_idx(g, c, s, xdrv, cj + h, TUa - g.du, nd);
+            const float b0 = unproj_idx(g, c, s, xdrv, cj - h, TUb + g.du, nd);
+            const float b1 = unproj_idx(g, c, s, xdrv, cj + h, TUb + g.du, nd);
+            const float lo = fminf(fminf(a0, a1), fminf(b0, b1));
+            const float hi = fmaxf(fmaxf(a0, a1), fmaxf(b0, b1));
             kA = max((int)floorf(fmaxf(lo, -2.f)) - 1, 0);
             kB = min((int)floorf(fminf(hi, (float)nd + 2.f)) + 1, nd - 1);
         }
-        if (kA > kB) continue;  // block-uniform
+        T.kr[jo] = make_int2(kA, kB);
+    }
+    __syncthreads();
+    // phase 1 of a line: its columns' footprints and z-prefix rows into buffer bb
+    auto phase1 = [&](int io, int bb) {
+        const int2 kr = T.kr[io];
+        const int nk = kr.y - kr.x + 1;
+        if (nk <= SCMAX && tid < nk) {
+            const int k = kr.x + tid;
+            const float cen = vox(g.d_pix, io, no), bx = vox(g.d_pix, k, nd);
+            T.col[bb][tid] = sf_col(g, c, s, xdrv ? bx : cen, xdrv ? cen : bx);
+            const int ix = xdrv ? k : io, iy = xdrv ? io : k;
+            T.off[bb][tid] = (ix * g.ny + iy) * g.nz;
+        }
+    };
+    auto next_line = [&](int io) {
+        do { ++io; } while (io < no && T.kr[io].x > T.kr[io].y);
+        return io;
+    };
+    // One barrier per line: the block builds line io's covering columns,
+    // weights and v profiles from buffer b together with the next line's
+    // footprints into buffer b ^ 1, then after the barrier each cell adds
+    // line io's columns.  Phase 3 of line io reads only phase-2 results of
+    // buffer b, which the block next writes two lines later, after the
+    // following line's barrier; T.wide[b] holds the index of the last wide
+    // line of buffer b (writers only store that index).
+    int io = next_line(-1), b = 0;
+    if (io < no) phase1(io, 0);
+    __syncthreads();
+    for (; io < no; b ^= 1) {
+        const int2 kr = T.kr[io];
+        const int kA = kr.x, kB = kr.y;
         const int nk = kB - kA + 1;
         const bool big = nk > SCMAX;
-        const int b = nl++ & 1;
-        // phase 1: the columns' footprints (buffer b was last read two lines
-        // ago, before the previous line's second barrier)
-        if (!big && tid < nk) {
-            const int k = kA + tid;
-            const float bb = vox(g.d_pix, k, nd);
-            T.col[b][tid] = sf_col(g, c, s, xdrv ? bb : cen, xdrv ? cen : bb);
-            const int ix = xdrv ? k : io, iy = xdrv ? io : k;
-            T.off[b][tid] = (ix * g.ny + iy) * g.nz;
-        }
-        if (tid == 0) T.wide[b] = 0;
-        __syncthreads();
+        const int nxt = next_line(io);
+        if (nxt < no) phase1(nxt, b ^ 1);
         if (!big) {
             // phase 2a: covering columns of each u cell (the footprints move
             // monotonically along the line, so they are consecutive; binary
@@ -268,7 +321,7 @@ sf3d_fp_kernel(vg_dd3d_geom g, const float *__restrict__ vol, const double *__re
                 if (wm == 0) {
                     T.cf[b][wu] = first;
                     T.cn[b][wu] = min(n, SKMAX);
-                    if (n > SKMAX) T.wide[b] = 1;
+                    if (n > SKMAX) T.wide[b] = io;
                 }
                 if (wm < n && wm < SKMAX) T.w[b][wu][wm] = uweight(T.col[b][first + wm], ua, ub, inv_du);
             }
@@ -277,15 +330,15 @@ sf3d_fp_kernel(vg_dd3d_geom g, const float *__restrict__ vol, const double *__re
                 const int t = p / SV, l = p % SV;
                 float gval = 0.f;
                 if (l < nvT)
-                    gval = vprofile(g, vol + T.off[b][t], T.col[b][t].mz, T.col[b][t].inv_mz,
-                                    vedge(g, v0 + l), vedge(g, v0 + l + 1), inv_dv);
+                    gval = vprofile2(g, vol + T.off[b][t], T.col[b][t].mz, T.col[b][t].inv_mz,
+                                     T.ve[l], T.ve[l + 1], hz, nzf, inv_dv);
                 T.gv[b][t][l] = gval;
             }
         }
         __syncthreads();
         // phase 3: each cell adds its covering columns' weighted profiles
         float part[8];
-        if (!big && !T.wide[b]) {
+        if (!big && T.wide[b] != io) {
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
                 const int j = 4 * warp + q;
@@ -322,6 +375,7 @@ sf3d_fp_kernel(vg_dd3d_geom g, const float *__restrict__ vol, const double *__re
             for (int q = 0; q < 8; ++q) { acc[q] += grp[q]; grp[q] = 0.f; }
             ngrp = 0;
         }
+        io = nxt;
     }
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
@@ -502,6 +556,7 @@ int check(const vg_dd3d_geom *g) {
                "sf3d: sizes must be positive");
     VG_REQUIRE(g->na < 65536 && ceil_div(g->nx, BT) < 65536 && ceil_div(g->ny, BT) < 65536 &&
                    ceil_div(g->nu, SU) < 65536, "sf3d: sizes too large");
+    VG_REQUIRE(g->nx <= SLINES && g->ny <= SLINES, "sf3d: nx and ny at most %d", SLINES);
     VG_REQUIRE((double)g->nx * g->ny * g->nz < 2147483648.0, "sf3d: volume above 2^31 voxels");
     VG_REQUIRE(g->du > 0.f && g->dv > 0.f && g->d_pix > 0.f && g->DSO > 0.f && g->DSD > 0.f,
                "sf3d: pitches and distances must be positive");
@@ -523,11 +578,15 @@ size_t chunk_views(const vg_dd3d_geom *g) {
     return n;
 }
 
+size_t bp_ws_bytes(const vg_dd3d_geom *g) {
+    return chunk_views(g) * (size_t)g->nu * g->nv * sizeof(float);
+}
+
 }  // namespace
 
 extern "C" size_t vg_sf3d_workspace_bytes(const vg_dd3d_geom *g) {
     if (check(g)) return 0;
-    return chunk_views(g) * (size_t)g->nu * g->nv * sizeof(float);
+    return bp_ws_bytes(g);
 }
 
 extern "C" int vg_sf3d_fp(const vg_dd3d_geom *g, const float *vol, const double *trig, float *sino,
@@ -546,7 +605,7 @@ extern "C" int vg_sf3d_bp(const vg_dd3d_geom *g, const float *sino, const double
     if (st) return st;
     VG_REQUIRE(sino && trig && vol, "sf3d_bp: null pointer");
     const size_t nch = chunk_views(g);
-    const size_t need = nch * (size_t)g->nu * g->nv * sizeof(float);
+    const size_t need = bp_ws_bytes(g);
     VG_REQUIRE(workspace && workspace_bytes >= need,
                "sf3d_bp: workspace of %zu bytes needed (vg_sf3d_workspace_bytes)", need);
     cudaStream_t s = as_stream(stream);

@@ -92,6 +92,15 @@ def sf_fp_cone_3d(img, ang_arr, nu, nv, DSO, DSD, du=1.0, dv=1.0, su=0.0, sv=0.0
     return _core.to_host_like(sino, img)
 
 
+def _sf3d_workspace(g, dev):
+    """Device workspace of vg_sf3d_workspace_bytes(g) bytes (8-byte aligned)."""
+    L = load()
+    n = int(L.vg_sf3d_workspace_bytes(ctypes.byref(g)))
+    if n == 0:
+        raise VirGpuError("vg_sf3d_workspace_bytes", 1, L.vg_last_error().decode(errors="replace"))
+    return torch.empty((n + 7) // 8, dtype=torch.float64, device=dev)
+
+
 def sf_bp_cone_3d(sino, ang_arr, img_shape, DSO, DSD, du=1.0, dv=1.0, su=0.0, sv=0.0, d_pix=1.0):
     """Exact adjoint of sf_fp_cone_3d: sino (na, nu, nv) -> vol (nx, ny, nz)."""
     dev = _core.device_of(sino)
@@ -103,12 +112,8 @@ def sf_bp_cone_3d(sino, ang_arr, img_shape, DSO, DSD, du=1.0, dv=1.0, su=0.0, sv
     if y.shape[0] != na:
         raise ValueError(f"sino has {y.shape[0]} views, ang_arr {na}")
     g = _g3(img_shape, na, y.shape[1], y.shape[2], du, dv, su, sv, d_pix, DSO, DSD)
-    L = load()
-    n = int(L.vg_sf3d_workspace_bytes(ctypes.byref(g)))
-    if n == 0:
-        raise VirGpuError("vg_sf3d_workspace_bytes", 1, L.vg_last_error().decode(errors="replace"))
-    ws = torch.empty((n + 3) // 4, dtype=torch.float32, device=dev)
+    ws = _sf3d_workspace(g, dev)
     vol = _core.empty(tuple(int(v) for v in img_shape), dev)
     call("vg_sf3d_bp", ctypes.byref(g), _core.ptr(y), _core.ptr(trig), _core.ptr(vol),
-         _core.ptr(ws), ws.numel() * 4, _core.stream(dev))
+         _core.ptr(ws), ws.numel() * 8, _core.stream(dev))
     return _core.to_host_like(vol, sino)
