@@ -67,6 +67,57 @@ def test_sirt_launch_count_without_gpu():
     assert L.vg_dd2d_sirt_launches(ctypes.byref(g)) == 0
 
 
+def test_batch_items_without_gpu():
+    """vg_sirt2d_batch_items (host-only): per problem na * chunks forward
+    projection items (chunks of 192, 384 or 768 bins), na table items and
+    (ny / 64) x (nx / 16) back projection tiles, rounded up; every (problem,
+    item) pair listed once; null buffers, misaligned workspaces and fan
+    detectors reaching the inverse map's pole are refused."""
+    import numpy as np
+    from vir_gb300 import _lib
+    L = _lib.load()
+    geoms = [(128, 128, 90, 192, 0), (256, 200, 101, 384, 1), (512, 512, 720, 768, 1),
+             (1024, 1024, 40, 1536, 0), (100, 300, 7, 450, 0)]
+    P = (_lib.Sirt2DProblem * len(geoms))()
+    for i, (nx, ny, na, nu, fan) in enumerate(geoms):
+        d = 1.0
+        g = _lib.DD2DGeom(nx, ny, na, nu, 1.0, 0.0, d, 2.0 * nx * d if fan else 0.0,
+                          4.0 * nx * d if fan else 0.0, fan, 0)
+        P[i] = _lib.Sirt2DProblem(g, 16, 16, 16, 16, 16, 16, 16, 256, 1.0, 0)  # never dereferenced
+    n = len(geoms)
+    nf, nt, nb = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    assert L.vg_sirt2d_batch_items(P, n, None, ctypes.byref(nf), None, ctypes.byref(nt), None,
+                                   ctypes.byref(nb)) == 0
+    chunk = lambda nu: 192 if nu <= 192 else (384 if nu <= 384 else 768)
+    ef = sum(na * -(-nu // chunk(nu)) for _, _, na, nu, _ in geoms)
+    et = sum(na for _, _, na, _, _ in geoms)
+    eb = sum(-(-ny // 64) * -(-nx // 16) for nx, ny, _, _, _ in geoms)
+    assert (nf.value, nt.value, nb.value) == (ef, et, eb)
+    fi = np.empty((ef, 2), np.int32)
+    ti = np.empty((et, 2), np.int32)
+    bi = np.empty((eb, 2), np.int32)
+    assert L.vg_sirt2d_batch_items(P, n, fi.ctypes.data, ctypes.byref(nf), ti.ctypes.data,
+                                   ctypes.byref(nt), bi.ctypes.data, ctypes.byref(nb)) == 0
+    for items, per in ((fi, lambda q: geoms[q][2] * -(-geoms[q][3] // chunk(geoms[q][3]))),
+                       (ti, lambda q: geoms[q][2]),
+                       (bi, lambda q: -(-geoms[q][1] // 64) * -(-geoms[q][0] // 16))):
+        pairs = set(map(tuple, items.tolist()))
+        assert len(pairs) == len(items)
+        assert pairs == {(q, k) for q in range(n) for k in range(per(q))}
+    bad = (_lib.Sirt2DProblem * 1)(P[0])
+    bad[0].workspace = 128  # not 256-byte aligned
+    assert L.vg_sirt2d_batch_items(bad, 1, None, ctypes.byref(nf), None, ctypes.byref(nt), None,
+                                   ctypes.byref(nb)) != 0
+    bad[0] = P[0]
+    bad[0].y = None
+    assert L.vg_sirt2d_batch_items(bad, 1, None, ctypes.byref(nf), None, ctypes.byref(nt), None,
+                                   ctypes.byref(nb)) != 0
+    bad[0] = P[1]
+    bad[0].g.DSD = 0.2 * bad[0].g.nu  # the detector reaches beyond DSD: the pole
+    assert L.vg_sirt2d_batch_items(bad, 1, None, ctypes.byref(nf), None, ctypes.byref(nt), None,
+                                   ctypes.byref(nb)) != 0
+
+
 def test_drop_in_table_resolves_and_installs():
     """Every vir function named in the drop-in table exists here, and
     install_into replaces it in an imported vir package (a stand-in tree of
