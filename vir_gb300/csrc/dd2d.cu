@@ -55,6 +55,7 @@
 #ifndef VG_FP_MAGIC
 #define VG_FP_MAGIC 1
 #endif
+
 #ifndef VG_BP_MAGIC
 #define VG_BP_MAGIC 1
 #endif
@@ -95,6 +96,11 @@ template <bool COH = false> __device__ __forceinline__ void ld8(const __nv_bfloa
         o[2 * i + 1] = __uint_as_float(w[i] & 0xffff0000u);
     }
 }
+
+// A compile-time bool usable in device code (selects a copy of a generic lambda).
+template <bool B> struct BoolC {
+    __host__ __device__ constexpr operator bool() const { return B; }
+};
 
 struct ViewGeo {
     float pd, od;  // driving-edge coefficients: p = pd*b + cp, o = od*b + co
@@ -198,12 +204,18 @@ constexpr FpVariant FP_VARIANTS[] = {{8, 6}, {8, 12}, {8, 24}, {4, 24}, {4, 48},
 constexpr int FP_NVARIANTS = sizeof(FP_VARIANTS) / sizeof(FP_VARIANTS[0]);
 
 // Line entries are (G_k, V_k) with G_k = S_k - V_k P_k, so F(U) = G_k + V_k U
-// for U in pixel k.  Entry slot pad_idx(k + 1) holds edge/pixel k; slot 0 is
-// a zero sentinel for U before the line's first edge (F = 0), and the closing
-// edge nd carries (S_nd, 0).  One spare slot every 16 keeps the scan's lanes
-// (16 entries apart) on different shared-memory banks.
-__host__ __device__ __forceinline__ int pad_idx(int m) { return m + (m >> 4); }
-__host__ __device__ inline int fp_line_entries(int nd) { return pad_idx(nd + 1) + 1; }
+// for U in pixel k.  Pixel p in -1 .. nd + 1 sits in slot fp_slot(p): p = -1 is
+// a zero sentinel for U before the line's first edge (F = 0), p = nd and
+// nd + 1 carry the line total (S_nd, 0).  One spare slot every 16 pixels keeps
+// the scan's lanes (8 pixels apart) on different shared-memory banks; the
+// spare falls between segments, so a lane's 8 pixels (p = 8 m ...) take
+// consecutive slots.
+__host__ __device__ __forceinline__ int fp_slot(int p) { return p + 1 + ((p + 16) >> 4); }
+__host__ __device__ inline int fp_line_entries(int nd) { return fp_slot(nd + 1) + 1; }
+// The walk finds pixel p as the bit pattern b = FP_MAGIC_BITS + 16 + p of a
+// round-down FMA onto 1.5 * 2^23 + 15; b + (b >> 4) = fp_slot(p) + FP_SLOT_BIAS.
+constexpr unsigned FP_MAGIC_BITS = 0x4B400000u;  // 1.5 * 2^23, a multiple of 16
+constexpr unsigned FP_SLOT_BIAS = FP_MAGIC_BITS + (FP_MAGIC_BITS >> 4) + 15u;
 
 struct BpWork {
     float2 *ts;  // [na][nu + 1]: (T_j - j du sino_j, du sino_j)
@@ -321,10 +333,16 @@ __device__ __forceinline__ void fp_block(const vg_dd2d_geom &g, int ia, int chun
         guard = Up >= fminf(Ua, Ub) && Up <= fmaxf(Ua, Ub);
     }
 
-    // line-independent factor of the inverse map at every bin edge:
-    // sweep index s(U) = (U a_l - b_l) C(U) + nd/2
+    // Line-independent factor of the inverse map at every bin edge, scaled
+    // for the slot lookup: with the sweep index s(U) = (U a_l - b_l) C(U) + nd/2,
+    // the walk forms t = sat((s + 1) / (nd + 2)) = sat((U a_l - b_l) C' + h')
+    // with C' = C / (nd + 2), h' = (nd/2 + 1) / (nd + 2); floor(t (nd + 2)) - 1
+    // is the pixel under U, clamped to -1 .. nd + 1 by the saturation (NaN
+    // gives 0, the sentinel).
+    const float ndp2 = (float)(nd + 2);
+    const float hq = (half + 1.f) / ndp2;
     {
-        const float sig = (rev ? -1.f : 1.f) / g.d_pix;
+        const float sig = (rev ? -1.f : 1.f) / (g.d_pix * ndp2);
         for (int e = threadIdx.x; e < FP_BINS + 32; e += FP_WARPS * 32) {
             const float U = det_edge(g, jbase + min(e, nb));
             UC[e] = make_float2(U, FAN ? sig / (g.DSD * v.pd + U * v.od) : sig / v.pd);
@@ -337,29 +355,29 @@ __device__ __forceinline__ void fp_block(const vg_dd2d_geom &g, int ia, int chun
     for (int i = 0; i < FP_MAXB; ++i) acc[i] = 0.f;
 
     // Stages line io into buffer Eb: (G, V) per pixel, the sentinel and the
-    // closing edge; returns the line's inverse-map coefficients (la, lb) and,
-    // for the guard, its first and last projected edges (Pf, Pl).
-    auto stage = [&](int io, float2 *Eb, float &la, float &lb, float &Pf, float &Pl) {
+    // closing edges; returns the line's inverse-map coefficients (la, lb) and,
+    // for the guard, its first and last projected edges (Pf <= Pl).  The sweep
+    // direction RVC is a compile-time constant in each of the two copies.
+    auto stage = [&](auto RVC, int io, float2 *Eb, float &la, float &lb, float &Pf, float &Pl) {
+        const bool RV = RVC;
         const Line Lg = line_geo<FAN>(g, v, centre_coord(g.d_pix, io, no));
         la = FAN ? g.DSO - Lg.co : 1.f;       // inverse map numerator U la - lb
         lb = FAN ? g.DSD * Lg.cp : Lg.cp;
-        Pf = 0.f;
-        Pl = 0.f;
-        if (guard) {
-            Pf = proj<FAN>(g, v, Lg.cp, Lg.co, edge_coord(g.d_pix, rev ? nd : 0, nd));
-            Pl = proj<FAN>(g, v, Lg.cp, Lg.co, edge_coord(g.d_pix, rev ? 0 : nd, nd));
+        if (GUARD) {
+            Pf = proj<FAN>(g, v, Lg.cp, Lg.co, edge_coord(g.d_pix, RV ? nd : 0, nd));
+            Pl = proj<FAN>(g, v, Lg.cp, Lg.co, edge_coord(g.d_pix, RV ? 0 : nd, nd));
         }
         const TX *row = base + (size_t)io * nd;
         // lanes own FP_SEG consecutive pixels (edge coordinate b0 + i db along
         // a lane's segment); along the segment the projection's numerator and
-        // denominator are affine in the edge number i: P_i = (n0 + i dn) / (d0 + i dd)
-        const float db = rev ? -g.d_pix : g.d_pix;
+        // denominator are affine in the edge number i: P_i = (n0 + i dn) / (d0 + i dd).
+        const float db = RV ? -g.d_pix : g.d_pix;
         const float dn = (FAN ? g.DSD : 1.f) * v.pd * db;
         const float dd = -v.od * db;
         float carry = 0.f;
         for (int r0 = 0; r0 < nd; r0 += 32 * FP_SEG) {
             const int m0 = r0 + lane * FP_SEG;
-            const float b0 = edge_coord(g.d_pix, rev ? nd - m0 : m0, nd);
+            const float b0 = edge_coord(g.d_pix, RV ? nd - m0 : m0, nd);
             const float n0 = (FAN ? g.DSD : 1.f) * fmaf(v.pd, b0, Lg.cp);
             const float d0 = g.DSO - fmaf(v.od, b0, Lg.co);
             float Pv[FP_SEG + 1], q[FP_SEG];
@@ -367,7 +385,9 @@ __device__ __forceinline__ void fp_block(const vg_dd2d_geom &g, int ia, int chun
             for (int i = 0; i <= FP_SEG; ++i) {
                 const float num = fmaf((float)i, dn, n0);
 #if VG_FAST_DIV
-                Pv[i] = FAN ? __fdividef(num, fmaf((float)i, dd, d0)) : num;
+                float r;  // approximate reciprocal (as __fdividef, without its range scaling)
+                asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(fmaf((float)i, dd, d0)));
+                Pv[i] = FAN ? num * r : num;
 #else
                 Pv[i] = FAN ? num / fmaf((float)i, dd, d0) : num;
 #endif
@@ -378,18 +398,22 @@ __device__ __forceinline__ void fp_block(const vg_dd2d_geom &g, int ia, int chun
             if (vec_rows && m0 + FP_SEG <= nd) {
                 static_assert(FP_SEG == 8, "segments of 8 pixels (one 16-byte load of bfloat16)");
                 float raw[FP_SEG];
-                ld8<COH>(row + (rev ? nd - FP_SEG - m0 : m0), raw);
+                ld8<COH>(row + (RV ? nd - FP_SEG - m0 : m0), raw);
 #pragma unroll
-                for (int i = 0; i < FP_SEG; ++i) q[i] = (rev ? raw[FP_SEG - 1 - i] : raw[i]) * Lg.scl;
+                for (int i = 0; i < FP_SEG; ++i) q[i] = (RV ? raw[FP_SEG - 1 - i] : raw[i]) * Lg.scl;
             } else {
-                const TX *px = row + (rev ? nd - 1 - m0 : m0);
-                const int step = rev ? -1 : 1;
+                const TX *px = row + (RV ? nd - 1 - m0 : m0);
+                const int step = RV ? -1 : 1;
 #pragma unroll
                 for (int i = 0; i < FP_SEG; ++i)
                     q[i] = (m0 + i < nd) ? ldf<COH>(px + i * step) * Lg.scl : 0.f;
             }
+            float D[FP_SEG];
 #pragma unroll
-            for (int i = 0; i < FP_SEG; ++i) tot = fmaf(q[i], Pv[i + 1] - Pv[i], tot);
+            for (int i = 0; i < FP_SEG; ++i) {
+                D[i] = Pv[i + 1] - Pv[i];
+                tot = fmaf(q[i], D[i], tot);
+            }
             float inc = tot;
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
@@ -399,35 +423,43 @@ __device__ __forceinline__ void fp_block(const vg_dd2d_geom &g, int ia, int chun
             float run = carry + inc - tot;
             carry += __shfl_sync(0xffffffffu, inc, 31);
             const int lim = nd - m0;  // pixel entries m0 + i with i < lim exist
+            float2 *seg = Eb + fp_slot(m0);  // the segment's slots are consecutive
+            if (lim >= FP_SEG) {
 #pragma unroll
-            for (int i = 0; i < FP_SEG; ++i) {
-                if (i < lim) Eb[pad_idx(m0 + i + 1)] = make_float2(fmaf(-q[i], Pv[i], run), q[i]);
-                run = fmaf(q[i], Pv[i + 1] - Pv[i], run);
+                for (int i = 0; i < FP_SEG; ++i) {
+                    seg[i] = make_float2(fmaf(-q[i], Pv[i], run), q[i]);
+                    run = fmaf(q[i], D[i], run);
+                }
+            } else {
+#pragma unroll
+                for (int i = 0; i < FP_SEG; ++i) {
+                    if (i < lim) seg[i] = make_float2(fmaf(-q[i], Pv[i], run), q[i]);
+                    run = fmaf(q[i], D[i], run);
+                }
             }
         }
-        // the sentinel before the first edge and the closing edge nd (line total)
+        // the sentinel before the first edge and the closing edges (line total)
         if (lane == 0) {
-            Eb[0] = make_float2(0.f, 0.f);
-            Eb[pad_idx(nd + 1)] = make_float2(carry, 0.f);
+            Eb[fp_slot(-1)] = make_float2(0.f, 0.f);
+            Eb[fp_slot(nd)] = make_float2(carry, 0.f);
+            Eb[fp_slot(nd + 1)] = make_float2(carry, 0.f);
         }
     };
 
-    // F of a staged line at detector edge (U, C(U))
-    auto F = [&](const float2 *Eb, float la, float lb, float Pf, float Pl, float2 uc) {
-        float sidx = fmaf(fmaf(uc.x, la, -lb), uc.y, half);
-        if (guard) sidx = uc.x <= Pf ? -1.f : (uc.x >= Pl ? (float)nd : sidx);
-        // slot of pixel floor(sidx): sentinel below the line, closing edge
-        // above (the conversion saturates, so the clamp also bounds +-inf)
-#if VG_FP_MAGIC
-        // floor from the bit pattern of a round-down add of 1.5 * 2^23, clamped
-        // in the integer domain (NaN and +-inf land on a sentinel)
-        const int kb = __float_as_int(__fadd_rd(sidx, 12582912.0f));
-        const int k = min(max(kb, 0x4B400000 - 1), 0x4B400000 + nd) - (0x4B400000 - 1);
-#else
-        const int k = min(max(__float2int_rd(sidx), -1), nd) + 1;
-#endif
-        const float2 t = Eb[pad_idx(k)];
-        return fmaf(t.y, uc.x, t.x);
+    // F of a staged line (shared address eb of its slot 0) at detector edge
+    // (U, C'(U)): the slot comes from the bit pattern of a round-down FMA of t
+    // onto 1.5 * 2^23 + 15 (FP_SLOT_BIAS), without clamps or conversions.
+    const unsigned eb = (unsigned)__cvta_generic_to_shared(E) - 8u * FP_SLOT_BIAS;
+    auto F = [&](float la, float lb, float Pf, float Pl, float2 uc) {
+        float t;
+        asm("fma.rn.sat.f32 %0, %1, %2, %3;" : "=f"(t) : "f"(fmaf(uc.x, la, -lb)), "f"(uc.y), "f"(hq));
+        if (guard) t = uc.x <= Pf ? 0.f : (uc.x >= Pl ? 1.f : t);
+        const unsigned b = __float_as_uint(__fmaf_rd(t, ndp2, 12582927.0f));
+        float2 e;
+        asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];"
+                     : "=f"(e.x), "=f"(e.y)
+                     : "r"(eb + 8u * (b + (b >> 4))));
+        return fmaf(e.y, uc.x, e.x);
     };
 
     // Each warp stages its lines io = warp, warp + FP_WARPS, ... one at a
@@ -437,15 +469,16 @@ __device__ __forceinline__ void fp_block(const vg_dd2d_geom &g, int ia, int chun
     // rotation of (lane 0 ? F(edge i) : F(edge i - 1)).
     const int src = (lane + 1) & 31;
     for (int io = warp; io < no; io += FP_WARPS) {
-        float la, lb, Pf, Pl;
+        float la, lb, Pf = 0.f, Pl = 0.f;
         __syncwarp();  // previous line's reads are done
-        stage(io, E, la, lb, Pf, Pl);
+        if (rev) stage(BoolC<true>{}, io, E, la, lb, Pf, Pl);
+        else stage(BoolC<false>{}, io, E, la, lb, Pf, Pl);
         __syncwarp();
         float f_prev = 0.f;
 #pragma unroll
         for (int i = 0; i <= FP_MAXB; ++i) {
             const float2 uc = UC[lane + 32 * i];  // edges past nb repeat the last one
-            const float f_new = F(E, la, lb, Pf, Pl, uc);
+            const float f_new = F(la, lb, Pf, Pl, uc);
             if (i > 0) {
                 const float r = __shfl_sync(0xffffffffu, lane == 0 ? f_new : f_prev, src);
                 acc[i - 1] += r - f_prev;
@@ -492,7 +525,7 @@ dd2d_fp_kernel(vg_dd2d_geom g, const float *__restrict__ img, const float *__res
                const double *__restrict__ trig, float *__restrict__ out, int mode,
                const float *__restrict__ y, const float *__restrict__ inv_w, BpWork pw) {
     extern __shared__ float2 smem2[];
-    __shared__ float2 UC[32 * FP_MAXB + 32];  // per bin edge (U, C(U)); entries past nb repeat nb
+    __shared__ float2 UC[32 * FP_MAXB + 32];  // per bin edge (U, C'(U)); entries past nb repeat nb
     fp_block<FAN, FP_WARPS, FP_MAXB, GUARD, float, float>(g, blockIdx.y, blockIdx.x, img, imgT, trig,
                                                            out, mode, y, inv_w, pw, smem2, UC);
 }
@@ -717,6 +750,9 @@ int launch_fp_t(const vg_dd2d_geom *g, const float *img, const float *imgT, cons
     if (smem > 48 * 1024 && smem > attr[guard]) {
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)smem);
+        if (e == cudaSuccess)  // the largest carveout, so that the tile's blocks per SM fit
+            e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                     (int)cudaSharedmemCarveoutMaxShared);
         if (e != cudaSuccess) return cuda_status(e, "dd2d_fp: shared memory attribute");
         attr[guard] = smem;
     }
