@@ -456,9 +456,13 @@ typedef struct {
 int vg_rd_fp(const vg_ray_geom *g, const float *img, const double *trig,
              float *sino, void *stream);
 
-/* aw_bp_par_2d / aw_bp_fan_2d / aw_bp_cone_3d (rd.py:461, 556, 665):
- * scatter along each ray (float atomics), scaled img / na / d_pix^2 * du
- * (2D) or img / na * du * dv (cone). */
+/* aw_bp_par_2d / aw_bp_fan_2d / aw_bp_cone_3d (rd.py:461, 556, 665),
+ * scaled img / na / d_pix^2 * du (2D) or img / na * du * dv (cone).  The 2D
+ * Amanatides-Woo back projection gathers, per pixel, s times the chord of
+ * every ray crossing it (deterministic; the walk's segment lengths, with
+ * rays within 1e-6 of an axis kept in the row or column they enter); the
+ * Joseph and cone back projections scatter along each ray (float atomics),
+ * as rd.py does. */
 int vg_rd_bp(const vg_ray_geom *g, const float *sino, const double *trig,
              float *img, void *stream);
 

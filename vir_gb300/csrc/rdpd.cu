@@ -7,9 +7,11 @@
 // (cos, sin) (rd.py:490-499); fan/cone rays run from the source
 // DSO (cos, sin, 0) to the detector point -(DSD - DSO)(cos, sin) +
 // u (-sin, cos) + v z (rd.py:584-603, 701-730); u = du (iu - (nu/2 - 0.5) +
-// su), v the same with nv.  The forward projection gathers along the ray;
-// the back projection (vir's own scatter, rd.py:152-176, 357-447) adds with
-// float atomics, so its summation order is not fixed.  Two defects of the
+// su), v the same with nv.  The forward projection gathers along the ray.
+// The 2D Amanatides-Woo back projection is a gather over the rays crossing
+// each pixel (aw_bp2d_gather, deterministic); the Joseph and cone back
+// projections follow vir's own scatter (rd.py:152-176, 357-447) with float
+// atomics, so their summation order is not fixed.  Two defects of the
 // reference are not reproduced: a ray parallel to an axis is clipped to
 // the slab it lies in (the reference's _intersect_bounding never clips
 // it, rd.py:52-64, so rays beside the image walk its edge row), and the
@@ -334,6 +336,236 @@ rd_kernel(vg_ray_geom g, const double *__restrict__ trig, const float *__restric
         if (DIM == 3 && !JOSEPH) val *= g.DSD / sqrtf(g.DSD * g.DSD + u * u + v * v);  // rd.py:782
         out[k] = val;
     }
+}
+
+// ---- 2D Amanatides-Woo back projection in gather form ----------------------
+//
+// The walk's back projection adds s * (t_next - t) to each pixel a ray
+// crosses (rd.py:152-176): the length of the ray's chord through the pixel.
+// Here a thread owns a 2 x 2 pixel patch and, for every view, sums s times
+// the chord of each ray whose detector coordinate falls in the patch's
+// shadow (about four rays at 2x magnification and 0.75 bins per pixel): no
+// atomics, a fixed summation order.  A chord is the overlap of the ray's
+// parameter intervals between the pixel's x planes and between its y planes,
+// t_k = A + k B per axis with (A, B) a function of the ray alone, so that
+// neighbouring pixels see bit-identical plane crossings and a ray's chords
+// telescope as the walk's segments do.  A ray the walk takes as parallel to
+// an axis (|h| <= 1e-6, rd.py:58-64, 99-109) never leaves the row or column
+// it enters in; those rays (|h| <= 1e-5, a superset) take the walk's own
+// set-up (make_ray, slab, the entry index) and are given that row or column.
+#ifndef VG_AWG_VS
+#define VG_AWG_VS 4
+#endif
+constexpr int AWG_VS = VG_AWG_VS;              // threads sharing a patch's views
+constexpr int AWG_TY = 32;                     // patches along y
+constexpr int AWG_TX = 8 / AWG_VS;             // patches along x
+constexpr int AWG_VC = 128;  // views staged per chunk
+constexpr float AWG_NEAR = 1e-5f;
+
+// Chords of the patch's 4 pixels from the x and y plane parameters (3 each):
+// pixel (i, j) spans [tx_i, tx_i+1] and [ty_j, ty_j+1] in either order.
+__device__ __forceinline__ void awg_chords(const float *tx, const float *ty, float w,
+                                           float (&acc)[2][2]) {
+    float ix0[2], ix1[2], iy0[2], iy1[2];
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+        ix0[i] = fminf(tx[i], tx[i + 1]);
+        ix1[i] = fmaxf(tx[i], tx[i + 1]);
+        iy0[i] = fminf(ty[i], ty[i + 1]);
+        iy1[i] = fmaxf(ty[i], ty[i + 1]);
+    }
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+            const float len = fminf(ix1[i], iy1[j]) - fmaxf(ix0[i], iy0[j]);
+            acc[i][j] = fmaf(w, fmaxf(len, 0.f), acc[i][j]);
+        }
+}
+
+// A ray within AWG_NEAR of an axis: the walk's own set-up.  Along an axis
+// with |h| > 1e-6 the pixel's planes bound the chord as above (t with the
+// unit direction); along the other the ray keeps the entry index the walk
+// computes (rd.py:67-74), and only that row or column receives it.  The
+// chord is clipped to the walk's [t_entry, t_exit].
+__device__ void awg_near(const vg_ray_geom &g, float c, float s, float u, int ix, int iy, float w,
+                         float (&acc)[2][2]) {
+    Ray R;
+    make_ray(g, c, s, u, 0.f, R);
+    const int n[2] = {g.nx, g.ny};
+    const int k0[2] = {ix, iy};
+    float lo[2], hi[2], c0[2], te = -INFINITY, tx = INFINITY;
+#pragma unroll
+    for (int a = 0; a < 2; ++a) {
+        float t0, t1;
+        bounds1(n[a], g.d_pix, lo[a], hi[a], c0[a]);
+        slab(R.o[a], R.h[a], lo[a], hi[a], t0, t1);
+        te = fmaxf(te, t0);
+        tx = fminf(tx, t1);
+    }
+    if (!(tx > te)) return;  // the walk does not enter the image
+    float in[2][2], out[2][2];  // [axis][pixel offset]: the pixel's t interval along the axis
+#pragma unroll
+    for (int a = 0; a < 2; ++a) {
+        if (fabsf(R.h[a]) > RD_EPS) {
+            float tp[3];
+#pragma unroll
+            for (int q = 0; q < 3; ++q) tp[q] = (lo[a] + (float)(k0[a] + q) * g.d_pix - R.o[a]) / R.h[a];
+#pragma unroll
+            for (int i = 0; i < 2; ++i) {
+                in[a][i] = fminf(tp[i], tp[i + 1]);
+                out[a][i] = fmaxf(tp[i], tp[i + 1]);
+            }
+        } else {
+            float r = fminf(fmaxf(R.o[a] + te * R.h[a], lo[a] + RD_EPS), hi[a] - RD_EPS);
+            const int ir = min(max((int)floorf((r - lo[a]) / g.d_pix), 0), n[a] - 1);
+#pragma unroll
+            for (int i = 0; i < 2; ++i) {
+                const bool on = k0[a] + i == ir;
+                in[a][i] = on ? -INFINITY : INFINITY;
+                out[a][i] = on ? INFINITY : -INFINITY;
+            }
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+            const float len = fminf(fminf(out[0][i], out[1][j]), tx) - fmaxf(fmaxf(in[0][i], in[1][j]), te);
+            if (len > 0.f) acc[i][j] = fmaf(w, len, acc[i][j]);
+        }
+}
+
+__device__ __forceinline__ float awg_rcp(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+// One block: AWG_TY x AWG_TX patches (2 AWG_TY x 2 AWG_TX pixels), each
+// patch's views split over AWG_VS threads whose sums are added in a fixed
+// order at the end.  Per view the block stages the view's constants: fan
+// (c, s, -DSD c, -DSD s | lox - DSO c, loy - DSO s); parallel (c, s, d/c, d/s |
+// s/c, lox/c, -c/s, loy/s: the plane parameters of the view's common direction).
+template <bool FAN>
+__global__ void __launch_bounds__(AWG_TY * AWG_TX * AWG_VS)
+aw_bp2d_gather(vg_ray_geom g, const double *__restrict__ trig, const float *__restrict__ sino,
+               float *__restrict__ img, float sc) {
+    __shared__ float4 V1[AWG_VC], V2[AWG_VC];
+    __shared__ float red[AWG_VS - 1][AWG_TY * AWG_TX][4];
+    const int tid = threadIdx.x;
+    const int pt = tid % (AWG_TY * AWG_TX), part = tid / (AWG_TY * AWG_TX);
+    const int iy = blockIdx.x * (2 * AWG_TY) + 2 * (pt % AWG_TY);  // patch origin
+    const int ix = blockIdx.y * (2 * AWG_TX) + 2 * (pt / AWG_TY);
+    const bool inside = ix < g.nx && iy < g.ny;
+    const float d = g.d_pix;
+    float lox, hix, c0x, loy, hiy, c0y;
+    bounds1(g.nx, d, lox, hix, c0x);
+    bounds1(g.ny, d, loy, hiy, c0y);
+    // the patch's planes x_k = lo + k d, k = ix .. ix + 2 (the walk's grid)
+    const float kx = (float)ix, ky = (float)iy;
+    const float px0 = lox + kx * d, py0 = loy + ky * d;  // patch corner
+    const float uoff = (float)g.nu / 2.f - 0.5f - g.su;    // u = du (iu - uoff)
+    const float rdu = 1.f / g.du;
+    float acc[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
+    for (int a0 = 0; a0 < g.na; a0 += AWG_VC) {
+        const int nv = min(AWG_VC, g.na - a0);
+        __syncthreads();
+        for (int k = tid; k < nv; k += AWG_TY * AWG_TX * AWG_VS) {
+            const float c = (float)__ldg(trig + 2 * (a0 + k)), s = (float)__ldg(trig + 2 * (a0 + k) + 1);
+            if (FAN) {
+                V1[k] = make_float4(c, s, -g.DSD * c, -g.DSD * s);
+                V2[k] = make_float4(lox - g.DSO * c, loy - g.DSO * s, 0.f, 0.f);
+            } else {
+                // ray o = u (-s, c), h = (c, s): A_x = (lox + u s) / c, B_x = d / c
+                const float rc = awg_rcp(c), rs = awg_rcp(s);
+                V1[k] = make_float4(c, s, d * rc, d * rs);
+                V2[k] = make_float4(s * rc, lox * rc, -c * rs, loy * rs);  // A = fma(u, .x, .y) ...
+            }
+        }
+        __syncthreads();
+        if (!inside) continue;
+        for (int vi = part; vi < nv; vi += AWG_VS) {
+            const float4 q = V1[vi], q2 = V2[vi];
+            const float c = q.x, s = q.y;
+            const float *row = sino + (size_t)(a0 + vi) * g.nu;
+            // the patch's shadow on the detector, widened by a hundredth of a bin
+            float umin, umax;
+            {
+                const float a00 = fmaf(px0, c, py0 * s), b00 = fmaf(py0, c, -px0 * s);
+                const float dax = 2.f * d * c, day = 2.f * d * s;  // corner steps of a, b
+                float us[4];
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const float ka = (k & 1) ? 1.f : 0.f, kb = (k & 2) ? 1.f : 0.f;
+                    const float aa = fmaf(kb, day, fmaf(ka, dax, a00));
+                    const float bb = fmaf(kb, dax, fmaf(ka, -day, b00));
+                    us[k] = FAN ? g.DSD * bb * awg_rcp(g.DSO - aa) : bb;
+                }
+                umin = fminf(fminf(us[0], us[1]), fminf(us[2], us[3]));
+                umax = fmaxf(fmaxf(us[0], us[1]), fmaxf(us[2], us[3]));
+            }
+            const int ja = max((int)ceilf(fmaf(umin, rdu, uoff) - 0.01f), 0);
+            const int jb = min((int)floorf(fmaf(umax, rdu, uoff) + 0.01f), g.nu - 1);
+            if (!FAN && (fabsf(c) <= AWG_NEAR || fabsf(s) <= AWG_NEAR)) {  // taken as axis-parallel
+                for (int iu = ja; iu <= jb; ++iu) {
+                    const float u = g.du * ((float)iu - ((float)g.nu / 2.f - 0.5f) + g.su);
+                    awg_near(g, c, s, u, ix, iy, __ldg(row + iu), acc);
+                }
+                continue;
+            }
+            for (int iu = ja; iu <= jb; ++iu) {
+                const float sv = __ldg(row + iu);
+                const float u = g.du * ((float)iu - ((float)g.nu / 2.f - 0.5f) + g.su);
+                float Ax, Bx, Ay, By, w;
+                if (FAN) {
+                    // direction (vx, vy) from the source, not normalised:
+                    // parameters t' = t / m, chords scaled by m
+                    const float vx = fmaf(-u, s, q.z), vy = fmaf(u, c, q.w);
+                    const float m2 = fmaf(vx, vx, vy * vy);
+                    const float m = m2 * rsqrtf(m2);
+                    if (fabsf(vx) <= AWG_NEAR * m || fabsf(vy) <= AWG_NEAR * m) {
+                        awg_near(g, c, s, u, ix, iy, sv, acc);
+                        continue;
+                    }
+                    const float rvx = awg_rcp(vx), rvy = awg_rcp(vy);
+                    Ax = q2.x * rvx; Bx = d * rvx;
+                    Ay = q2.y * rvy; By = d * rvy;
+                    w = sv * m;
+                } else {
+                    Ax = fmaf(u, q2.x, q2.y); Bx = q.z;
+                    Ay = fmaf(u, q2.z, q2.w); By = q.w;
+                    w = sv;
+                }
+                float tx[3], ty[3];
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    tx[k] = fmaf(kx + (float)k, Bx, Ax);
+                    ty[k] = fmaf(ky + (float)k, By, Ay);
+                }
+                awg_chords(tx, ty, w, acc);
+            }
+        }
+    }
+    // the view parts' sums, added in part order
+    if (AWG_VS > 1) {
+        if (part > 0) {
+#pragma unroll
+            for (int i = 0; i < 4; ++i) red[part - 1][pt][i] = acc[i >> 1][i & 1];
+        }
+        __syncthreads();
+        if (part > 0) return;
+#pragma unroll
+        for (int p = 0; p < AWG_VS - 1; ++p)
+#pragma unroll
+            for (int i = 0; i < 4; ++i) acc[i >> 1][i & 1] += red[p][pt][i];
+    }
+    if (!inside) return;
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 2; ++j)
+            if (ix + i < g.nx && iy + j < g.ny) img[(size_t)(ix + i) * g.ny + iy + j] = acc[i][j] * sc;
 }
 
 // ---- pixel-driven ------------------------------------------------------------
@@ -770,11 +1002,19 @@ extern "C" int vg_rd_bp(const vg_ray_geom *g, const float *sino, const double *t
     if (s) return s;
     VG_REQUIRE(img && trig && sino, "rd_bp: null pointer");
     cudaStream_t st = as_stream(stream);
-    cudaError_t e = cudaMemsetAsync(img, 0, img_count(g) * sizeof(float), st);
-    if (e != cudaSuccess) return cuda_status(e, "rd_bp: clear");
     // img / na / d_pix^2 * du (rd.py:538, 646); cone img / na * du * dv (rd.py:786)
     const float sc = g->kind == 2 ? g->du * g->dv / (float)g->na
                                   : g->du / ((float)g->na * g->d_pix * g->d_pix);
+    if (g->kind < 2 && !g->joseph) {  // 2D walk: the gather form writes every pixel
+        dim3 grid(ceil_div(g->ny, 2 * AWG_TY), ceil_div(g->nx, 2 * AWG_TX));
+        VG_REQUIRE(grid.y < 65536, "rd_bp: nx too large");
+        const int nt = AWG_TY * AWG_TX * AWG_VS;
+        if (g->kind == 1) aw_bp2d_gather<true><<<grid, nt, 0, st>>>(*g, trig, sino, img, sc);
+        else aw_bp2d_gather<false><<<grid, nt, 0, st>>>(*g, trig, sino, img, sc);
+        return launch_status("rd_bp");
+    }
+    cudaError_t e = cudaMemsetAsync(img, 0, img_count(g) * sizeof(float), st);
+    if (e != cudaSuccess) return cuda_status(e, "rd_bp: clear");
     if (g->joseph) launch_rd<true, true>(*g, trig, sino, img, sc, st);
     else launch_rd<false, true>(*g, trig, sino, img, sc, st);
     return launch_status("rd_bp");
