@@ -217,8 +217,16 @@ __host__ __device__ inline int fp_line_entries(int nd) { return fp_slot(nd + 1) 
 constexpr unsigned FP_MAGIC_BITS = 0x4B400000u;  // 1.5 * 2^23, a multiple of 16
 constexpr unsigned FP_SLOT_BIAS = FP_MAGIC_BITS + (FP_MAGIC_BITS >> 4) + 15u;
 
+// Per-view back-projection table: entry i = j + 1 for bin j in -1 .. nu + 1
+// holds the running integral G of the sinogram row in the lookup coordinate
+// t' = (t + 1) / (nu + 2) (t the position in bins from U_0), G = x + y t':
+// (0, 0) before the detector (j = -1), (T_j - (j + 1) du s_j, du s_j (nu + 2))
+// on bin j, (T_nu, 0) past it (j = nu, nu + 1).  A lookup saturates t' to
+// [0, 1] and takes i = floor(t' (nu + 2)), so it needs no clamps.
+__host__ __device__ inline int bp_tab_len(int nu) { return nu + 3; }
+
 struct BpWork {
-    float2 *ts;  // [na][nu + 1]: (T_j - j du sino_j, du sino_j)
+    float2 *ts;  // [na][nu + 3], see bp_tab_len
     float *scl;  // [na][scl_stride]: signed line scale for the view's driving axis
 };
 
@@ -230,7 +238,7 @@ __host__ __device__ inline int scl_stride(const vg_dd2d_geom &g) {
 }
 
 __host__ __device__ inline size_t bp_ws_ts_bytes(const vg_dd2d_geom *g) {
-    return ((size_t)g->na * (g->nu + 1) * sizeof(float2) + 255) & ~(size_t)255;
+    return ((size_t)g->na * bp_tab_len(g->nu) * sizeof(float2) + 255) & ~(size_t)255;
 }
 size_t bp_ws_bytes(const vg_dd2d_geom *g) {
     return bp_ws_ts_bytes(g) + (((size_t)g->na * scl_stride(*g) * sizeof(float) + 255) & ~(size_t)255);
@@ -249,7 +257,7 @@ template <bool FAN, int NT = 256>
 __device__ __forceinline__ void bp_prep_view(const vg_dd2d_geom &g, const float *row, int ia,
                                              const double *__restrict__ trig, BpWork w,
                                              double *wsum) {
-    float2 *ts = w.ts + (size_t)ia * (g.nu + 1);
+    float2 *ts = w.ts + (size_t)ia * bp_tab_len(g.nu);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     // contiguous segment per thread
     const int per = (g.nu + NT - 1) / NT;
@@ -269,15 +277,20 @@ __device__ __forceinline__ void bp_prep_view(const vg_dd2d_geom &g, const float 
     for (int q = 0; q < warp; ++q) off += wsum[q];
     double run = off + inc - loc;
     const double du = (double)g.du;
+    const float yk = g.du * (float)(g.nu + 2);
     for (int i = 0; i < per; ++i) {
         const int j = j0 + i;
         if (j < g.nu) {
             const float sv = row[j];
-            ts[j] = make_float2((float)((run - (double)j * (double)sv) * du), g.du * sv);
+            ts[j + 1] = make_float2((float)((run - (double)(j + 1) * (double)sv) * du), yk * sv);
             run += (double)sv;
         }
     }
-    if (threadIdx.x == NT - 1) ts[g.nu] = make_float2((float)(run * du), 0.f);
+    if (threadIdx.x == 0) ts[0] = make_float2(0.f, 0.f);
+    if (threadIdx.x == NT - 1) {
+        ts[g.nu + 1] = make_float2((float)(run * du), 0.f);
+        ts[g.nu + 2] = make_float2((float)(run * du), 0.f);
+    }
     // line scales of this view, negated for lines whose edges project in
     // decreasing order (the pixel's interval is then [P(b+1), P(b)])
     const ViewGeo v = view_geo(trig, ia);
@@ -582,22 +595,23 @@ __device__ __forceinline__ float rcp_approx(float x) {
 #endif
 }
 
+// G at the lookup coordinate tq = sat((t + 1) / (nu + 2)) (see bp_tab_len):
+// the slot floor(tq (nu + 2)) is the bit pattern of a round-down FMA onto
+// 1.5 * 2^23 less that constant's, folded into the address.
 template <bool COH = false>
-__device__ __forceinline__ float bp_G(const float2 *__restrict__ ts, int nu, float t) {
-    // t: position in bins from U_0.  Before U_0 entry 0 gives x_0 = 0; past
-    // U_nu entry nu holds (T_nu, 0).
-    const float tc = fmaxf(t, 0.f);
-#if VG_BP_MAGIC
-    // floor from the bit pattern of a round-down add of 1.5 * 2^23 (FMA pipe),
-    // clamped in the integer domain (huge t lands on entry nu)
-    const int jb = min(__float_as_int(__fadd_rd(tc, 12582912.0f)), 0x4B400000 + nu);
-    const float2 e = ldro<COH>(ts + (jb - 0x4B400000));
-#else
-    // the conversion saturates
-    const int j = min(__float2int_rz(tc), nu);
-    const float2 e = ldro<COH>(ts + j);
-#endif
-    return fmaf(e.y, tc, e.x);
+__device__ __forceinline__ float bp_G(const float2 *__restrict__ ts, float nup2, float tq) {
+    const unsigned bits = __float_as_uint(__fmaf_rd(tq, nup2, 12582912.0f));
+    const float2 *p = reinterpret_cast<const float2 *>(reinterpret_cast<uintptr_t>(ts) +
+                                                      8ull * bits - 8ull * 0x4B400000u);
+    const float2 e = ldro<COH>(p);
+    return fmaf(e.y, tq, e.x);
+}
+
+// a b + c saturated to [0, 1] (NaN to 0)
+__device__ __forceinline__ float fma_sat(float a, float b, float c) {
+    float r;
+    asm("fma.rn.sat.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
 }
 
 // Each thread owns a 2x2 pixel patch.  A view drives along x (X-driven) or y:
@@ -625,7 +639,10 @@ __device__ __forceinline__ void bp_block(const vg_dd2d_geom &g, int tile_y, int 
     const int ix = tile_x * (2 * BP_TX) + 2 * ty;
     const bool inside = iy < g.ny && ix < g.nx;
     const int sstr = scl_stride(g);
-    const float t0 = -det_edge(g, 0) / g.du;
+    // lookup coordinate tq = (t + 1) / (nu + 2): the view coefficients and the
+    // offset carry the factor
+    const float nup2 = (float)(g.nu + 2), kq = 1.f / nup2;
+    const float t0 = (1.f - det_edge(g, 0) / g.du) * kq;
     const float bx = edge_coord(g.d_pix, ix, g.nx), by = edge_coord(g.d_pix, iy, g.ny);
     const float cx0 = bx + 0.5f * g.d_pix, cy0 = by + 0.5f * g.d_pix;
     const float2 *ts_all = w.ts;
@@ -635,7 +652,7 @@ __device__ __forceinline__ void bp_block(const vg_dd2d_geom &g, int tile_y, int 
         __syncthreads();
         if (tid < nv) {
             const ViewGeo v = view_geo(trig, a0 + tid);
-            const float k = (FAN ? g.DSD : 1.f) / g.du;
+            const float k = (FAN ? g.DSD : 1.f) / g.du * kq;
             Vs[tid] = FAN ? make_float4(k * v.pd, -v.od, k * v.po, -v.oo)
                           : make_float4(k * v.pd, 0.f, k * v.po, 0.f);
             Xs[tid] = v.xdrv;
@@ -651,7 +668,7 @@ __device__ __forceinline__ void bp_block(const vg_dd2d_geom &g, int tile_y, int 
             const float c0 = xd ? cy0 : cx0;  // centre of the first line
             const int io0 = xd ? iy : ix;
             const int no = xd ? g.ny : g.nx;
-            const float2 *ts = ts_all + (size_t)(a0 + vi) * (g.nu + 1);
+            const float2 *ts = ts_all + (size_t)(a0 + vi) * bp_tab_len(g.nu);
             // signed scales of lines io0 and io0 + 1 (io0 is even; rows padded)
             const float2 sc2 = ldro<COH>(reinterpret_cast<const float2 *>(w.scl + (size_t)(a0 + vi) * sstr + io0));
             float cL[2][2];  // [line][position along the driving axis]
@@ -664,9 +681,9 @@ __device__ __forceinline__ void bp_block(const vg_dd2d_geom &g, int tile_y, int 
 #pragma unroll
                 for (int e = 0; e < 3; ++e) {
                     const float b = fmaf((float)e, g.d_pix, b0);
-                    const float t = FAN ? fmaf(fmaf(q.x, b, nc), rcp_approx(fmaf(q.y, b, dc)), t0)
-                                        : fmaf(q.x, b, nc);
-                    G[e] = bp_G<COH>(ts, g.nu, t);
+                    const float tq = FAN ? fma_sat(fmaf(q.x, b, nc), rcp_approx(fmaf(q.y, b, dc)), t0)
+                                         : fma_sat(q.x, b, nc);
+                    G[e] = bp_G<COH>(ts, nup2, tq);
                 }
                 const float s = (io0 + L < no) ? (L ? sc2.y : sc2.x) : 0.f;
                 cL[L][0] = (G[1] - G[0]) * s;
