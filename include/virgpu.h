@@ -374,15 +374,18 @@ int vg_dd3d_bp(const vg_dd3d_geom *g, const float *sino, const double *trig,
  * over the cell; l_phi0 = d |r| / max(|r_x|, |r_y|) for the transaxial ray r
  * through the column centre, l_theta = sqrt(1 + v^2 / (u^2 + DSD^2)) at the
  * cell centre.
- * vg_sf3d_fp: sino (na, nu, nv) = the line integrals above, gather form.
- * vg_sf3d_bp: vol = its exact adjoint; workspace of
- *   vg_sf3d_workspace_bytes(g) bytes (the l_theta-weighted sinogram of a
- *   chunk of views, at most 256 MiB or one view), 4-byte aligned.
+ * vg_sf3d_fp: sino (na, nu, nv) = the line integrals above, gather form;
+ *   workspace: the volume's per-column running sums over z (nx ny (nz + 1)
+ *   floats, FP64-accumulated) from which each column's v profile is read.
+ * vg_sf3d_bp: vol = its exact adjoint; workspace: the l_theta-weighted
+ *   sinogram of a chunk of views (at most 256 MiB or one view).
+ * Both take vg_sf3d_workspace_bytes(g) bytes (the larger need), 4-byte
+ * aligned.
  * nx and ny at most 2048.
  * The volume must lie inside the source circle (half diagonal below DSO). */
 size_t vg_sf3d_workspace_bytes(const vg_dd3d_geom *g);
 int vg_sf3d_fp(const vg_dd3d_geom *g, const float *vol, const double *trig, float *sino,
-               void *stream);
+               void *workspace, size_t workspace_bytes, void *stream);
 int vg_sf3d_bp(const vg_dd3d_geom *g, const float *sino, const double *trig, float *vol,
                void *workspace, size_t workspace_bytes, void *stream);
 

@@ -125,7 +125,8 @@ _PROTOS = {
     "vg_sirt2d_batch_run": [c_void_p, c_int, c_int, c_void_p, c_int, c_void_p, c_int, c_void_p,
                             c_int, c_int, c_int, c_void_p, ctypes.c_ulonglong, c_void_p, c_void_p,
                             c_void_p, c_void_p],
-    "vg_sf3d_fp": [ctypes.POINTER(DD3DGeom), c_void_p, c_void_p, c_void_p, c_void_p],
+    "vg_sf3d_fp": [ctypes.POINTER(DD3DGeom), c_void_p, c_void_p, c_void_p, c_void_p, c_size_t,
+                   c_void_p],
     "vg_sf3d_bp": [ctypes.POINTER(DD3DGeom), c_void_p, c_void_p, c_void_p, c_void_p, c_size_t,
                    c_void_p],
     "vg_dd3d_bp": [ctypes.POINTER(DD3DGeom), c_void_p, c_void_p, c_void_p, c_void_p, c_size_t,

@@ -22,14 +22,17 @@
 // The forward projection returns these line integrals; the back projection
 // is its exact adjoint (vir has no back projector for this footprint).
 //
-//  FP (sf3d_fp_kernel): block = (view, 32 u x 64 v cells), thread = 4 u
-//    cells (warp) x 2 v cells (lanes).  For each orthogonal pixel line whose
-//    columns reach the tile, the block tabulates in shared memory the
-//    columns' footprints, the covering columns and F1 weights of each u
-//    cell, and each column's v profile over the tile's v cells
-//    g(c, l) = sum_z f(c, z) F2(l; c, z); each cell then adds
-//    F1 * l_phi0 * g over its 1-8 covering columns.  Lines where a u cell
-//    meets more columns, or the tile more than 64, take a per-cell path.
+//  FP (sf3d_zprefix, sf3d_fp_kernel): the volume's per-column running sums
+//    over z are formed first (workspace).  Block = (view, 32 u x 64 v cells),
+//    thread = 4 u cells (warp) x 2 v cells (lanes).  For each orthogonal
+//    pixel line whose columns reach the tile, the block tabulates in shared
+//    memory the columns' footprints, the covering columns and F1 weights of
+//    each u cell, and each column's v profile over the tile's v cells
+//    g(c, l) = sum_z f(c, z) F2(l; c, z) as the running integral at the 65
+//    v edges (the z sums interpolated at the edge's slice coordinate); each
+//    cell then adds F1 * l_phi0 * (difference of its edges) over its 1-8
+//    covering columns.  Lines where a u cell meets more columns, or the tile
+//    more than 64, take a per-cell path.
 //  BP (sf3d_bp_kernel): the sinogram is first multiplied by l_theta
 //    (sf3d_weight, into the workspace, a chunk of views at a time); block =
 //    8 x 8 columns x 32 slices, thread = one slice of 8 columns; per view a
@@ -134,34 +137,6 @@ __device__ __forceinline__ float vprofile(const vg_dd3d_geom &g, const float *__
     return acc * inv_dv;
 }
 
-// vprofile for a v cell [va, vb] in slice coordinates s = v / (M d) + nz / 2:
-// the cell meets slices floor(sa) .. floor(sb); when that is at most two
-// slices (the cell no taller than a slice), both are read at once and
-// weighted by their overlaps, else the slices are walked.
-__device__ __forceinline__ float vprofile2(const vg_dd3d_geom &g, const float *__restrict__ col,
-                                           float mz, float inv_mz, float va, float vb, float hz,
-                                           float nzf, float inv_dv) {
-    const float sa = fmaxf(fmaf(va, inv_mz, hz), 0.f), sb = fminf(fmaf(vb, inv_mz, hz), nzf);
-    if (!(sb > sa)) return 0.f;
-    const float fa = floorf(sa);
-    const int z0 = (int)fa;
-    float acc;
-    if (sb <= fa + 2.f) {
-        const float f0 = __ldg(col + z0);                       // z0 < nz since sa < sb <= nz
-        const float f1 = z0 + 1 < g.nz ? __ldg(col + z0 + 1) : 0.f;
-        const float w0 = fminf(sb, fa + 1.f) - sa, w1 = fmaxf(sb - (fa + 1.f), 0.f);
-        acc = fmaf(f0, w0, f1 * w1);
-    } else {
-        acc = 0.f;
-        const int z1 = min((int)floorf(sb), g.nz - 1);
-        for (int z = z0; z <= z1; ++z) {
-            const float ov = fminf(sb, (float)(z + 1)) - fmaxf(sa, (float)z);
-            if (ov > 0.f) acc = fmaf(__ldg(col + z), ov, acc);
-        }
-    }
-    return acc * (mz * inv_dv);
-}
-
 // Fractional pixel index, along the driving axis, of the point of the line
 // at orthogonal coordinate `cen` that projects to u (x, y = (b, cen) when
 // X-driven, else (cen, b)):  b (DSD pd + u od) = u (DSO - oc) - DSD pc.
@@ -173,6 +148,33 @@ __device__ __forceinline__ float unproj_idx(const vg_dd3d_geom &g, float c, floa
     return __fdividef(b, g.d_pix) + 0.5f * nd;
 }
 
+// Per-column running sums over z for the forward projection's v profiles:
+// zp[c][z] = sum_{z' < z} f(c, z') for z = 0 .. nz (column c = x ny + y),
+// accumulated in FP64 and rounded once, so that a profile's edge value
+// (an interpolation of zp) and the difference of two of them carry a
+// rounding of the column's total, not of its summation.  One warp per column.
+__global__ void __launch_bounds__(256)
+sf3d_zprefix(vg_dd3d_geom g, const float *__restrict__ vol, float *__restrict__ zp) {
+    const size_t col = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (col >= (size_t)g.nx * g.ny) return;
+    const float *f = vol + col * g.nz;
+    float *p = zp + col * (g.nz + 1);
+    if (lane == 0) p[0] = 0.f;
+    double carry = 0.0;
+    for (int z0 = 0; z0 < g.nz; z0 += 32) {
+        const int z = z0 + lane;
+        double v = z < g.nz ? (double)__ldg(f + z) : 0.0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const double t = __shfl_up_sync(0xffffffffu, v, o);
+            if (lane >= o) v += t;
+        }
+        if (z < g.nz) p[z + 1] = (float)(carry + v);
+        carry += __shfl_sync(0xffffffffu, v, 31);
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Forward projection
 // ---------------------------------------------------------------------------
@@ -181,10 +183,10 @@ constexpr int SU = 32, SV = 64, SCMAX = 64, SKMAX = 8, SLINES = 2048;
 // per-line tables, double-buffered by line parity
 struct SfFpTab {
     SfCol col[2][SCMAX];
-    int off[2][SCMAX];      // voxel index of (column, z = 0)
+    int poff[2][SCMAX];     // index of (column, z = 0) in the z-prefix array
     int cf[2][SU], cn[2][SU];  // covering columns (table index, count) per u cell
     float w[2][SU][SKMAX];  // F1 l_phi0 weights of those columns
-    float gv[2][SCMAX][SV];
+    float gv[2][SCMAX][SV + 1];  // per column: the v profile's running integral at the v edges
     int2 kr[SLINES];        // per line: the range [x, y] of columns that can reach the tile
     float ve[SV + 1];       // the tile's v cell edges
     int wide[2];
@@ -212,8 +214,8 @@ __device__ __noinline__ float sf_cell_line(const vg_dd3d_geom &g, const float *_
 }
 
 __global__ void __launch_bounds__(256, 3)
-sf3d_fp_kernel(vg_dd3d_geom g, const float *__restrict__ vol, const double *__restrict__ trig,
-               float *__restrict__ sino) {
+sf3d_fp_kernel(vg_dd3d_geom g, const float *__restrict__ vol, const float *__restrict__ zp,
+               const double *__restrict__ trig, float *__restrict__ sino) {
     __shared__ SfFpTab T;
     const int ia = blockIdx.z;
     const int u0 = blockIdx.y * SU, v0 = blockIdx.x * SV;
@@ -270,7 +272,7 @@ sf3d_fp_kernel(vg_dd3d_geom g, const float *__restrict__ vol, const double *__re
             const float cen = vox(g.d_pix, io, no), bx = vox(g.d_pix, k, nd);
             T.col[bb][tid] = sf_col(g, c, s, xdrv ? bx : cen, xdrv ? cen : bx);
             const int ix = xdrv ? k : io, iy = xdrv ? io : k;
-            T.off[bb][tid] = (ix * g.ny + iy) * g.nz;
+            T.poff[bb][tid] = (ix * g.ny + iy) * (g.nz + 1);
         }
     };
     auto next_line = [&](int io) {
@@ -325,14 +327,21 @@ sf3d_fp_kernel(vg_dd3d_geom g, const float *__restrict__ vol, const double *__re
                 }
                 if (wm < n && wm < SKMAX) T.w[b][wu][wm] = uweight(T.col[b][first + wm], ua, ub, inv_du);
             }
-            // phase 2b: v profiles of the table's columns over the tile's v cells
-            for (int p = tid; p < nk * SV; p += 256) {
-                const int t = p / SV, l = p % SV;
-                float gval = 0.f;
-                if (l < nvT)
-                    gval = vprofile2(g, vol + T.off[b][t], T.col[b][t].mz, T.col[b][t].inv_mz,
-                                     T.ve[l], T.ve[l + 1], hz, nzf, inv_dv);
-                T.gv[b][t][l] = gval;
+            // phase 2b: per column, the running integral of its v profile at the
+            // tile's v edges: the column's z-prefix interpolated at the edge's
+            // slice coordinate s = v / (M d) + nz/2, times M d / dv; a cell's
+            // profile is the difference of its two edges
+            for (int p = tid; p < nk * (SV + 1); p += 256) {
+                const int t = p / (SV + 1), l = p - t * (SV + 1);
+                float e = 0.f;
+                if (l <= nvT) {
+                    const float sz = fminf(fmaxf(fmaf(T.ve[l], T.col[b][t].inv_mz, hz), 0.f), nzf);
+                    const float zf = fminf(floorf(sz), nzf - 1.f);
+                    const float *pc = zp + T.poff[b][t] + (int)zf;
+                    const float p0 = __ldg(pc), p1 = __ldg(pc + 1);
+                    e = fmaf(p1 - p0, sz - zf, p0) * (T.col[b][t].mz * inv_dv);
+                }
+                T.gv[b][t][l] = e;
             }
         }
         __syncthreads();
@@ -347,8 +356,9 @@ sf3d_fp_kernel(vg_dd3d_geom g, const float *__restrict__ vol, const double *__re
                     const int f0 = T.cf[b][j], n = T.cn[b][j];
                     for (int m = 0; m < n; ++m) {
                         const float w = T.w[b][j][m];
-                        pa = fmaf(w, T.gv[b][f0 + m][lane], pa);
-                        pb = fmaf(w, T.gv[b][f0 + m][32 + lane], pb);
+                        const float *gr = T.gv[b][f0 + m];
+                        pa = fmaf(w, gr[lane + 1] - gr[lane], pa);
+                        pb = fmaf(w, gr[33 + lane] - gr[32 + lane], pb);
                     }
                 }
                 part[2 * q] = pa;
@@ -557,7 +567,8 @@ int check(const vg_dd3d_geom *g) {
     VG_REQUIRE(g->na < 65536 && ceil_div(g->nx, BT) < 65536 && ceil_div(g->ny, BT) < 65536 &&
                    ceil_div(g->nu, SU) < 65536, "sf3d: sizes too large");
     VG_REQUIRE(g->nx <= SLINES && g->ny <= SLINES, "sf3d: nx and ny at most %d", SLINES);
-    VG_REQUIRE((double)g->nx * g->ny * g->nz < 2147483648.0, "sf3d: volume above 2^31 voxels");
+    // (nz + 1: the forward projection's z sums index the volume's columns with one extra entry)
+    VG_REQUIRE((double)g->nx * g->ny * (g->nz + 1) < 2147483648.0, "sf3d: volume above 2^31 voxels");
     VG_REQUIRE(g->du > 0.f && g->dv > 0.f && g->d_pix > 0.f && g->DSO > 0.f && g->DSD > 0.f,
                "sf3d: pitches and distances must be positive");
     // every voxel in front of the source (its footprint's projections are
@@ -582,20 +593,36 @@ size_t bp_ws_bytes(const vg_dd3d_geom *g) {
     return chunk_views(g) * (size_t)g->nu * g->nv * sizeof(float);
 }
 
+// the forward projection's z-prefix array: nx ny (nz + 1) floats
+size_t fp_ws_bytes(const vg_dd3d_geom *g) {
+    return (size_t)g->nx * g->ny * (g->nz + 1) * sizeof(float);
+}
+
 }  // namespace
 
 extern "C" size_t vg_sf3d_workspace_bytes(const vg_dd3d_geom *g) {
     if (check(g)) return 0;
-    return bp_ws_bytes(g);
+    const size_t f = fp_ws_bytes(g), b = bp_ws_bytes(g);
+    return f > b ? f : b;
 }
 
 extern "C" int vg_sf3d_fp(const vg_dd3d_geom *g, const float *vol, const double *trig, float *sino,
-                          void *stream) {
+                          void *workspace, size_t workspace_bytes, void *stream) {
     int st = check(g);
     if (st) return st;
     VG_REQUIRE(vol && trig && sino, "sf3d_fp: null pointer");
+    const size_t need = fp_ws_bytes(g);
+    VG_REQUIRE(workspace && workspace_bytes >= need,
+               "sf3d_fp: workspace of %zu bytes needed (vg_sf3d_workspace_bytes)", need);
+    VG_REQUIRE(((uintptr_t)workspace & 3) == 0, "sf3d_fp: workspace must be 4-byte aligned");
+    cudaStream_t s = as_stream(stream);
+    float *zp = static_cast<float *>(workspace);
+    const size_t ncol = (size_t)g->nx * g->ny;
+    sf3d_zprefix<<<ceil_div((long long)ncol * 32, 256), 256, 0, s>>>(*g, vol, zp);
+    st = launch_status("sf3d_zprefix");
+    if (st) return st;
     dim3 grid(ceil_div(g->nv, SV), ceil_div(g->nu, SU), g->na);
-    sf3d_fp_kernel<<<grid, 256, 0, as_stream(stream)>>>(*g, vol, trig, sino);
+    sf3d_fp_kernel<<<grid, 256, 0, s>>>(*g, vol, zp, trig, sino);
     return launch_status("sf3d_fp");
 }
 

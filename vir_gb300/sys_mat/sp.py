@@ -87,8 +87,9 @@ def sf_fp_cone_3d(img, ang_arr, nu, nv, DSO, DSD, du=1.0, dv=1.0, su=0.0, sv=0.0
     na = trig.numel() // 2
     g = _g3(x.shape, na, nu, nv, du, dv, su, sv, d_pix, DSO, DSD)
     sino = _core.empty((na, int(nu), int(nv)), dev)
+    ws = _sf3d_workspace(g, dev)
     call("vg_sf3d_fp", ctypes.byref(g), _core.ptr(x), _core.ptr(trig), _core.ptr(sino),
-         _core.stream(dev))
+         _core.ptr(ws), ws.numel() * 8, _core.stream(dev))
     return _core.to_host_like(sino, img)
 
 
