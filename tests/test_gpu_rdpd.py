@@ -262,3 +262,25 @@ def test_aw_bp_gather_fan_benchmark_geometry(vg, orc):
     lhs = float((A.double() * torch.from_numpy(y).cuda().double()).sum())
     rhs = float((x.double() * B.double()).sum()) * 720 * 0.9 ** 2 / float(np.float32(1.2))
     assert abs(lhs - rhs) / lhs < 1e-5
+
+
+@pytest.mark.parametrize("geo", ["par", "fan"])
+def test_aw_bp_gather_odd_image(vg, orc, geo):
+    """Odd, non-square images (the last 2 x 2 patch of a row or column half
+    outside) and a detector shifted off centre, against the FP64 walk."""
+    from vir_gb300.sys_mat import rd
+    rng = np.random.default_rng(41)
+    na, nu = 30, 90
+    angs = np.linspace(0.2, 0.2 + (2 * np.pi if geo == "fan" else np.pi), na, endpoint=False)
+    y = rng.random((na, nu)).astype(np.float32)
+    kw = dict(du=0.9, su=1.7, d_pix=0.8)
+    if geo == "par":
+        bp = rd.aw_bp_par_2d(y, angs, (37, 53), **kw)
+        bo = orc.aw_bp_par_2d(y, angs, (37, 53), **kw)
+        tol = 2e-5
+    else:
+        bp = rd.aw_bp_fan_2d(y, angs, (37, 53), 90.0, 160.0, **kw)
+        bo = orc.aw_bp_fan_2d(y, angs, (37, 53), 90.0, 160.0, **kw)
+        tol = 1e-4
+    assert bp.shape == (37, 53)
+    assert rel(bp, bo) < tol

@@ -70,7 +70,7 @@ def test_sirt_launch_count_without_gpu():
 def test_batch_items_without_gpu():
     """vg_sirt2d_batch_items (host-only): per problem na * chunks forward
     projection items (chunks of 192, 384 or 768 bins), na table items and
-    (ny / 64) x (nx / 16) back projection tiles, rounded up; every (problem,
+    (ny / 16) x (nx / 64) back projection tiles, rounded up; every (problem,
     item) pair listed once; null buffers, misaligned workspaces and fan
     detectors reaching the inverse map's pole are refused."""
     import numpy as np
@@ -91,7 +91,7 @@ def test_batch_items_without_gpu():
     chunk = lambda nu: 192 if nu <= 192 else (384 if nu <= 384 else 768)
     ef = sum(na * -(-nu // chunk(nu)) for _, _, na, nu, _ in geoms)
     et = sum(na for _, _, na, _, _ in geoms)
-    eb = sum(-(-ny // 64) * -(-nx // 16) for nx, ny, _, _, _ in geoms)
+    eb = sum(-(-ny // 16) * -(-nx // 64) for nx, ny, _, _, _ in geoms)
     assert (nf.value, nt.value, nb.value) == (ef, et, eb)
     fi = np.empty((ef, 2), np.int32)
     ti = np.empty((et, 2), np.int32)
@@ -100,7 +100,7 @@ def test_batch_items_without_gpu():
                                    ctypes.byref(nt), bi.ctypes.data, ctypes.byref(nb)) == 0
     for items, per in ((fi, lambda q: geoms[q][2] * -(-geoms[q][3] // chunk(geoms[q][3]))),
                        (ti, lambda q: geoms[q][2]),
-                       (bi, lambda q: -(-geoms[q][1] // 64) * -(-geoms[q][0] // 16))):
+                       (bi, lambda q: -(-geoms[q][1] // 16) * -(-geoms[q][0] // 64))):
         pairs = set(map(tuple, items.tolist()))
         assert len(pairs) == len(items)
         assert pairs == {(q, k) for q in range(n) for k in range(per(q))}
