@@ -37,28 +37,23 @@
 
 #include <cuda_bf16.h>
 
-// Edge projections divide with __fdividef (reciprocal + multiply, 2 ulp)
-// unless built with -DVG_FAST_DIV=0 (IEEE division).
+// The forward projection's fused SIRT epilogue also writes the back
+// projection's tables (two launches per update; 0 restores the separate
+// table kernel).
 #ifndef VG_SIRT_FUSED_TABLES
 #define VG_SIRT_FUSED_TABLES 1
 #endif
 
+// Edge projections and bin positions use approximate reciprocals
+// (rcp.approx, about 1 ulp) unless built with -DVG_FAST_DIV=0 (IEEE division).
 #ifndef VG_FAST_DIV
 #define VG_FAST_DIV 1
 #endif
 
-// VG_FP_MAGIC / VG_BP_MAGIC = 1: the forward projection's inverse edge map
-// and the back projection's table lookups take their floor by a round-down
-// add of 1.5 * 2^23 (an FMA-pipe add whose bit pattern holds the integer)
-// instead of a float-to-int conversion on the XU pipe (the same integer for
-// |x| < 2^22, clamped in the integer domain beyond).
-#ifndef VG_FP_MAGIC
-#define VG_FP_MAGIC 1
-#endif
-
-#ifndef VG_BP_MAGIC
-#define VG_BP_MAGIC 1
-#endif
+// Both projections find a pixel or bin index as the bit pattern of a
+// round-down FMA onto 1.5 * 2^23 (an FMA-pipe operation; exact floor for
+// values below 2^22), after saturating the lookup coordinate to [0, 1] in
+// the preceding FMA, so that no clamp or float-to-int conversion is needed.
 
 namespace {
 
