@@ -331,6 +331,52 @@ def storage_error(probs, dev, n_check=2, iters=50):
     return out
 
 
+def c3_summary(dev, stream):
+    """The batched-SIRT configuration (64 parallel/fan problems of seed 3, 50
+    updates): one CUDA graph of per-problem chains, one launch per step (the
+    plain FP32 path), one persistent launch in each storage mode; its
+    iterates against the graph's, and the final-iterate error of each storage
+    mode against the FP64 oracle's SIRT on the two smallest problems."""
+    import torch
+    from vir_gb300.batched import BatchedSIRT2D, PersistentSIRT2D
+    from vir_gb300.workloads import batched_problems
+    probs = batched_problems(64, seed=3)
+    b = BatchedSIRT2D(probs, n_streams=16)
+    res = {}
+    for mode in ("graph", "plain"):
+        b.reset()
+        res[mode] = _event_ms(lambda: b.run(50) if mode == "graph" else b.plain(50), 1, stream)
+    b.reset()
+    b.run(50)
+    xg = [x.clone() for x in b.images()]
+    del b
+    torch.cuda.empty_cache()
+    pers = {}
+    for st in ("fp32", "bf16y", "bf16x", "bf16"):
+        pb = PersistentSIRT2D(probs, device=dev, storage=st)
+        pb.run(1)
+        pb.reset()
+        pers[st] = _event_ms(lambda: pb.run(50, wait=False), 1, stream)
+        if st == "fp32":
+            pb.reset()
+            status = pb.run(50)
+            diff = max(float((a - c).abs().max() / c.abs().max()) for a, c in zip(pb.images(), xg))
+            grid = pb.grid_blocks
+        del pb
+        torch.cuda.empty_cache()
+    units = sum(p["sino"].shape[0] * p["img_shape"][0] * p["img_shape"][1] for p in probs)
+    return {"metric": "batched SIRT iter/s (50 updates x 64 problems)",
+            "graph_ms": res["graph"], "plain_ms": res["plain"],
+            "persistent_ms": pers, "persistent_status": status,
+            "persistent_grid_blocks": grid,
+            "persistent_vs_graph_max_rel_diff": diff,
+            "speedup_vs_plain": {"graph": res["plain"] / res["graph"],
+                                 **{"persistent_" + k: res["plain"] / v for k, v in pers.items()}},
+            "fwd_back_gups_graph": 2 * 50 * units / (res["graph"] / 1e3) / 1e9,
+            "fwd_back_gups_persistent": 2 * 50 * units / (pers["fp32"] / 1e3) / 1e9,
+            "storage_error": storage_error(probs, dev)}
+
+
 def run_workload(args):
     """One JSON line for a configuration other than the default C2 line:
     per-kernel CUDA-event times (median of --steps after --warmup), GUPS and
@@ -702,52 +748,16 @@ def run_workload(args):
         print(json.dumps(line), flush=True)
         return 0
     elif wl == "c3":
-        from vir_gb300.batched import BatchedSIRT2D
-        from vir_gb300.workloads import batched_problems
-        from vir_gb300.batched import PersistentSIRT2D
-        probs = batched_problems(64, seed=3)
         if args.kernels_only:  # profiling aid: N persistent launches of 2 updates each
-            pb = PersistentSIRT2D(probs, device=dev)
+            from vir_gb300.batched import PersistentSIRT2D
+            from vir_gb300.workloads import batched_problems
+            pb = PersistentSIRT2D(batched_problems(64, seed=3), device=dev)
             for _ in range(args.kernels_only):
                 pb.reset()
                 pb.run(2)
             print(json.dumps({"kernels_only": args.kernels_only, "workload": wl, "ok": True}))
             return 0
-        b = BatchedSIRT2D(probs, n_streams=16)
-        res = {}
-        for mode in ("graph", "plain"):
-            b.reset()
-            res[mode] = _event_ms(lambda: b.run(50) if mode == "graph" else b.plain(50), 1, stream)
-        b.reset()
-        b.run(50)
-        xg = [x.clone() for x in b.images()]
-        del b
-        torch.cuda.empty_cache()
-        pers = {}
-        for st in ("fp32", "bf16y", "bf16x", "bf16"):
-            pb = PersistentSIRT2D(probs, device=dev, storage=st)
-            pb.run(1)
-            pb.reset()
-            pers[st] = _event_ms(lambda: pb.run(50, wait=False), 1, stream)
-            if st == "fp32":
-                pb.reset()
-                status = pb.run(50)
-                diff = max(float((a - c).abs().max() / c.abs().max()) for a, c in zip(pb.images(), xg))
-                grid = pb.grid_blocks
-            del pb
-            torch.cuda.empty_cache()
-        units = sum(p["sino"].shape[0] * p["img_shape"][0] * p["img_shape"][1] for p in probs)
-        line.update({"metric": "batched SIRT iter/s (50 updates x 64 problems)",
-                     "graph_ms": res["graph"], "plain_ms": res["plain"],
-                     "persistent_ms": pers, "persistent_status": status,
-                     "persistent_grid_blocks": grid,
-                     "persistent_vs_graph_max_rel_diff": diff,
-                     "speedup_vs_plain": {"graph": res["plain"] / res["graph"],
-                                          **{"persistent_" + k: res["plain"] / v
-                                             for k, v in pers.items()}},
-                     "fwd_back_gups_graph": 2 * 50 * units / (res["graph"] / 1e3) / 1e9,
-                     "fwd_back_gups_persistent": 2 * 50 * units / (pers["fp32"] / 1e3) / 1e9,
-                     "storage_error": storage_error(probs, dev)})
+        line.update(c3_summary(dev, stream))
         print(json.dumps(line), flush=True)
         return 0
     if args.kernels_only:
@@ -825,6 +835,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-c3", action="store_true",
+                    help="leave out the batched-SIRT summary (the C3 problem set) of the default line")
     ap.add_argument("--kernels-only", type=int, default=0, metavar="N",
                     help="profiling aid: run the two fused SIRT kernels N times each, no timing")
     ap.add_argument("--workload", default="c2", choices=["c2"] + sorted(EXTRA),
@@ -1001,6 +1013,11 @@ def main():
             "rmse_vs_phantom_rel": abs(rmse - r_orc) / r_orc,
             "rmse_vs_phantom_oracle": r_orc, "criterion": 1e-4,
             "what": f"the GPU iterate after {U} updates vs the FP64 oracle's"}
+    if rank == 0 and world == 1 and not args.no_c3:
+        # after the timed region: the batched-SIRT configuration, so that its
+        # speed-ups over the plain path and its error against the oracle are
+        # part of the benchmark record
+        line["batched"] = {"workload": EXTRA["c3"], **c3_summary(dev, stream)}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
