@@ -1013,6 +1013,27 @@ def main():
             "rmse_vs_phantom_rel": abs(rmse - r_orc) / r_orc,
             "rmse_vs_phantom_oracle": r_orc, "criterion": 1e-4,
             "what": f"the GPU iterate after {U} updates vs the FP64 oracle's"}
+    if rank == 0 and world == 1:
+        # the FBP half of the configuration: fan FBP of the same noisy
+        # sinogram with the Ram-Lak and Hann windows (cosine weight, FFT ramp
+        # filter, 1/U^2-weighted back projection), against the phantom and,
+        # with the CPU legs, against the FP64 oracle's FBP
+        f32 = lambda v: float(np.float32(v))
+        y_dev = torch.from_numpy(y).to(dev)
+        line["fbp"] = {}
+        for filt in ("ramp", "hann"):
+            run = lambda: rc.fbp_2d(y_dev, angs, img.shape, geom="fan", DSO=w["DSO"], DSD=w["DSD"],
+                                    du=w["du"], d_pix=w["d_pix"], filter_type=filt)
+            ms = _event_ms(run, 10, stream)
+            rec = run().cpu().numpy()
+            rec_f = {"ms": ms, "rmse_vs_phantom": float(np.sqrt(np.mean((rec - img) ** 2)))}
+            if not args.no_cpu_baseline:
+                from oracle import oracle as orc
+                ref = orc.fbp_2d(y, angs, img.shape, fan=True, DSO=f32(w["DSO"]), DSD=f32(w["DSD"]),
+                                 du=f32(w["du"]), d_pix=f32(w["d_pix"]), filter_type=filt)
+                rec_f["oracle_max_rel"] = float(np.abs(rec - ref).max() / np.abs(ref).max())
+                rec_f["oracle_rel_l2"] = float(np.linalg.norm(rec - ref) / np.linalg.norm(ref))
+            line["fbp"]["ram-lak" if filt == "ramp" else filt] = rec_f
     if rank == 0 and world == 1 and not args.no_c3:
         # after the timed region: the batched-SIRT configuration, so that its
         # speed-ups over the plain path and its error against the oracle are
