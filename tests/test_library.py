@@ -48,6 +48,25 @@ def test_argument_errors_without_gpu():
     assert b"positive" in L.vg_last_error()
 
 
+def test_sf3d_workspace_without_gpu():
+    """vg_sf3d_workspace_bytes (host only) covers both cone SF calls: the
+    forward projection's per-column z sums, nx ny (nz + 1) floats, and the
+    back projection's weighted view chunk (at most 256 MiB or one view);
+    a forward projection given less is refused before any launch."""
+    from vir_gb300 import _lib
+    L = _lib.load()
+    for (n, nz, na, nu, nv) in ((256, 256, 360, 512, 384), (64, 40, 10, 80, 60), (512, 512, 720, 1024, 768)):
+        g = _lib.DD3DGeom(n, n, nz, na, nu, nv, 1.6, 1.6, 0.0, 0.0, 1.0, 600.0, 1100.0)
+        fp_need = n * n * (nz + 1) * 4
+        chunk = max(1, min(na, (256 << 20) // (nu * nv * 4)))
+        bp_need = chunk * nu * nv * 4
+        assert L.vg_sf3d_workspace_bytes(ctypes.byref(g)) == max(fp_need, bp_need)
+    g = _lib.DD3DGeom(64, 64, 40, 10, 80, 60, 1.6, 1.6, 0.0, 0.0, 1.0, 600.0, 1100.0)
+    p = ctypes.c_void_p(256)  # never dereferenced
+    st = L.vg_sf3d_fp(ctypes.byref(g), p, p, p, p, 64 * 64 * 41 * 4 - 4, None)
+    assert st == 1 and b"workspace" in L.vg_last_error()
+
+
 def test_sirt_launch_count_without_gpu():
     """vg_dd2d_sirt_launches (host-only): 2 launches per SIRT update when one
     8-warp block holds all bins of a view (the forward projection then writes
