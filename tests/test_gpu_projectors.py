@@ -371,3 +371,30 @@ def test_dd_fp_every_tile_variant_vs_oracle(vg, orc, fan):
         s.g.variant = v
         fp = s.fp(x).cpu().numpy()
         assert rel(fp, fo) < 1e-4, v
+
+
+def test_sirt_2d_reuses_prepared_state(vg):
+    """sirt_2d keeps a geometry's prepared state (weights, buffers, update
+    graph): calls with different sinograms (numpy, then a pinned CPU tensor),
+    alternating, give bit for bit the iterates of fresh states, and a new
+    update count is captured anew."""
+    import torch
+    from vir_gb300 import reconstruction as rc
+    rng = np.random.default_rng(51)
+    angs = np.linspace(0, 2 * np.pi, 60, endpoint=False)
+    geo = dict(geom="fan", DSO=150.0, DSD=300.0, du=1.5, d_pix=1.0)
+    y1 = rng.random((60, 140)).astype(np.float32)
+    y2 = rng.random((60, 140)).astype(np.float32)
+
+    def fresh(y, iters):
+        s = rc.SIRT2D(y, angs, (96, 96), **geo)
+        return s.run(iters - 1).cpu().numpy()
+
+    rc.prepared_sirt.clear()
+    a1 = rc.sirt_2d(y1, angs, (96, 96), iters=6, **geo)
+    a2 = rc.sirt_2d(torch.from_numpy(y2).pin_memory(), angs, (96, 96), iters=6, **geo)
+    a1b = rc.sirt_2d(y1, angs, (96, 96), iters=6, **geo)
+    a2c = rc.sirt_2d(y2, angs, (96, 96), iters=9, **geo)
+    assert np.array_equal(a1, fresh(y1, 6)) and np.array_equal(a1b, a1)
+    assert np.array_equal(np.asarray(a2), fresh(y2, 6))
+    assert np.array_equal(a2c, fresh(y2, 9))

@@ -21,7 +21,9 @@ isocentre and filters at the isocentre spacing du * DSO / DSD.
 """
 from __future__ import annotations
 
+import collections
 import ctypes
+import threading
 
 import numpy as np
 import torch
@@ -79,6 +81,20 @@ class SIRT2D:
         self.r = torch.empty((na, nu), dtype=torch.float32, device=self.dev)
         self._graph = None
         self._graph_n = 0
+
+    def load_sino(self, sino):
+        """Copy a new measured sinogram of the same shape into the resident
+        ``y`` (asynchronous from pinned host memory; ordered before the next
+        update on the current stream)."""
+        if _core.is_torch(sino):
+            src = sino.detach()
+            if src.dtype != torch.float32:
+                src = src.float()
+        else:
+            src = torch.from_numpy(np.ascontiguousarray(np.asarray(sino), dtype=np.float32))
+        if tuple(src.shape) != tuple(self.y.shape):
+            raise ValueError(f"sino shape {tuple(src.shape)} != {tuple(self.y.shape)}")
+        self.y.copy_(src, non_blocking=True)
 
     # projector pair on this geometry
     def fp(self, img: torch.Tensor) -> torch.Tensor:
@@ -223,14 +239,66 @@ def sirt_3d(sino, ang_arr, img_shape, DSO, DSD, du=1.0, dv=1.0, su=0.0, sv=0.0, 
     return _core.to_host_like(x.clone(), sino)
 
 
+class _PreparedSirt:
+    """The prepared SIRT2D states of the last few geometries sirt_2d has
+    seen (weights W_sino = FP(1) and W_img = BP(1), device buffers, the
+    captured update graph): a call on a geometry seen before copies its
+    sinogram into the prepared state and replays the graph, as an FFT
+    library reuses a plan.  Each state has its own lock, so concurrent calls
+    on one geometry take turns; the states hold their device buffers until
+    evicted (at most ``cap``)."""
+
+    def __init__(self, cap=4):
+        self._d = collections.OrderedDict()
+        self._cap = cap
+        self._lock = threading.Lock()
+
+    def get(self, key, make):
+        with self._lock:
+            e = self._d.get(key)
+            if e is not None:
+                self._d.move_to_end(key)
+                return e
+        e = (threading.Lock(), make())
+        with self._lock:
+            self._d[key] = e
+            while len(self._d) > self._cap:
+                self._d.popitem(last=False)
+        return e
+
+    def clear(self):
+        with self._lock:
+            self._d.clear()
+
+
+prepared_sirt = _PreparedSirt()
+
+
 def sirt_2d(sino, ang_arr, img_shape, geom="par", DSO=0.0, DSD=0.0, du=1.0, su=0.0, d_pix=1.0,
             gamma=1.0, iters=100, W_sino=None, W_img=None, graph=True):
     """vir's SIRT (``iters - 1`` updates, x0 = 1e-5) on the parallel or fan
-    distance-driven pair.  numpy in -> numpy out."""
-    s = SIRT2D(sino, ang_arr, img_shape, geom=geom, DSO=DSO, DSD=DSD, du=du, su=su, d_pix=d_pix,
-               gamma=gamma, W_sino=W_sino, W_img=W_img)
-    x = s.run(int(iters) - 1, graph=graph)
-    return _core.to_host_like(x.clone(), sino)
+    distance-driven pair.  numpy in -> numpy out.  Without caller weights the
+    geometry's prepared state (weights, buffers, update graph) is reused
+    across calls (``prepared_sirt``)."""
+    if W_sino is not None or W_img is not None:
+        s = SIRT2D(sino, ang_arr, img_shape, geom=geom, DSO=DSO, DSD=DSD, du=du, su=su,
+                   d_pix=d_pix, gamma=gamma, W_sino=W_sino, W_img=W_img)
+        x = s.run(int(iters) - 1, graph=graph)
+        return _core.to_host_like(x.clone(), sino)
+    dev = _core.device_of(sino)
+    a = _core.host_angles(ang_arr)
+    f = _core.f32
+    key = (str(dev), a.dtype.str, a.shape, a.tobytes(), tuple(int(v) for v in np.shape(sino)),
+           tuple(int(v) for v in img_shape), geom, f(DSO), f(DSD), f(du), f(su), f(d_pix),
+           float(gamma))
+    lock, s = prepared_sirt.get(key, lambda: SIRT2D(sino, ang_arr, img_shape, geom=geom, DSO=DSO,
+                                                    DSD=DSD, du=du, su=su, d_pix=d_pix,
+                                                    gamma=gamma, device=dev))
+    with lock:
+        s.load_sino(sino)
+        s.reset()
+        x = s.run(int(iters) - 1, graph=graph).clone()
+    return _core.to_host_like(x, sino)
 
 
 def fan_preweight(nu, du, su, DSO, DSD):
