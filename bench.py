@@ -993,7 +993,11 @@ def main():
                                     "note": "unique inputs + outputs of the launch (image and "
                                             "sinogram); L2-resident, so not a DRAM bound"}},
         "e2e": {"value": e2e_val, "unit": "iter/s", "h2d_bytes_per_step": int(y.nbytes),
-                "d2h_bytes_per_step": int(img.nbytes)},
+                "d2h_bytes_per_step": int(img.nbytes),
+                "note": "reconstruction.sirt_2d on a pinned host sinogram: each step copies the "
+                        "sinogram in, runs all updates from x0 = 1e-5 and copies the image out; "
+                        "the geometry's weights FP(1), BP(1) and its update graph are prepared "
+                        "by the first call and reused (reconstruction.prepared_sirt)"},
         "gpu_launches": K * U * launches_per_update,      # library kernels per update (2 or 3)
         "clocks": clk.summary(),
     }
