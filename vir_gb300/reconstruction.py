@@ -245,8 +245,10 @@ class _PreparedSirt:
     captured update graph): a call on a geometry seen before copies its
     sinogram into the prepared state and replays the graph, as an FFT
     library reuses a plan.  Each state has its own lock, so concurrent calls
-    on one geometry take turns; the states hold their device buffers until
-    evicted (at most ``cap``)."""
+    on one geometry take turns on the host, and an event recorded after each
+    call's work, which the next caller's stream waits on, so that their GPU
+    work also runs in turn when they use different streams; the states hold
+    their device buffers until evicted (at most ``cap``)."""
 
     def __init__(self, cap=4):
         self._d = collections.OrderedDict()
@@ -259,7 +261,7 @@ class _PreparedSirt:
             if e is not None:
                 self._d.move_to_end(key)
                 return e
-        e = (threading.Lock(), make())
+        e = [threading.Lock(), make(), None]  # lock, state, event after the last call's work
         with self._lock:
             self._d[key] = e
             while len(self._d) > self._cap:
@@ -291,13 +293,19 @@ def sirt_2d(sino, ang_arr, img_shape, geom="par", DSO=0.0, DSD=0.0, du=1.0, su=0
     key = (str(dev), a.dtype.str, a.shape, a.tobytes(), tuple(int(v) for v in np.shape(sino)),
            tuple(int(v) for v in img_shape), geom, f(DSO), f(DSD), f(du), f(su), f(d_pix),
            float(gamma))
-    lock, s = prepared_sirt.get(key, lambda: SIRT2D(sino, ang_arr, img_shape, geom=geom, DSO=DSO,
-                                                    DSD=DSD, du=du, su=su, d_pix=d_pix,
-                                                    gamma=gamma, device=dev))
-    with lock:
+    e = prepared_sirt.get(key, lambda: SIRT2D(sino, ang_arr, img_shape, geom=geom, DSO=DSO,
+                                              DSD=DSD, du=du, su=su, d_pix=d_pix, gamma=gamma,
+                                              device=dev))
+    with e[0]:
+        s = e[1]
+        cur = torch.cuda.current_stream(s.dev)
+        if e[2] is not None:
+            cur.wait_event(e[2])  # the previous call's work on this state, on any stream
         s.load_sino(sino)
         s.reset()
         x = s.run(int(iters) - 1, graph=graph).clone()
+        e[2] = torch.cuda.Event()
+        e[2].record(cur)
     return _core.to_host_like(x, sino)
 
 
