@@ -398,3 +398,24 @@ def test_sirt_2d_reuses_prepared_state(vg):
     assert np.array_equal(a1, fresh(y1, 6)) and np.array_equal(a1b, a1)
     assert np.array_equal(np.asarray(a2), fresh(y2, 6))
     assert np.array_equal(a2c, fresh(y2, 9))
+
+
+def test_sirt_resumes_from_an_iterate(vg):
+    """x0 may be an iterate to resume from (the ``initial`` image of
+    processing/SIRT/sirt.py:15-29): 2 updates, then 3 more started from their
+    iterate, give bit for bit the iterate of 5 updates, on the fan pair and
+    on the cone pair."""
+    from vir_gb300 import reconstruction as rc
+    rng = np.random.default_rng(71)
+    angs = np.linspace(0, 2 * np.pi, 60, endpoint=False)
+    geo = dict(geom="fan", DSO=150.0, DSD=300.0, du=1.5, d_pix=1.0)
+    y = rng.random((60, 140)).astype(np.float32)
+    x5 = rc.sirt_2d(y, angs, (96, 96), iters=6, **geo)
+    x2 = rc.sirt_2d(y, angs, (96, 96), iters=3, **geo)
+    assert np.array_equal(rc.sirt_2d(y, angs, (96, 96), iters=4, x0=x2, **geo), x5)
+    a3 = np.linspace(0, 2 * np.pi, 24, endpoint=False)
+    y3 = rng.random((24, 24, 20)).astype(np.float32)
+    kw = dict(du=1.4, dv=1.4, d_pix=1.0)
+    v5 = rc.sirt_3d(y3, a3, (16, 16, 12), 40.0, 80.0, iters=6, **kw)
+    v2 = rc.sirt_3d(y3, a3, (16, 16, 12), 40.0, 80.0, iters=3, **kw)
+    assert np.array_equal(rc.sirt_3d(y3, a3, (16, 16, 12), 40.0, 80.0, iters=4, x0=v2, **kw), v5)

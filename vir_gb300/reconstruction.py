@@ -33,6 +33,18 @@ from ._lib import DD2DGeom, DD3DGeom, call, dd2d_workspace
 from .filtration import filter_rows_device
 
 
+def _initial(x0, shape, dev):
+    """vir's start value (a scalar, 1e-5) or an iterate to resume from (an
+    image of ``shape``, as ``initial`` of processing/SIRT/sirt.py:15-29):
+    (scalar or None, float32 device tensor or None)."""
+    if np.ndim(x0) == 0:
+        return float(np.float32(float(x0))), None
+    t = _core.to_device(x0, dev)
+    if tuple(t.shape) != tuple(shape):
+        raise ValueError(f"x0 has shape {tuple(t.shape)}, the image {tuple(shape)}")
+    return None, t
+
+
 def _geom(nx, ny, na, nu, du, su, d_pix, DSO, DSD, fan, variant=0):
     return DD2DGeom(int(nx), int(ny), int(na), int(nu), _core.f32(du), _core.f32(su),
                     _core.f32(d_pix), _core.f32(DSO), _core.f32(DSD), int(fan), int(variant))
@@ -76,8 +88,9 @@ class SIRT2D:
             W_img = _core.to_device(W_img, self.dev)
         self.inv_ws = torch.where(W_sino != 0, 1.0 / W_sino, torch.zeros_like(W_sino))
         self.inv_wi = torch.where(W_img != 0, 1.0 / W_img, torch.zeros_like(W_img))
-        self.x = torch.full((nx, ny), float(np.float32(x0)), dtype=torch.float32, device=self.dev)
-        self.xT = self.x.t().contiguous()
+        self.x = torch.empty((nx, ny), dtype=torch.float32, device=self.dev)
+        self.xT = torch.empty((ny, nx), dtype=torch.float32, device=self.dev)
+        self.reset(x0)
         self.r = torch.empty((na, nu), dtype=torch.float32, device=self.dev)
         self._graph = None
         self._graph_n = 0
@@ -143,8 +156,14 @@ class SIRT2D:
         return self.x
 
     def reset(self, x0=1e-5):
-        self.x.fill_(float(np.float32(x0)))
-        self.xT.fill_(float(np.float32(x0)))
+        """Restart from x0: a scalar (vir's 1e-5) or an (nx, ny) iterate to resume from."""
+        v, t = _initial(x0, self.x.shape, self.dev)
+        if t is None:
+            self.x.fill_(v)
+            self.xT.fill_(v)
+        else:
+            self.x.copy_(t)
+            self.xT.copy_(t.t())
 
 
 class SIRT3D:
@@ -178,7 +197,8 @@ class SIRT3D:
         self.inv_ws = torch.where(W_sino != 0, 1.0 / W_sino, torch.zeros_like(W_sino))
         self.inv_wi = torch.where(W_img != 0, 1.0 / W_img, torch.zeros_like(W_img))
         del W_sino, W_img
-        self.x = torch.full(shape, float(np.float32(x0)), dtype=torch.float32, device=self.dev)
+        self.x = torch.empty(shape, dtype=torch.float32, device=self.dev)
+        self.reset(x0)
         self.r = torch.empty_like(self.y)
         self._graph = None
         self._graph_n = 0
@@ -228,13 +248,19 @@ class SIRT3D:
         return self.x
 
     def reset(self, x0=1e-5):
-        self.x.fill_(float(np.float32(x0)))
+        """Restart from x0: a scalar (vir's 1e-5) or an (nx, ny, nz) iterate to resume from."""
+        v, t = _initial(x0, self.x.shape, self.dev)
+        if t is None:
+            self.x.fill_(v)
+        else:
+            self.x.copy_(t)
 
 
 def sirt_3d(sino, ang_arr, img_shape, DSO, DSD, du=1.0, dv=1.0, su=0.0, sv=0.0, d_pix=1.0,
-            gamma=1.0, iters=20, graph=True):
-    """vir's SIRT (``iters - 1`` updates, x0 = 1e-5) on the cone-beam DD pair."""
-    s = SIRT3D(sino, ang_arr, img_shape, DSO, DSD, du, dv, su, sv, d_pix, gamma)
+            gamma=1.0, iters=20, graph=True, x0=1e-5):
+    """vir's SIRT (``iters - 1`` updates, x0 = 1e-5) on the cone-beam DD pair;
+    ``x0`` may be an iterate to resume from."""
+    s = SIRT3D(sino, ang_arr, img_shape, DSO, DSD, du, dv, su, sv, d_pix, gamma, x0=x0)
     x = s.run(int(iters) - 1, graph=graph)
     return _core.to_host_like(x.clone(), sino)
 
@@ -277,14 +303,15 @@ prepared_sirt = _PreparedSirt()
 
 
 def sirt_2d(sino, ang_arr, img_shape, geom="par", DSO=0.0, DSD=0.0, du=1.0, su=0.0, d_pix=1.0,
-            gamma=1.0, iters=100, W_sino=None, W_img=None, graph=True):
+            gamma=1.0, iters=100, W_sino=None, W_img=None, graph=True, x0=1e-5):
     """vir's SIRT (``iters - 1`` updates, x0 = 1e-5) on the parallel or fan
-    distance-driven pair.  numpy in -> numpy out.  Without caller weights the
-    geometry's prepared state (weights, buffers, update graph) is reused
-    across calls (``prepared_sirt``)."""
+    distance-driven pair.  numpy in -> numpy out.  ``x0`` may be an iterate
+    to resume from (``initial`` of processing/SIRT/sirt.py).  Without caller
+    weights the geometry's prepared state (weights, buffers, update graph) is
+    reused across calls (``prepared_sirt``)."""
     if W_sino is not None or W_img is not None:
         s = SIRT2D(sino, ang_arr, img_shape, geom=geom, DSO=DSO, DSD=DSD, du=du, su=su,
-                   d_pix=d_pix, gamma=gamma, W_sino=W_sino, W_img=W_img)
+                   d_pix=d_pix, gamma=gamma, x0=x0, W_sino=W_sino, W_img=W_img)
         x = s.run(int(iters) - 1, graph=graph)
         return _core.to_host_like(x.clone(), sino)
     dev = _core.device_of(sino)
@@ -302,7 +329,7 @@ def sirt_2d(sino, ang_arr, img_shape, geom="par", DSO=0.0, DSD=0.0, du=1.0, su=0
         if e[2] is not None:
             cur.wait_event(e[2])  # the previous call's work on this state, on any stream
         s.load_sino(sino)
-        s.reset()
+        s.reset(x0)
         x = s.run(int(iters) - 1, graph=graph).clone()
         e[2] = torch.cuda.Event()
         e[2].record(cur)
