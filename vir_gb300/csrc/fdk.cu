@@ -2,7 +2,7 @@
 // geometry of dd_fp_cone_3d: cosine pre-weight, row ramp filter along u,
 // distance-weighted voxel-driven backprojection.
 //
-// vir has no FDK (SURVEY: absent); the weights extend its fan-beam spec to
+// vir has no FDK; the weights extend its fan-beam specification to
 // the cone: the equispaced pre-weight of processing/reconstruction.py:99-107
 // becomes DSD / sqrt(DSD^2 + u^2 + v^2) on the flat detector, the filter is
 // filtration.filter_sino's 2H at the isocentre pitch du DSO / DSD, and the
